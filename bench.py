@@ -1,0 +1,292 @@
+#!/usr/bin/env python3
+"""Throughput of the full-rank plume step (the reference's `fluid3D` stage).
+
+Workload: the 128x192x128 plume -- closed box, box source with +-0.05 seeded
+noise, buoyancy 1, vorticity 2 -- with FP32 fields and FP64 CG scalars, MIC(0)
+PCG to a relative residual of 1e-6.  A "step" is one FLUID_3D_MIC::step
+(source, buoyancy, vorticity confinement, advection, damping, projection).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is steps/s from CUDA events on the library's
+stream around the K timed steps (state resident in HBM); `e2e` is steps/s
+through the public API with the source values copied from pinned host memory
+and the velocity snapshot (FP64, reference layout) copied back every step.
+N > 1 runs N independent replicas (one per GPU, launched by torchrun); the
+path has no data exchange between plumes.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "steps/s, PCG iters/step @128x192x128: learned/FP32 vs plain MIC-PCG, res 1e-6"
+RES = (128, 192, 128)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-over-ranks for N replicas (gloo over 127.0.0.1)."""
+
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v):
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+def bytes_per_step(nint, iters, S, P):
+    """Algorithmic HBM bytes of one step: each pass reads its operands once and
+    writes its results once; 1 byte of cell flags per stencil pass."""
+    return nint * (51 * S + 3 * P + 6 + iters * (16 * S + 2 * P + 3))
+
+
+def bytes_per_iteration(nint, S, P):
+    return nint * (16 * S + 2 * P + 3)
+
+
+def cpu_baseline(res, steps):
+    """The oracle (FP64 CPU restatement of the reference step, 1 thread) on the
+    first `steps` steps of the same plume: steps/s."""
+    from cfs_plume_gb300 import _abi
+    from oracle import oracle
+    p = _abi.plume_config(res, precision=_abi.PREC_FP64)
+    o = oracle.Oracle(p)
+    t0 = time.perf_counter()
+    iters = []
+    for s in range(steps):
+        o.add_source(s)
+        iters.append(o.step().iterations)
+    dt = time.perf_counter() - t0
+    return steps / dt, iters, dt
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference step's CPU implementation, timed on the
+    host.  The reference sources are not present on the GPU host, so the
+    oracle port (a line-by-line restatement pinned bit-for-bit to the
+    reference) stands in; the reference step is single-threaded."""
+    if rank != 0:
+        return 0
+    res = RES
+    sample = max(1, min(args.steps, 3))
+    v, iters, dt = cpu_baseline(res, sample)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": world,
+        "steps": sample, "warmup": 0, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "plume 128x192x128, closed box, box source +-0.05 seeded noise, "
+                               "buoyancy 1, vorticity 2, MIC(0)-PCG rel-residual 1e-6",
+                   "res": list(res)},
+        "pcg_iters_per_step": statistics.mean(iters),
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
+                         "sample": "first %d steps from rest of the same plume (%.1f s)" % (sample, dt)},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--res", default=None, help="X,Y,Z (default 128,192,128)")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--cpu-steps", type=int, default=1, help="oracle steps for cpu_baseline (0: skip)")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    a = ap.parse_args()
+    rank, world, local = dist_env()
+    if a.impl == "reference":
+        return run_reference(a, rank, world)
+    a.warmup = max(a.warmup, 3)
+
+    from cfs_plume_gb300 import _abi
+    from cfs_plume_gb300.plume import Plume
+    import numpy as np
+
+    res = tuple(int(v) for v in a.res.split(",")) if a.res else RES
+    prec = _abi.PREC_FP32 if a.precision == "fp32" else _abi.PREC_FP64
+    S = 4 if prec == _abi.PREC_FP32 else 8
+    P = S
+    dist = Dist(world)
+    p = _abi.plume_config(res, precision=prec, seed=rank, device=local)
+    g = Plume(p)
+    nint = (res[0] - 2) * (res[1] - 2) * (res[2] - 2)
+
+    # warm-up (not timed)
+    g.run_timed(0, a.warmup)
+    clocks = ClockSampler(local)
+    dist.barrier()
+    g.lib.plume_sync(g.h)
+    clocks.start()
+    ms, stats = g.run_timed(a.warmup, a.steps)
+    clk = clocks.stop()
+    dist.barrier()
+    ms_max = dist.max(ms)
+    iters = [s.iterations for s in stats]
+    launches = sum(s.launches for s in stats)
+    ms_solve = sum(s.ms_solve for s in stats)
+    steps_total = dist.sum(a.steps)
+    value = steps_total / (ms_max / 1000.0)
+
+    # end to end through the public API with host buffers
+    n_e2e = a.e2e_steps if a.e2e_steps is not None else max(3, min(a.steps, 10))
+    lo, hi = p.box_lo, p.box_hi
+    nbox = (hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2])
+    rng = np.random.default_rng(rank)
+    src = [1.0 + 0.05 * (2.0 * rng.random(nbox) - 1.0) for _ in range(n_e2e)]
+    vel = np.empty(3 * g.N)
+    dist.barrier()
+    t0 = time.perf_counter()
+    base = a.warmup + a.steps
+    for k in range(n_e2e):
+        g.add_source_values(src[k])
+        g.step(stats=False)
+        g.lib.plume_download(g.h, _abi.FIELD_ID["velocity"], vel.ctypes.data, vel.size)
+    e2e_s = time.perf_counter() - t0
+    dist.barrier()
+    e2e_s = dist.max(e2e_s)
+    e2e = dist.sum(n_e2e) / e2e_s
+
+    peak, peak_kind = measured_peaks()
+    mean_iters = statistics.mean(iters)
+    step_bytes = bytes_per_step(nint, mean_iters, S, P)
+    solve_bytes = sum(nint * (5 * S + 2 * P + 2) + it * bytes_per_iteration(nint, S, P) for it in iters)
+    achieved_solve = solve_bytes / (ms_solve / 1000.0) / 1e9 if ms_solve > 0 else None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if S == 4 else "f64",
+        "data": "synthetic",
+        "config": {"workload": "plume %dx%dx%d, closed box, box source +-0.05 seeded noise, "
+                               "buoyancy 1, vorticity 2, MIC(0)-PCG rel-residual 1e-6" % res,
+                   "res": list(res), "solver": "plain MIC(0)-PCG (learned start not in this build)",
+                   "precision": "FP32 fields, FP64 CG scalars/MIC diagonal" if S == 4 else "FP64",
+                   "l2": "step working set %.0f MB > 129 MB L2 (no flush needed)" %
+                         (37 * S * g.N / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "pcg_iters_per_step": mean_iters,
+        "achieved_gbs_step": step_bytes / (ms_max / a.steps / 1000.0) / 1e9,
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "poisson solve (MIC-PCG)",
+                     "achieved": achieved_solve, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved_solve / peak) if achieved_solve else None,
+                     "peak_kind": peak_kind, "traffic": None,
+                     "bytes_model": "N_int*(5S+2P+2 + iters*(16S+2P+3)) per solve"},
+        "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": nbox * 8,
+                "d2h_bytes_per_step": 3 * g.N * 8},
+        "clocks": clk,
+    }
+    if rank == 0 and a.cpu_steps > 0:
+        v, it_cpu, dt = cpu_baseline(res, a.cpu_steps)
+        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
+                                "sample": "first %d step(s) from rest of the same plume, FP64 "
+                                          "oracle (%.1f s, %s PCG iterations)" % (a.cpu_steps, dt, it_cpu)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,116 @@
+// common.cuh -- device-side helpers shared by the plume kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace plume {
+
+#define PL_GRID_STRIDE(i, n) \
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += blockDim.x * gridDim.x)
+
+// Grid geometry.  Index = x + y*X + z*X*Y (x fastest), the reference layout
+// (src/geometry/FIELD_3D.h:54-57).  `wall` holds the six BC flags in the
+// reference order front(z=0), back(z=Z-1), left(x=0), right(x=X-1),
+// top(y=Y-1), bottom(y=0); 1 = obstacle slab (FLUID_3D_MIC.cpp:105-159).
+struct Grid {
+  int X, Y, Z;
+  int slab;        // X*Y
+  int N;           // X*Y*Z
+  int nx, ny, nz;  // interior extents (X-2, Y-2, Z-2)
+  int nint;        // nx*ny*nz
+  int wall[6];
+};
+
+__host__ __device__ inline bool on_border(const Grid& g, int x, int y, int z) {
+  return x == 0 || y == 0 || z == 0 || x == g.X - 1 || y == g.Y - 1 || z == g.Z - 1;
+}
+
+// Full-grid index of interior cell number i (interior cells enumerated x fastest).
+__device__ inline int interior_cell(const Grid& g, int i, int& x, int& y, int& z) {
+  const int t = i / g.nx;
+  x = 1 + (i - t * g.nx);
+  y = 1 + (t % g.ny);
+  z = 1 + t / g.ny;
+  return x + y * g.X + z * g.slab;
+}
+
+// Is the face neighbour of an interior cell an obstacle?  Only the wall slabs
+// are obstacles, so the neighbour across a face is a wall exactly when the
+// cell touches that face and the face's flag is set.
+__device__ inline bool wall_xm(const Grid& g, int x) { return x == 1 && g.wall[2] == 1; }
+__device__ inline bool wall_xp(const Grid& g, int x) { return x == g.X - 2 && g.wall[3] == 1; }
+__device__ inline bool wall_ym(const Grid& g, int y) { return y == 1 && g.wall[5] == 1; }
+__device__ inline bool wall_yp(const Grid& g, int y) { return y == g.Y - 2 && g.wall[4] == 1; }
+__device__ inline bool wall_zm(const Grid& g, int z) { return z == 1 && g.wall[0] == 1; }
+__device__ inline bool wall_zp(const Grid& g, int z) { return z == g.Z - 2 && g.wall[1] == 1; }
+
+// Deterministic block reduction (fixed shuffle tree, fixed smem order).
+template <typename A>
+__device__ inline A warp_sum(A v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+template <typename A>
+__device__ inline A warp_max(A v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    A w = __shfl_down_sync(0xffffffffu, v, o);
+    v = (w > v) ? w : v;
+  }
+  return v;
+}
+
+// Sum over the block; result valid in thread 0.  `sh` needs blockDim/32 slots.
+template <typename A>
+__device__ inline A block_sum(A v, A* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  A r = 0;
+  if (wid == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : A(0);
+    r = warp_sum(r);
+  }
+  return r;
+}
+template <typename A>
+__device__ inline A block_max(A v, A* sh, A ident) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  A r = ident;
+  if (wid == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : ident;
+    r = warp_max(r);
+  }
+  return r;
+}
+
+// SplitMix64 finaliser; identical integer recipe on host (oracle) and device.
+__host__ __device__ inline uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Seeded plume source value 1 + noise*(2u - 1), u in [0,1) from (seed, step, cell).
+__host__ __device__ inline double source_value(uint64_t seed, int32_t step, int64_t cell,
+                                               double noise) {
+  uint64_t h = mix64(seed + 0x9E3779B97F4A7C15ull);
+  h = mix64(h + (uint64_t)(uint32_t)step * 0xD1B54A32D192ED03ull);
+  h = mix64(h + (uint64_t)cell);
+  const double u = (double)(h >> 11) * (1.0 / 9007199254740992.0);
+#ifdef __CUDA_ARCH__
+  // explicit rounding: no multiply-add contraction, same bits as the host
+  return __dadd_rn(1.0, __dmul_rn(noise, __dadd_rn(__dmul_rn(2.0, u), -1.0)));
+#else
+  return 1.0 + noise * (2.0 * u - 1.0);
+#endif
+}
+
+}  // namespace plume

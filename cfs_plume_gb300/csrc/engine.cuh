@@ -1,0 +1,595 @@
+// engine.cuh -- Engine<T>: device state and step orchestration for one plume.
+//
+// Included by engine_f64.cu (T = double, no multiply-add contraction) and
+// engine_f32.cu (T = float).  The step follows FLUID_3D_MIC::step
+// (FLUID_3D_MIC.cpp:179-223) stage for stage; the cached copies the reference
+// keeps for the reduced solvers are produced as extra kernel outputs or by
+// pointer rotation instead of separate full-array copies.
+#pragma once
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "common.cuh"
+#include "engine.h"
+#include "solver_kernels.cuh"
+#include "step_kernels.cuh"
+
+namespace plume {
+
+#define PL_TRY(expr)                                                          \
+  do {                                                                        \
+    cudaError_t e_ = (expr);                                                  \
+    if (e_ != cudaSuccess) return fail_cuda(e_, #expr, __FILE__, __LINE__);   \
+  } while (0)
+#define PL_CHECK_LAUNCH() \
+  do {                    \
+    ++launches_;          \
+    PL_TRY(cudaGetLastError()); \
+  } while (0)
+
+inline int grid_for(long long n, int threads = 256, int cap = 152 * 32) {
+  long long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return (int)b;
+}
+
+// Column source cells of FLUID_3D_MIC::addSmokeTestCase (FLUID_3D_MIC.cpp:
+// 674-700), evaluated with the reference's float sqrtf and float literals.
+inline std::vector<int> column_cells(int X, int Y, int Z) {
+  std::vector<int> cells;
+  int maxRes = X;
+  if (Y > maxRes) maxRes = Y;
+  if (Z > maxRes) maxRes = Z;
+  const double dx = 1.0f / (double)maxRes;
+  const double xTotal = dx * X, zTotal = dx * Z;
+  const double heighMin = 0.05, heighMax = 0.10;
+  for (int z = 0; z < Z; z++)
+    for (int y = (int)(heighMin * Y); y <= (int)(heighMax * Y); y++)
+      for (int x = 0; x < X; x++) {
+        const double xLength = x * dx - xTotal * 0.4f;
+        const double zLength = z * dx - zTotal * 0.5f;
+        const double radius = sqrtf((float)(xLength * xLength + zLength * zLength));
+        if (radius < 0.075f * xTotal) cells.push_back(x + y * X + z * X * Y);
+      }
+  return cells;
+}
+
+template <typename T>
+class EngineT : public Engine {
+ public:
+  EngineT() {}
+  ~EngineT() override { release(); }
+
+  // ------------------------------------------------------------------ init
+  int init(const plume_params& p) override {
+    p_ = p;
+    for (int k = 0; k < 3; k++)
+      if (p.res[k] < 4) return fail(PLUME_ERR_INVALID, "every grid dimension must be >= 4");
+    const long long N = (long long)p.res[0] * p.res[1] * p.res[2];
+    if (N > (1ll << 30)) return fail(PLUME_ERR_INVALID, "grid larger than 2^30 cells");
+    for (int k = 0; k < 6; k++)
+      if (p.bc[k] != 0 && p.bc[k] != 1) return fail(PLUME_ERR_INVALID, "bc flags must be 0 or 1");
+    if (p.criterion != PLUME_CRIT_REFERENCE && p.criterion != PLUME_CRIT_REL2)
+      return fail(PLUME_ERR_INVALID, "unknown criterion");
+    if (p.source == PLUME_SRC_BOX)
+      for (int k = 0; k < 3; k++)
+        if (p.box_lo[k] < 0 || p.box_hi[k] > p.res[k] || p.box_lo[k] > p.box_hi[k])
+          return fail(PLUME_ERR_INVALID, "source box outside the grid");
+    if (p.warm_start == PLUME_WARM_LEARNED)
+      return fail(PLUME_ERR_UNSUPPORTED, "learned warm start is not available in this engine");
+    g_.X = p.res[0];
+    g_.Y = p.res[1];
+    g_.Z = p.res[2];
+    g_.slab = g_.X * g_.Y;
+    g_.N = (int)N;
+    g_.nx = g_.X - 2;
+    g_.ny = g_.Y - 2;
+    g_.nz = g_.Z - 2;
+    g_.nint = g_.nx * g_.ny * g_.nz;
+    for (int k = 0; k < 6; k++) g_.wall[k] = p.bc[k];
+    int maxRes = g_.X > g_.Y ? g_.X : g_.Y;
+    maxRes = g_.Z > maxRes ? g_.Z : maxRes;
+    dx_ = 1.0f / (double)maxRes;  // FLUID_3D_MIC.cpp:46
+    set_consts();
+
+    PL_TRY(cudaSetDevice(p.device));
+    PL_TRY(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
+    for (auto* e : {&ev_[0], &ev_[1], &ev_[2], &ev_[3]}) PL_TRY(cudaEventCreate(e));
+
+    // one pool: 13 scalar planes + 8 vector fields (24 planes) of T, the FP64
+    // MIC diagonal, the obstacle bytes, solver state and reduction partials.
+    const size_t n = (size_t)g_.N;
+    const size_t aT = align(n * sizeof(T));
+    const size_t bytes = 37 * aT + align(n * sizeof(double)) + align(n) +
+                         align(sizeof(CgState)) + align(2 * kRedBlocks * sizeof(double));
+    cudaError_t e = cudaMalloc(&pool_, bytes);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return fail(PLUME_ERR_OOM, "device allocation of the field pool failed");
+    }
+    PL_TRY(cudaMemsetAsync(pool_, 0, bytes, s_));
+    char* cur = pool_;
+    auto take = [&](size_t b) { char* r = cur; cur += align(b); return r; };
+    T** scal[] = {&dens_, &dens_old_, &heat_, &heat_old_, &pres_, &div_, &mag_,
+                  &r_,    &d_,        &q_ad_, &z_,        &qf_, &P_};
+    for (T** s : scal) *s = (T*)take(n * sizeof(T));
+    V3<T>* vecs[] = {&vel_, &vel_old_, &spare_, &prevort_, &postadv_, &preproj_, &force_, &vort_};
+    for (V3<T>* v : vecs) {
+      v->x = (T*)take(n * sizeof(T));
+      v->y = (T*)take(n * sizeof(T));
+      v->z = (T*)take(n * sizeof(T));
+    }
+    P64_ = (double*)take(n * sizeof(double));
+    obst_ = (uint8_t*)take(n);
+    st_ = (CgState*)take(sizeof(CgState));
+    part_ = (double*)take(2 * kRedBlocks * sizeof(double));
+
+    // obstacle slabs (FLUID_3D_MIC.cpp:105-159), kept for download and the
+    // state file; kernels derive walls from the flags.
+    std::vector<uint8_t> ob(n, 0);
+    for (int z = 0; z < g_.Z; z++)
+      for (int y = 0; y < g_.Y; y++)
+        for (int x = 0; x < g_.X; x++) {
+          const bool w = (z == 0 && p.bc[0] == 1) || (z == g_.Z - 1 && p.bc[1] == 1) ||
+                         (y == 0 && p.bc[5] == 1) || (y == g_.Y - 1 && p.bc[4] == 1) ||
+                         (x == 0 && p.bc[2] == 1) || (x == g_.X - 1 && p.bc[3] == 1);
+          ob[x + y * g_.X + z * g_.slab] = w ? 1 : 0;
+        }
+    PL_TRY(cudaMemcpyAsync(obst_, ob.data(), n, cudaMemcpyHostToDevice, s_));
+
+    if (p.source == PLUME_SRC_COLUMN) {
+      std::vector<int> cells = column_cells(g_.X, g_.Y, g_.Z);
+      n_col_ = (int)cells.size();
+      if (n_col_ > 0) {
+        PL_TRY(cudaMalloc(&col_cells_, cells.size() * sizeof(int)));
+        PL_TRY(cudaMemcpyAsync(col_cells_, cells.data(), cells.size() * sizeof(int),
+                               cudaMemcpyHostToDevice, s_));
+      }
+    }
+    PL_TRY(cudaMallocHost(&st_host_, sizeof(CgState)));
+    PL_TRY(cudaMallocHost(&stage_, n * 3 * sizeof(double)));
+
+    // MIC(0) diagonal, built once: the reference rebuilds an identical one at
+    // every solve (FLUID_3D_MIC.cpp:921-922) since the walls never change.
+    PL_TRY(build_mic_diagonal(g_, P64_, p.mic_tau, p.mic_sigma, s_));
+    k_convert_precon<T><<<grid_for(g_.N), 256, 0, s_>>>(g_.N, P64_, P_);
+    PL_CHECK_LAUNCH();
+    PL_TRY(cudaStreamSynchronize(s_));
+    return PLUME_OK;
+  }
+
+  // --------------------------------------------------------------- sources
+  int add_source(int32_t step_index) override {
+    if (p_.source == PLUME_SRC_COLUMN && n_col_ > 0) {
+      k_source_list<T><<<grid_for(n_col_), 256, 0, s_>>>(dens_, heat_, col_cells_, n_col_);
+      PL_CHECK_LAUNCH();
+    } else if (p_.source == PLUME_SRC_BOX) {
+      const int bx = p_.box_hi[0] - p_.box_lo[0], by = p_.box_hi[1] - p_.box_lo[1],
+                bz = p_.box_hi[2] - p_.box_lo[2];
+      if (bx > 0 && by > 0 && bz > 0) {
+        k_source_box<T><<<grid_for((long long)bx * by * bz), 256, 0, s_>>>(
+            dens_, heat_, g_, p_.box_lo[0], p_.box_lo[1], p_.box_lo[2], bx, by, bz, p_.seed,
+            step_index, p_.source_noise);
+        PL_CHECK_LAUNCH();
+      }
+    }
+    return PLUME_OK;
+  }
+
+  int add_source_values(const double* values, size_t n) override {
+    if (p_.source != PLUME_SRC_BOX) return fail(PLUME_ERR_STATE, "source values need a box source");
+    const int bx = p_.box_hi[0] - p_.box_lo[0], by = p_.box_hi[1] - p_.box_lo[1],
+              bz = p_.box_hi[2] - p_.box_lo[2];
+    const size_t nb = (size_t)bx * by * bz;
+    if (!values || n != nb) return fail(PLUME_ERR_INVALID, "values must cover the source box");
+    if (nb == 0) return PLUME_OK;
+    if (src_dev_ == nullptr) {
+      PL_TRY(cudaMalloc(&src_dev_, nb * sizeof(T)));
+      PL_TRY(cudaMallocHost(&src_host_, nb * sizeof(T)));
+    }
+    PL_TRY(cudaStreamSynchronize(s_));  // src_host_ may still feed a previous copy
+    for (size_t k = 0; k < nb; k++) src_host_[k] = (T)values[k];
+    PL_TRY(cudaMemcpyAsync(src_dev_, src_host_, nb * sizeof(T), cudaMemcpyHostToDevice, s_));
+    k_source_box_values<T><<<grid_for((long long)nb), 256, 0, s_>>>(
+        dens_, heat_, g_, p_.box_lo[0], p_.box_lo[1], p_.box_lo[2], bx, by, bz, src_dev_);
+    PL_CHECK_LAUNCH();
+    return PLUME_OK;
+  }
+
+  int run_timed(int32_t first_step, int32_t n, double* ms, plume_step_stats* stats) override {
+    cudaEvent_t a, b;
+    PL_TRY(cudaEventCreate(&a));
+    PL_TRY(cudaEventCreate(&b));
+    PL_TRY(cudaEventRecord(a, s_));
+    int rc = run(first_step, n, stats);
+    if (rc == PLUME_OK) {
+      PL_TRY(cudaEventRecord(b, s_));
+      PL_TRY(cudaEventSynchronize(b));
+      float f = 0.f;
+      PL_TRY(cudaEventElapsedTime(&f, a, b));
+      *ms = f;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return rc;
+  }
+
+  // ------------------------------------------------------------------ step
+  int step(plume_step_stats* stats) override {
+    const int cache = p_.cache_fields ? 1 : 0;
+    const int gN = grid_for(g_.N);
+    const int gI = grid_for(g_.nint);
+    const int nfaces = 2 * (g_.Y * g_.Z + g_.X * g_.Z + g_.X * g_.Y);
+    const int gF = grid_for(nfaces);
+    launches_ = 0;
+    PL_TRY(cudaEventRecord(ev_[0], s_));
+    // forces: walls, buoyancy, prevorticity (FLUID_3D_MIC.cpp:188-199)
+    k_forces<T><<<gN, 256, 0, s_>>>(g_, vel_, dens_, heat_, prevort_, c_, cache);
+    PL_CHECK_LAUNCH();
+    if (c_.has_vort) {  // addVorticity returns early when eps <= 0 (line 527)
+      k_vort1<T><<<gN, 256, 0, s_>>>(g_, vel_, vort_, mag_, c_);
+      PL_CHECK_LAUNCH();
+      k_vort2<T><<<gN, 256, 0, s_>>>(g_, vel_, vort_, mag_, force_, c_, cache);
+      PL_CHECK_LAUNCH();
+    }
+    // advectStam (lines 595-650): boundary copy, swap, advect + fix-up
+    const int ox = p_.bc[2] == 0, oy = p_.bc[4] == 0, oz = p_.bc[0] == 0;
+    k_face_bc<T><<<gF, 256, 0, s_>>>(g_, vel_, ox ? 1 : 0, oy ? 1 : 0, oz ? 1 : 0);
+    PL_CHECK_LAUNCH();
+    std::swap(vel_, vel_old_);
+    std::swap(dens_, dens_old_);
+    std::swap(heat_, heat_old_);
+    k_advect<T><<<gN, 256, 0, s_>>>(g_, c_, vel_old_, dens_old_, heat_old_, vel_, dens_, heat_,
+                                    postadv_, cache, ox, oy, oz);
+    PL_CHECK_LAUNCH();
+    // damping (lines 209-212); the input buffer becomes `prediffusion`
+    k_damping<T><<<gN, 256, 0, s_>>>(g_, c_, vel_, spare_, preproj_, cache);
+    PL_CHECK_LAUNCH();
+    std::swap(vel_, spare_);
+    // project (lines 314-399)
+    k_face_bc<T><<<gF, 256, 0, s_>>>(g_, vel_, ox ? 2 : 0, oy ? 2 : 0, oz ? 2 : 0);
+    PL_CHECK_LAUNCH();
+    const int keep_p = (p_.warm_start == PLUME_WARM_PREVIOUS) ? 1 : 0;
+    k_divergence<T><<<gI, 256, 0, s_>>>(g_, c_, vel_, div_, pres_, keep_p);
+    PL_CHECK_LAUNCH();
+    k_copy_border_all<T><<<gF, 256, 0, s_>>>(g_, pres_);
+    PL_CHECK_LAUNCH();
+    PL_TRY(cudaEventRecord(ev_[1], s_));
+    int rc = solve_device(div_, pres_);
+    if (rc != PLUME_OK) return rc;
+    PL_TRY(cudaEventRecord(ev_[2], s_));
+    k_gradient<T><<<gI, 256, 0, s_>>>(g_, c_, vel_, pres_);
+    PL_CHECK_LAUNCH();
+    PL_TRY(cudaEventRecord(ev_[3], s_));
+    total_time_ += 0.1;  // FLUID_3D_MIC.cpp:221 (goalTime)
+    total_steps_ += 1;
+    if (stats) return fill_stats(stats);
+    return PLUME_OK;
+  }
+
+  int run(int32_t first_step, int32_t n, plume_step_stats* stats) override {
+    for (int k = 0; k < n; k++) {
+      int rc = add_source(first_step + k);
+      if (rc == PLUME_OK) rc = step(stats ? stats + k : nullptr);
+      if (rc != PLUME_OK) return rc;
+    }
+    return PLUME_OK;
+  }
+
+  // ------------------------------------------------------------- transfer
+  int download(int field, double* dst, size_t n) override {
+    const size_t N = (size_t)g_.N;
+    if (!dst) return fail(PLUME_ERR_INVALID, "null destination");
+    const bool cached = (field == PLUME_F_PREVORTICITY || field == PLUME_F_POSTADVECTION ||
+                         field == PLUME_F_PREPROJECTION || field == PLUME_F_CACHED_QUADRATIC ||
+                         field == PLUME_F_FORCE);
+    if (cached && !p_.cache_fields)
+      return fail(PLUME_ERR_STATE, "field is not kept when cache_fields = 0");
+    const T* s = scalar_ptr(field);
+    if (s) {
+      if (n != N) return fail(PLUME_ERR_INVALID, "scalar field needs N doubles");
+      return fetch_plane(s, dst, 1, 0);
+    }
+    V3<T> v;
+    if (field == PLUME_F_CACHED_QUADRATIC) {
+      if (n != 3 * N) return fail(PLUME_ERR_INVALID, "vector field needs 3N doubles");
+      // _cachedQuadratic = velocity - velocityOld right after advection
+      // (FLUID_3D_MIC.cpp:627) = postadvection - velocityOld.
+      std::vector<double> a(3 * N), b(3 * N);
+      int rc = fetch_vec(postadv_, a.data());
+      if (rc == PLUME_OK) rc = fetch_vec(vel_old_, b.data());
+      if (rc != PLUME_OK) return rc;
+      if (std::is_same<T, float>::value) {
+        for (size_t k = 0; k < 3 * N; k++) dst[k] = (double)((float)a[k] - (float)b[k]);
+      } else {
+        for (size_t k = 0; k < 3 * N; k++) dst[k] = a[k] - b[k];
+      }
+      return PLUME_OK;
+    }
+    if (!vector_ref(field, v)) return fail(PLUME_ERR_INVALID, "unknown field");
+    if (n != 3 * N) return fail(PLUME_ERR_INVALID, "vector field needs 3N doubles");
+    return fetch_vec(v, dst);
+  }
+
+  int upload(int field, const double* src, size_t n) override {
+    const size_t N = (size_t)g_.N;
+    if (!src) return fail(PLUME_ERR_INVALID, "null source");
+    T* s = nullptr;
+    switch (field) {
+      case PLUME_F_DENSITY: s = dens_; break;
+      case PLUME_F_DENSITY_OLD: s = dens_old_; break;
+      case PLUME_F_HEAT: s = heat_; break;
+      case PLUME_F_HEAT_OLD: s = heat_old_; break;
+      case PLUME_F_PRESSURE: s = pres_; break;
+      default: break;
+    }
+    if (s) {
+      if (n != N) return fail(PLUME_ERR_INVALID, "scalar field needs N doubles");
+      return put_plane(s, src, 1, 0);
+    }
+    V3<T> v;
+    switch (field) {
+      case PLUME_F_VELOCITY: v = vel_; break;
+      case PLUME_F_VELOCITY_OLD: v = vel_old_; break;
+      case PLUME_F_VORTICITY: v = vort_; break;
+      default: return fail(PLUME_ERR_UNSUPPORTED, "field is derived and cannot be uploaded");
+    }
+    if (n != 3 * N) return fail(PLUME_ERR_INVALID, "vector field needs 3N doubles");
+    int rc = put_plane(v.x, src, 3, 0);
+    if (rc == PLUME_OK) rc = put_plane(v.y, src, 3, 1);
+    if (rc == PLUME_OK) rc = put_plane(v.z, src, 3, 2);
+    return rc;
+  }
+
+  int download_obstacles(uint8_t* dst, size_t n) override {
+    if (!dst || n != (size_t)g_.N) return fail(PLUME_ERR_INVALID, "obstacles need N bytes");
+    PL_TRY(cudaMemcpyAsync(dst, obst_, n, cudaMemcpyDeviceToHost, s_));
+    PL_TRY(cudaStreamSynchronize(s_));
+    return PLUME_OK;
+  }
+
+  // -------------------------------------------------------- solver access
+  int solve(const double* b, double* x, plume_step_stats* stats) override {
+    if (!b || !x) return fail(PLUME_ERR_INVALID, "null buffer");
+    // uses the divergence/pressure planes as right-hand side and unknown
+    int rc = put_plane(div_, b, 1, 0);
+    if (rc == PLUME_OK) rc = put_plane(pres_, x, 1, 0);
+    if (rc != PLUME_OK) return rc;
+    PL_TRY(cudaEventRecord(ev_[1], s_));
+    rc = solve_device(div_, pres_);
+    if (rc != PLUME_OK) return rc;
+    PL_TRY(cudaEventRecord(ev_[2], s_));
+    PL_TRY(cudaEventRecord(ev_[0], s_));
+    PL_TRY(cudaEventRecord(ev_[3], s_));
+    rc = fetch_plane(pres_, x, 1, 0);
+    if (rc == PLUME_OK && stats) rc = fill_stats(stats);
+    return rc;
+  }
+
+  int mic_apply(const double* r, double* z, double* q) override {
+    int rc = put_plane(r_, r, 1, 0);
+    if (rc != PLUME_OK) return rc;
+    rc = mic_sweeps(r_, qf_, z_, nullptr);
+    if (rc == PLUME_OK) rc = fetch_plane(z_, z, 1, 0);
+    if (rc == PLUME_OK && q) rc = fetch_plane(qf_, q, 1, 0);
+    return rc;
+  }
+
+  int mic_precon(double* precon) override {
+    PL_TRY(cudaMemcpyAsync(stage_, P64_, (size_t)g_.N * sizeof(double), cudaMemcpyDeviceToHost,
+                           s_));
+    PL_TRY(cudaStreamSynchronize(s_));
+    memcpy(precon, stage_, (size_t)g_.N * sizeof(double));
+    return PLUME_OK;
+  }
+
+  int sync() override {
+    PL_TRY(cudaStreamSynchronize(s_));
+    return PLUME_OK;
+  }
+  int32_t total_steps() const override { return total_steps_; }
+  double total_time() const override { return total_time_; }
+  double dx() const override { return dx_; }
+  const plume_params& params() const override { return p_; }
+  std::string& last_error() override { return err_; }
+
+ private:
+  static size_t align(size_t b) { return (b + 255) & ~(size_t)255; }
+
+  void set_consts() {
+    const double dt = p_.dt, dx = dx_;
+    c_.dt = (T)dt;
+    c_.beta = (T)p_.buoyancy;
+    c_.eps = (T)p_.vorticity_eps;
+    c_.dx = (T)dx;
+    c_.gridSize = (T)(0.5 / dx);
+    c_.oneOverDx = (T)(1.0 / dx);
+    c_.dt0 = (T)(dt / dx);
+    c_.divc = (T)(-dx * 0.5);
+    c_.wMinus = (T)(1.0 - p_.damping_w);
+    c_.sixth = (T)((1. / 6.) * p_.damping_w);
+    c_.xHi = (T)(g_.X - 2.5);
+    c_.yHi = (T)(g_.Y - 2.5);
+    c_.zHi = (T)(g_.Z - 2.5);
+    c_.has_vort = p_.vorticity_eps > 0.0 ? 1 : 0;
+    c_.has_beta = p_.buoyancy != 0.0 ? 1 : 0;
+  }
+
+  // MIC forward then backward sweep, one launch per hyperplane.
+  int mic_sweeps(const T* r, T* q, T* z, const CgState* st) {
+    const int planes = g_.nx + g_.ny + g_.nz - 2;
+    const int gp = grid_for((long long)g_.ny * g_.nz);
+    for (int s = 0; s < planes; s++) {
+      k_mic_fwd_plane<T><<<gp, 256, 0, s_>>>(g_, P_, r, q, s, st);
+      PL_CHECK_LAUNCH();
+    }
+    for (int s = planes - 1; s >= 0; s--) {
+      k_mic_bwd_plane<T><<<gp, 256, 0, s_>>>(g_, P_, q, z, s, st);
+      PL_CHECK_LAUNCH();
+    }
+    return PLUME_OK;
+  }
+
+  // MIC-PCG on device (FLUID_3D_MIC.cpp:918-1015); x holds the initial guess.
+  int solve_device(const T* b, T* x) {
+    const int crit = p_.criterion;
+    k_cg_init<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, b, x, r_, st_, part_, p_.tol,
+                                                     p_.max_iters, crit);
+    PL_CHECK_LAUNCH();
+    int rc = mic_sweeps(r_, qf_, z_, nullptr);
+    if (rc != PLUME_OK) return rc;
+    k_cg_init2<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, r_, z_, d_, st_, part_);
+    PL_CHECK_LAUNCH();
+    const int gI = grid_for(g_.nint);
+    int chunk = 4;
+    for (int it = 0; it < p_.max_iters + chunk;) {
+      for (int k = 0; k < chunk; k++) {
+        k_cg_spmv<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, d_, q_ad_, st_, part_);
+        PL_CHECK_LAUNCH();
+        k_cg_axpy<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, d_, q_ad_, x, r_, st_, part_);
+        PL_CHECK_LAUNCH();
+        rc = mic_sweeps(r_, qf_, z_, st_);
+        if (rc != PLUME_OK) return rc;
+        k_cg_rz<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, r_, z_, st_, part_);
+        PL_CHECK_LAUNCH();
+        k_cg_dir<T><<<gI, 256, 0, s_>>>(g_, z_, d_, st_, 1);
+        PL_CHECK_LAUNCH();
+      }
+      it += chunk;
+      PL_TRY(cudaMemcpyAsync(st_host_, st_, sizeof(CgState), cudaMemcpyDeviceToHost, s_));
+      PL_TRY(cudaStreamSynchronize(s_));
+      if (st_host_->done) break;
+      if (chunk < 16) chunk *= 2;
+    }
+    return PLUME_OK;
+  }
+
+  int fill_stats(plume_step_stats* st) {
+    PL_TRY(cudaMemcpyAsync(st_host_, st_, sizeof(CgState), cudaMemcpyDeviceToHost, s_));
+    PL_TRY(cudaStreamSynchronize(s_));
+    memset(st, 0, sizeof(*st));
+    st->iterations = st_host_->iter;
+    st->launches = launches_;
+    st->converged = st_host_->converged;
+    st->max_residual = st_host_->maxR;
+    st->rhs_norm = sqrt(st_host_->bb);
+    st->rel_residual = st_host_->bb > 0 ? sqrt(st_host_->rr) / sqrt(st_host_->bb) : 0.0;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ev_[0], ev_[3]) == cudaSuccess) st->ms_total = ms;
+    if (cudaEventElapsedTime(&ms, ev_[1], ev_[2]) == cudaSuccess) st->ms_solve = ms;
+    (void)cudaGetLastError();
+    return PLUME_OK;
+  }
+
+  const T* scalar_ptr(int field) const {
+    switch (field) {
+      case PLUME_F_DENSITY: return dens_;
+      case PLUME_F_DENSITY_OLD: return dens_old_;
+      case PLUME_F_HEAT: return heat_;
+      case PLUME_F_HEAT_OLD: return heat_old_;
+      case PLUME_F_PRESSURE: return pres_;
+      case PLUME_F_DIVERGENCE: return div_;
+      case PLUME_F_CACHED_PRESSURE: return pres_;      // solvePoisson leaves it untouched after
+      case PLUME_F_CACHED_DIVERGENCE: return div_;  // the copy (FLUID_3D_MIC.cpp:364,369)
+      default: return nullptr;
+    }
+  }
+  bool vector_ref(int field, V3<T>& v) const {
+    switch (field) {
+      case PLUME_F_VELOCITY: v = vel_; return true;
+      case PLUME_F_VELOCITY_OLD: v = vel_old_; return true;
+      case PLUME_F_FORCE: v = force_; return true;
+      case PLUME_F_VORTICITY: v = vort_; return true;
+      case PLUME_F_PREPROJECTION: v = preproj_; return true;
+      case PLUME_F_PREDIFFUSION: v = spare_; return true;
+      case PLUME_F_PREADVECTION: v = vel_old_; return true;  // same data after the swap (line 617)
+      case PLUME_F_POSTADVECTION: v = postadv_; return true;
+      case PLUME_F_PREVORTICITY: v = prevort_; return true;
+      default: return false;
+    }
+  }
+
+  // device plane -> host doubles at dst[k*stride + off]
+  int fetch_plane(const T* src, double* dst, int stride, int off) {
+    const size_t N = (size_t)g_.N;
+    PL_TRY(cudaMemcpyAsync(stage_, src, N * sizeof(T), cudaMemcpyDeviceToHost, s_));
+    PL_TRY(cudaStreamSynchronize(s_));
+    const T* h = (const T*)stage_;
+    for (size_t k = 0; k < N; k++) dst[k * stride + off] = (double)h[k];
+    return PLUME_OK;
+  }
+  int fetch_vec(const V3<T>& v, double* dst) {
+    int rc = fetch_plane(v.x, dst, 3, 0);
+    if (rc == PLUME_OK) rc = fetch_plane(v.y, dst, 3, 1);
+    if (rc == PLUME_OK) rc = fetch_plane(v.z, dst, 3, 2);
+    return rc;
+  }
+  int put_plane(T* dst, const double* src, int stride, int off) {
+    const size_t N = (size_t)g_.N;
+    PL_TRY(cudaStreamSynchronize(s_));
+    T* h = (T*)stage_;
+    for (size_t k = 0; k < N; k++) h[k] = (T)src[k * stride + off];
+    PL_TRY(cudaMemcpyAsync(dst, stage_, N * sizeof(T), cudaMemcpyHostToDevice, s_));
+    PL_TRY(cudaStreamSynchronize(s_));
+    return PLUME_OK;
+  }
+
+  int fail(int code, const char* msg) {
+    err_ = msg;
+    return code;
+  }
+  int fail_cuda(cudaError_t e, const char* what, const char* file, int line) {
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s: %s (%s:%d)", cudaGetErrorString(e), what, file, line);
+    err_ = buf;
+    (void)cudaGetLastError();
+    return (e == cudaErrorMemoryAllocation) ? PLUME_ERR_OOM : PLUME_ERR_CUDA;
+  }
+
+  void release() {
+    if (s_) cudaStreamSynchronize(s_);
+    if (pool_) cudaFree(pool_);
+    if (col_cells_) cudaFree(col_cells_);
+    if (src_dev_) cudaFree(src_dev_);
+    if (src_host_) cudaFreeHost(src_host_);
+    if (st_host_) cudaFreeHost(st_host_);
+    if (stage_) cudaFreeHost(stage_);
+    for (auto e : ev_)
+      if (e) cudaEventDestroy(e);
+    if (s_) cudaStreamDestroy(s_);
+    pool_ = nullptr;
+    s_ = nullptr;
+  }
+
+  plume_params p_{};
+  Grid g_{};
+  StepConsts<T> c_{};
+  double dx_ = 0, total_time_ = 0;
+  int total_steps_ = 0;
+  int launches_ = 0;
+  cudaStream_t s_ = nullptr;
+  cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+  char* pool_ = nullptr;
+  T *dens_ = nullptr, *dens_old_ = nullptr, *heat_ = nullptr, *heat_old_ = nullptr;
+  T *pres_ = nullptr, *div_ = nullptr, *mag_ = nullptr;
+  T *r_ = nullptr, *d_ = nullptr, *q_ad_ = nullptr, *z_ = nullptr, *qf_ = nullptr, *P_ = nullptr;
+  V3<T> vel_{}, vel_old_{}, spare_{}, prevort_{}, postadv_{}, preproj_{}, force_{}, vort_{};
+  double* P64_ = nullptr;
+  uint8_t* obst_ = nullptr;
+  CgState* st_ = nullptr;
+  double* part_ = nullptr;
+  int* col_cells_ = nullptr;
+  T* src_dev_ = nullptr;
+  T* src_host_ = nullptr;
+  int n_col_ = 0;
+  CgState* st_host_ = nullptr;
+  void* stage_ = nullptr;
+  std::string err_;
+};
+
+}  // namespace plume

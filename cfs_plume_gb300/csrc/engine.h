@@ -1,0 +1,46 @@
+// engine.h -- host-side interface of one plume simulation on one GPU.
+//
+// The C ABI (plume_api.cpp) owns an Engine through this interface; the
+// implementation is a template on the field type (engine.cuh), instantiated
+// once for FP64 (parity mode, compiled without multiply-add contraction) and
+// once for FP32 (fields in FP32, CG scalars and the MIC diagonal in FP64).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "../../include/plume.h"
+
+namespace plume {
+
+class Engine {
+ public:
+  virtual ~Engine() {}
+  // Allocates device state and builds the MIC diagonal.  Returns plume_status.
+  virtual int init(const plume_params& p) = 0;
+  virtual int add_source(int32_t step_index) = 0;
+  virtual int add_source_values(const double* values, size_t n) = 0;
+  virtual int run_timed(int32_t first_step, int32_t n, double* ms, plume_step_stats* stats) = 0;
+  // Enqueue one step; if stats != nullptr, wait for it and fill stats.
+  virtual int step(plume_step_stats* stats) = 0;
+  virtual int run(int32_t first_step, int32_t n, plume_step_stats* stats) = 0;
+  virtual int download(int field, double* dst, size_t n) = 0;
+  virtual int upload(int field, const double* src, size_t n) = 0;
+  virtual int download_obstacles(uint8_t* dst, size_t n) = 0;
+  // Poisson solve on a caller right-hand side (interior of `b`), x in/out.
+  virtual int solve(const double* b, double* x, plume_step_stats* stats) = 0;
+  // Forward/backward MIC sweeps of the engine's preconditioner on r (FP64 in/out).
+  virtual int mic_apply(const double* r, double* z, double* q) = 0;
+  virtual int mic_precon(double* precon) = 0;
+  virtual int sync() = 0;
+  virtual int32_t total_steps() const = 0;
+  virtual double total_time() const = 0;
+  virtual double dx() const = 0;
+  virtual const plume_params& params() const = 0;
+  virtual std::string& last_error() = 0;
+};
+
+Engine* make_engine_f64();
+Engine* make_engine_f32();
+
+}  // namespace plume

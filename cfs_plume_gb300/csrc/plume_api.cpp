@@ -1,0 +1,234 @@
+// plume_api.cpp -- the C ABI of libplume (include/plume.h).
+//
+// Thin layer: argument checks, status codes, and the host-side file output.
+// All field arithmetic happens in the CUDA engines; there is no CPU path.
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/plume.h"
+#include "../../include/plume_solver.h"
+#include "engine.h"
+#include "snapshot.h"
+
+struct plume_handle {
+  plume::Engine* eng = nullptr;
+  std::string err;
+};
+
+namespace {
+thread_local std::string g_create_error;
+
+int set_err(plume_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+int from_engine(plume_handle* h, int code) {
+  if (code != PLUME_OK) h->err = h->eng->last_error();
+  return code;
+}
+}  // namespace
+
+extern "C" {
+
+void plume_default_params(plume_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->abi_version = PLUME_ABI_VERSION;
+  p->res[0] = 48;  // fluid3D.cpp:313-315
+  p->res[1] = 64;
+  p->res[2] = 48;
+  const int bc[6] = {1, 1, 1, 1, 0, 0};  // fluid3D.cpp:321-327
+  for (int k = 0; k < 6; k++) p->bc[k] = bc[k];
+  p->dt = 0.1;
+  p->buoyancy = (double)0.1f;
+  p->vorticity_eps = 0.0;
+  p->damping_w = 0.9;
+  p->mic_tau = 0.97;
+  p->mic_sigma = 0.25;
+  p->source = PLUME_SRC_COLUMN;
+  p->precision = PLUME_PREC_FP64;
+  p->criterion = PLUME_CRIT_REFERENCE;
+  p->tol = 1e-10;
+  p->max_iters = 1000;
+  p->warm_start = PLUME_WARM_ZERO;
+  p->cache_fields = 1;
+  p->device = 0;
+}
+
+int plume_create(const plume_params* p, plume_handle** out) {
+  if (!out) return PLUME_ERR_INVALID;
+  *out = nullptr;
+  if (!p) {
+    g_create_error = "null params";
+    return PLUME_ERR_INVALID;
+  }
+  if (p->abi_version != PLUME_ABI_VERSION) {
+    g_create_error = "abi_version mismatch";
+    return PLUME_ERR_INVALID;
+  }
+  if (p->precision != PLUME_PREC_FP64 && p->precision != PLUME_PREC_FP32) {
+    g_create_error = "unknown precision";
+    return PLUME_ERR_INVALID;
+  }
+  plume_handle* h = new (std::nothrow) plume_handle();
+  if (!h) return PLUME_ERR_OOM;
+  h->eng = (p->precision == PLUME_PREC_FP64) ? plume::make_engine_f64() : plume::make_engine_f32();
+  const int rc = h->eng->init(*p);
+  if (rc != PLUME_OK) {
+    g_create_error = h->eng->last_error();
+    delete h->eng;
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return PLUME_OK;
+}
+
+void plume_destroy(plume_handle* h) {
+  if (!h) return;
+  delete h->eng;
+  delete h;
+}
+
+int plume_add_source(plume_handle* h, int32_t step_index) {
+  if (!h) return PLUME_ERR_INVALID;
+  return from_engine(h, h->eng->add_source(step_index));
+}
+
+int plume_add_source_values(plume_handle* h, const double* values, size_t n) {
+  if (!h) return PLUME_ERR_INVALID;
+  return from_engine(h, h->eng->add_source_values(values, n));
+}
+
+int plume_run_timed(plume_handle* h, int32_t first_step_index, int32_t n, double* ms_device,
+                    plume_step_stats* stats) {
+  if (!h || !ms_device) return PLUME_ERR_INVALID;
+  if (n < 0) return set_err(h, PLUME_ERR_INVALID, "negative step count");
+  return from_engine(h, h->eng->run_timed(first_step_index, n, ms_device, stats));
+}
+
+int plume_step(plume_handle* h, plume_step_stats* stats) {
+  if (!h) return PLUME_ERR_INVALID;
+  return from_engine(h, h->eng->step(stats));
+}
+
+int plume_run(plume_handle* h, int32_t first_step_index, int32_t n, plume_step_stats* stats) {
+  if (!h) return PLUME_ERR_INVALID;
+  if (n < 0) return set_err(h, PLUME_ERR_INVALID, "negative step count");
+  return from_engine(h, h->eng->run(first_step_index, n, stats));
+}
+
+int plume_download(plume_handle* h, int32_t field, double* dst, size_t n) {
+  if (!h) return PLUME_ERR_INVALID;
+  if (field < 0 || field >= PLUME_F_COUNT) return set_err(h, PLUME_ERR_INVALID, "unknown field");
+  return from_engine(h, h->eng->download(field, dst, n));
+}
+
+int plume_upload(plume_handle* h, int32_t field, const double* src, size_t n) {
+  if (!h) return PLUME_ERR_INVALID;
+  if (field < 0 || field >= PLUME_F_COUNT) return set_err(h, PLUME_ERR_INVALID, "unknown field");
+  return from_engine(h, h->eng->upload(field, src, n));
+}
+
+int plume_download_obstacles(plume_handle* h, uint8_t* dst, size_t n) {
+  if (!h) return PLUME_ERR_INVALID;
+  return from_engine(h, h->eng->download_obstacles(dst, n));
+}
+
+int plume_get_info(plume_handle* h, int32_t res[3], int32_t* total_steps, double* total_time,
+                   double* dx) {
+  if (!h) return PLUME_ERR_INVALID;
+  const plume_params& p = h->eng->params();
+  if (res)
+    for (int k = 0; k < 3; k++) res[k] = p.res[k];
+  if (total_steps) *total_steps = h->eng->total_steps();
+  if (total_time) *total_time = h->eng->total_time();
+  if (dx) *dx = h->eng->dx();
+  return PLUME_OK;
+}
+
+static plume::FieldFetch make_fetch(plume_handle* h) {
+  return [h](int field, std::vector<double>& buf) {
+    const plume_params& p = h->eng->params();
+    const size_t N = (size_t)p.res[0] * p.res[1] * p.res[2];
+    const bool vec = field == PLUME_F_VELOCITY || field == PLUME_F_VELOCITY_OLD ||
+                     field == PLUME_F_FORCE || field == PLUME_F_VORTICITY ||
+                     field == PLUME_F_PREPROJECTION || field == PLUME_F_PREDIFFUSION ||
+                     field == PLUME_F_PREADVECTION || field == PLUME_F_CACHED_QUADRATIC ||
+                     field == PLUME_F_POSTADVECTION || field == PLUME_F_PREVORTICITY;
+    buf.resize(vec ? 3 * N : N);
+    return h->eng->download(field, buf.data(), buf.size());
+  };
+}
+
+int plume_write_state(plume_handle* h, const char* path) {
+  if (!h) return PLUME_ERR_INVALID;
+  if (!path) return set_err(h, PLUME_ERR_INVALID, "null path");
+  const plume_params& p = h->eng->params();
+  if (!p.cache_fields) return set_err(h, PLUME_ERR_STATE, "state file needs cache_fields = 1");
+  plume::StateHeader hd;
+  for (int k = 0; k < 3; k++) hd.res[k] = p.res[k];
+  hd.total_steps = h->eng->total_steps();
+  hd.dx = h->eng->dx();
+  hd.total_time = h->eng->total_time();
+  hd.dt = p.dt;
+  hd.buoyancy = p.buoyancy;
+  hd.vorticity_eps = p.vorticity_eps;
+  std::vector<uint8_t> ob((size_t)p.res[0] * p.res[1] * p.res[2]);
+  int rc = h->eng->download_obstacles(ob.data(), ob.size());
+  if (rc != PLUME_OK) return from_engine(h, rc);
+  return plume::write_state_gz(path, hd, make_fetch(h), ob, h->err);
+}
+
+int plume_append_streams(plume_handle* h, const char* dir) {
+  if (!h) return PLUME_ERR_INVALID;
+  if (!dir) return set_err(h, PLUME_ERR_INVALID, "null directory");
+  const plume_params& p = h->eng->params();
+  if (!p.cache_fields) return set_err(h, PLUME_ERR_STATE, "streams need cache_fields = 1");
+  return plume::append_streams(dir, p.res, make_fetch(h), h->err);
+}
+
+const char* plume_strerror(int status) {
+  switch (status) {
+    case PLUME_OK: return "ok";
+    case PLUME_ERR_INVALID: return "invalid argument";
+    case PLUME_ERR_CUDA: return "CUDA error";
+    case PLUME_ERR_OOM: return "out of memory";
+    case PLUME_ERR_TIMEOUT: return "device wait timed out";
+    case PLUME_ERR_IO: return "file I/O error";
+    case PLUME_ERR_NOT_CONVERGED: return "solver did not converge";
+    case PLUME_ERR_UNSUPPORTED: return "unsupported";
+    case PLUME_ERR_STATE: return "call not allowed in this state";
+    default: return "unknown status";
+  }
+}
+
+const char* plume_last_error(plume_handle* h) {
+  if (!h) return g_create_error.c_str();
+  return h->err.c_str();
+}
+
+// ---- solver-level entry points (include/plume_solver.h) ----
+int plume_solve_poisson(plume_handle* h, const double* b, double* x, plume_step_stats* stats) {
+  if (!h) return PLUME_ERR_INVALID;
+  return from_engine(h, h->eng->solve(b, x, stats));
+}
+
+int plume_mic_apply(plume_handle* h, const double* r, double* z, double* q) {
+  if (!h || !r || !z) return PLUME_ERR_INVALID;
+  return from_engine(h, h->eng->mic_apply(r, z, q));
+}
+
+int plume_mic_diagonal(plume_handle* h, double* precon) {
+  if (!h || !precon) return PLUME_ERR_INVALID;
+  return from_engine(h, h->eng->mic_precon(precon));
+}
+
+int plume_sync(plume_handle* h) {
+  if (!h) return PLUME_ERR_INVALID;
+  return from_engine(h, h->eng->sync());
+}
+
+}  // extern "C"

@@ -1,0 +1,294 @@
+// snapshot.cpp -- reference-format state files and SVD streams (host C++).
+#include "snapshot.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "../../include/plume.h"
+
+#if defined(PLUME_HAVE_ZLIB)
+#include <zlib.h>
+#endif
+
+namespace plume {
+
+namespace {
+
+// gzip output.  With zlib: gzopen(path, "wb1") exactly as the reference.
+// Without zlib headers at build time: a gzip member of stored (uncompressed)
+// deflate blocks, which zlib's gzread reads like any other member.
+class GzOut {
+ public:
+  bool open(const std::string& path) {
+#if defined(PLUME_HAVE_ZLIB)
+    f_ = gzopen(path.c_str(), "wb1");
+    return f_ != nullptr;
+#else
+    f_ = fopen(path.c_str(), "wb");
+    if (!f_) return false;
+    static const unsigned char hdr[10] = {0x1f, 0x8b, 8, 0, 0, 0, 0, 0, 0, 3};
+    fwrite(hdr, 1, 10, f_);
+    crc_ = 0xffffffffu;
+    size_ = 0;
+    return true;
+#endif
+  }
+  bool write(const void* data, size_t n) {
+    const unsigned char* p = (const unsigned char*)data;
+#if defined(PLUME_HAVE_ZLIB)
+    while (n > 0) {
+      const unsigned chunk = n > (1u << 30) ? (1u << 30) : (unsigned)n;
+      if (gzwrite(f_, p, chunk) != (int)chunk) return false;
+      p += chunk;
+      n -= chunk;
+    }
+    return true;
+#else
+    while (n > 0) {
+      const size_t chunk = n > 65535 ? 65535 : n;
+      const unsigned char b[5] = {0, (unsigned char)(chunk & 0xff), (unsigned char)(chunk >> 8),
+                                  (unsigned char)(~chunk & 0xff),
+                                  (unsigned char)((~chunk >> 8) & 0xff)};
+      if (fwrite(b, 1, 5, f_) != 5 || fwrite(p, 1, chunk, f_) != chunk) return false;
+      update_crc(p, chunk);
+      size_ += chunk;
+      p += chunk;
+      n -= chunk;
+    }
+    return true;
+#endif
+  }
+  bool close() {
+#if defined(PLUME_HAVE_ZLIB)
+    return gzclose(f_) == Z_OK;
+#else
+    const unsigned char last[5] = {1, 0, 0, 0xff, 0xff};  // final empty stored block
+    fwrite(last, 1, 5, f_);
+    const uint32_t crc = crc_ ^ 0xffffffffu;
+    unsigned char tail[8];
+    for (int k = 0; k < 4; k++) tail[k] = (unsigned char)(crc >> (8 * k));
+    for (int k = 0; k < 4; k++) tail[4 + k] = (unsigned char)((uint32_t)size_ >> (8 * k));
+    fwrite(tail, 1, 8, f_);
+    return fclose(f_) == 0;
+#endif
+  }
+
+ private:
+#if defined(PLUME_HAVE_ZLIB)
+  gzFile f_ = nullptr;
+#else
+  void update_crc(const unsigned char* p, size_t n) {
+    static uint32_t table[256];
+    static bool init = false;
+    if (!init) {
+      for (uint32_t i = 0; i < 256; i++) {
+        uint32_t c = i;
+        for (int k = 0; k < 8; k++) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+        table[i] = c;
+      }
+      init = true;
+    }
+    uint32_t c = crc_;
+    for (size_t i = 0; i < n; i++) c = table[(c ^ p[i]) & 0xff] ^ (c >> 8);
+    crc_ = c;
+  }
+  FILE* f_ = nullptr;
+  uint32_t crc_ = 0;
+  uint64_t size_ = 0;
+#endif
+};
+
+template <typename V>
+bool put(GzOut& g, const V& v) {
+  return g.write(&v, sizeof(V));
+}
+
+// FIELD_3D::writeGz / VECTOR3_FIELD_3D::writeGz (FIELD_3D.cpp:5993-6014,
+// VECTOR3_FIELD_3D.cpp:1327-1346): 3 ints, center, lengths, doubles.
+bool put_field(GzOut& g, const int res[3], const double center[3], const double lengths[3],
+               const std::vector<double>& data) {
+  bool ok = put(g, res[0]) && put(g, res[1]) && put(g, res[2]);
+  for (int k = 0; k < 3; k++) ok = ok && put(g, center[k]);
+  for (int k = 0; k < 3; k++) ok = ok && put(g, lengths[k]);
+  return ok && g.write(data.data(), data.size() * sizeof(double));
+}
+
+}  // namespace
+
+int write_state_gz(const std::string& path_in, const StateHeader& h, const FieldFetch& fetch,
+                   const std::vector<uint8_t>& obstacles, std::string& err) {
+  std::string path = path_in;
+  const size_t n = path.size();
+  if (n < 2 || path[n - 1] != 'z' || path[n - 2] != 'g') path += ".gz";  // line 1025-1027
+  GzOut g;
+  if (!g.open(path)) {
+    err = "could not open " + path;
+    return PLUME_ERR_IO;
+  }
+  const int X = h.res[0], Y = h.res[1], Z = h.res[2];
+  int maxRes = X > Y ? X : Y;
+  maxRes = Z > maxRes ? Z : maxRes;
+  const int ints[10] = {X, Y, Z, maxRes, 1, X, X * Y, X * Y * Z, X * Y, h.total_steps};
+  const double dbls[7] = {h.dx, h.total_time, h.dt, h.buoyancy, h.vorticity_eps, 1e-3, 1e-10};
+  bool ok = g.write(ints, sizeof(ints)) && g.write(dbls, sizeof(dbls));
+  const double center[3] = {0, 0, 0};
+  const double lengths[3] = {h.dx * X, h.dx * Y, h.dx * Z};  // FLUID_3D_MIC.cpp:56
+  std::vector<double> buf;
+  // fields in the order of lines 1057-1076
+  const int order[] = {PLUME_F_DENSITY,       PLUME_F_DENSITY_OLD,      PLUME_F_HEAT,
+                       PLUME_F_HEAT_OLD,      PLUME_F_PRESSURE,         PLUME_F_DIVERGENCE,
+                       PLUME_F_VELOCITY,      PLUME_F_VELOCITY_OLD,     PLUME_F_FORCE,
+                       PLUME_F_VORTICITY,     PLUME_F_PREPROJECTION,    PLUME_F_PREDIFFUSION,
+                       PLUME_F_PREADVECTION,  PLUME_F_CACHED_QUADRATIC, PLUME_F_POSTADVECTION,
+                       PLUME_F_CACHED_PRESSURE, PLUME_F_CACHED_DIVERGENCE};
+  for (int f : order) {
+    if (!ok) break;
+    int rc = fetch(f, buf);
+    if (rc != PLUME_OK) {
+      g.close();
+      err = "field download failed while writing " + path;
+      return rc;
+    }
+    ok = put_field(g, h.res, center, lengths, buf);
+  }
+  // obstacles, center, lengths, IOP count (lines 1078-1091)
+  ok = ok && g.write(obstacles.data(), obstacles.size());
+  for (int k = 0; k < 3; k++) ok = ok && put(g, center[k]);
+  for (int k = 0; k < 3; k++) ok = ok && put(g, lengths[k]);
+  const int howMany = 0;
+  ok = ok && put(g, howMany);
+  // prevorticity, then the never-assigned midMaccormack and postIOP fields
+  // (default-constructed: zero dims, zero center and lengths, no data)
+  if (ok) {
+    int rc = fetch(PLUME_F_PREVORTICITY, buf);
+    if (rc != PLUME_OK) {
+      g.close();
+      err = "field download failed while writing " + path;
+      return rc;
+    }
+    ok = put_field(g, h.res, center, lengths, buf);
+  }
+  const int zres[3] = {0, 0, 0};
+  const double zero3[3] = {0, 0, 0};
+  const std::vector<double> empty;
+  ok = ok && put_field(g, zres, zero3, zero3, empty);
+  ok = ok && put_field(g, zres, zero3, zero3, empty);
+  const bool closed = g.close();
+  if (!ok || !closed) {
+    err = "write failed: " + path;
+    return PLUME_ERR_IO;
+  }
+  return PLUME_OK;
+}
+
+namespace {
+
+// peelBoundary + flattened (VECTOR3_FIELD_3D.cpp:3139-3151, 3222-3232;
+// FIELD_3D.cpp:6679-6689, 6722-6733): interior cells, x fastest.
+void peel(const int res[3], const std::vector<double>& full, int comps, std::vector<double>& out) {
+  const int X = res[0], Y = res[1], Z = res[2];
+  out.resize((size_t)comps * (X - 2) * (Y - 2) * (Z - 2));
+  size_t o = 0;
+  for (int z = 1; z < Z - 1; z++)
+    for (int y = 1; y < Y - 1; y++)
+      for (int x = 1; x < X - 1; x++) {
+        const size_t c = (size_t)x + (size_t)y * X + (size_t)z * X * Y;
+        for (int k = 0; k < comps; k++) out[o++] = full[comps * c + k];
+      }
+}
+
+// VECTOR::norm2 on Linux: sqrt of the serial dot (VECTOR.cpp:426-437).
+double norm2(const std::vector<double>& v) {
+  double s = 0;
+  for (double x : v) s += x * x;
+  return sqrt(s);
+}
+
+}  // namespace
+
+int append_streams(const std::string& dir, const int res[3], const FieldFetch& fetch,
+                   std::string& err) {
+  static const char* dims_names[6] = {"velocity.final.matrix.dims", "velocity.preproject.matrix.dims",
+                                      "velocity.prediffuse.matrix.dims",
+                                      "velocity.preadvect.matrix.dims", "velocity.iop.matrix.dims",
+                                      "pressure.matrix.dims"};
+  int rows[6] = {0, 0, 0, 0, 0, 0}, cols[6] = {0, 0, 0, 0, 0, 0};
+  for (int k = 0; k < 6; k++) {  // lines 1347-1361
+    FILE* f = fopen((dir + dims_names[k]).c_str(), "rb");
+    if (!f) continue;
+    int r = 0, c = 0;
+    if (fread(&r, sizeof(int), 1, f) == 1 && fread(&c, sizeof(int), 1, f) == 1) {
+      rows[k] = r;
+      cols[k] = c;
+    }
+    fclose(f);
+  }
+  const int nint = (res[0] - 2) * (res[1] - 2) * (res[2] - 2);
+  for (int k = 0; k < 5; k++)
+    if (cols[k] == 0) cols[k] = 3 * nint;
+  if (cols[5] == 0) cols[5] = nint;
+
+  struct Row {
+    const char* file;
+    int field;
+    int comps;
+    int dims_slot;
+  };
+  // lines 1402-1461: four velocity streams, then pressure and divergence rows
+  // into the same pressure stream; the IOP stream is only created.
+  const Row rows_to_write[6] = {
+      {"velocity.final.matrix.transpose", PLUME_F_VELOCITY, 3, 0},
+      {"velocity.preproject.matrix.transpose", PLUME_F_PREPROJECTION, 3, 1},
+      {"velocity.prediffuse.matrix.transpose", PLUME_F_PREDIFFUSION, 3, 2},
+      {"velocity.preadvect.matrix.transpose", PLUME_F_PREADVECTION, 3, 3},
+      {"pressure.matrix.transpose", PLUME_F_PRESSURE, 1, 5},
+      {"pressure.matrix.transpose", PLUME_F_DIVERGENCE, 1, 5},
+  };
+  {
+    FILE* iop = fopen((dir + "velocity.iop.matrix.transpose").c_str(), "ab");
+    if (!iop) {
+      err = "could not open streams under " + dir;
+      return PLUME_ERR_IO;
+    }
+    fclose(iop);
+  }
+  std::vector<double> full, peeled;
+  for (const Row& r : rows_to_write) {
+    int rc = fetch(r.field, full);
+    if (rc != PLUME_OK) {
+      err = "field download failed while appending streams";
+      return rc;
+    }
+    peel(res, full, r.comps, peeled);
+    FILE* f = fopen((dir + r.file).c_str(), "ab");
+    if (!f) {
+      err = std::string("could not open ") + dir + r.file;
+      return PLUME_ERR_IO;
+    }
+    bool ok = true;
+    if (norm2(peeled) > 1e-7) {
+      ok = fwrite(peeled.data(), sizeof(double), peeled.size(), f) == peeled.size();
+      rows[r.dims_slot]++;
+    }
+    if (fclose(f) != 0 || !ok) {
+      err = std::string("write failed: ") + dir + r.file;
+      return PLUME_ERR_IO;
+    }
+  }
+  for (int k = 0; k < 6; k++) {  // lines 1465-1474
+    FILE* f = fopen((dir + dims_names[k]).c_str(), "wb");
+    if (!f) {
+      err = std::string("could not write ") + dir + dims_names[k];
+      return PLUME_ERR_IO;
+    }
+    const bool ok = fwrite(&rows[k], sizeof(int), 1, f) == 1 && fwrite(&cols[k], sizeof(int), 1, f) == 1;
+    if (fclose(f) != 0 || !ok) {
+      err = std::string("write failed: ") + dir + dims_names[k];
+      return PLUME_ERR_IO;
+    }
+  }
+  return PLUME_OK;
+}
+
+}  // namespace plume

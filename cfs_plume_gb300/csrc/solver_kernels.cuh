@@ -1,0 +1,365 @@
+// solver_kernels.cuh -- MIC(0)-preconditioned CG of FLUID_3D_MIC::solvePoisson
+// (FLUID_3D_MIC.cpp:918-1015) as device kernels.
+//
+// The Poisson matrix of the plume (heat = false, FLUID_3D_MIC.cpp:772-801) has
+// off-diagonal entries -1 (fluid neighbour) or 0 (wall neighbour) and a
+// diagonal equal to the number of non-wall neighbours, so the kernels derive
+// every coefficient from the cell's position and the wall flags instead of
+// reading the reference's four coefficient fields.
+//
+// CG scalars live in device memory (CgState) and are computed by the last
+// block of each reduction kernel from per-block partials summed in a fixed
+// order, so a solve is deterministic and needs no host round trip per
+// iteration.  Every iteration kernel returns at entry once `done` is set.
+#pragma once
+#include "common.cuh"
+
+namespace plume {
+
+struct CgState {
+  double deltaNew, deltaOld, alpha, beta;
+  double maxR, oldMaxR;  // signed max of r (reference criterion)
+  double rr, bb;         // r.r and b.b
+  double dq;             // d.(A d)
+  double tol;            // absolute (reference) or relative (rel2) tolerance
+  int iter, max_iters, criterion, done;
+  int converged, broke, pad0, pad1;
+  unsigned int ticket[4];
+};
+
+constexpr int kRedThreads = 256;
+constexpr int kRedBlocks = 608;  // 4 x 152 SMs
+
+// Off-diagonal coefficient toward a neighbour: -1 unless the neighbour is a wall.
+template <typename T>
+__device__ inline T coef(bool wall) {
+  return wall ? T(0) : T(-1);
+}
+
+// Diagonal: number of non-wall neighbours (buildA, FLUID_3D_MIC.cpp:784-791).
+template <typename T>
+__device__ inline T adiag(const Grid& g, int x, int y, int z) {
+  T a = T(0);
+  if (!wall_xp(g, x)) a += T(1);
+  if (!wall_xm(g, x)) a += T(1);
+  if (!wall_yp(g, y)) a += T(1);
+  if (!wall_ym(g, y)) a += T(1);
+  if (!wall_zp(g, z)) a += T(1);
+  if (!wall_zm(g, z)) a += T(1);
+  return a;
+}
+
+// multA (FLUID_3D_MIC.cpp:811-822) at one interior cell, in the reference order.
+template <typename T>
+__device__ inline T mult_a_cell(const Grid& g, const T* xf, int i, int x, int y, int z) {
+  return adiag<T>(g, x, y, z) * xf[i] + xf[i - 1] * coef<T>(wall_xm(g, x)) +
+         xf[i + 1] * coef<T>(wall_xp(g, x)) + xf[i - g.X] * coef<T>(wall_ym(g, y)) +
+         xf[i + g.X] * coef<T>(wall_yp(g, y)) + xf[i - g.slab] * coef<T>(wall_zm(g, z)) +
+         xf[i + g.slab] * coef<T>(wall_zp(g, z));
+}
+
+// ------------------------------------------------- last-block reductions
+__device__ inline bool arrive_last(unsigned int* ticket) {
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned int t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+
+// Sum the gridDim.x partials in a fixed order (valid in thread 0).
+__device__ inline double sum_partials(const double* part, double* sh) {
+  double s = 0.0;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) s += __ldcg(part + k);
+  return block_sum(s, sh);
+}
+__device__ inline double max_partials(const double* part, double* sh) {
+  double s = -1.0e308;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+    const double v = __ldcg(part + k);
+    s = v > s ? v : s;
+  }
+  return block_max(s, sh, -1.0e308);
+}
+
+// ------------------------------------------------------------ MIC diagonal
+// buildMICPreconditioner (FLUID_3D_MIC.cpp:825-856) for the cells of one
+// hyperplane x+y+z = const (interior coordinates); the recurrence only reads
+// the x-1, y-1, z-1 neighbours, which lie on the previous hyperplane.  FP64.
+// `P64` is zero on the border, as the reference's _precon is.  Defined only in
+// the FP64 translation unit (compiled without multiply-add contraction), so
+// both engines use the same diagonal bits.
+#ifdef PLUME_DEFINE_PRECON
+__global__ void k_mic_precon_plane(Grid g, double* P64, int s, double tau, double sig) {
+  PL_GRID_STRIDE(k, g.ny * g.nz) {
+    const int j = k % g.ny, l = k / g.ny;
+    const int ix = s - j - l;
+    if (ix < 0 || ix >= g.nx) continue;
+    const int x = ix + 1, y = j + 1, z = l + 1;
+    const int i = x + y * g.X + z * g.slab;
+    const int xm = i - 1, ym = i - g.X, zm = i - g.slab;
+    // A+ at the minus neighbours (FLUID_3D_MIC.cpp:792-797 written by this
+    // cell, or by the neighbour itself when it is an interior cell):
+    const double ai_xm = coef<double>(wall_xm(g, x));
+    const double aj_ym = coef<double>(wall_ym(g, y));
+    const double ak_zm = coef<double>(wall_zm(g, z));
+    // A+ of the neighbours toward their other plus-directions; only needed
+    // when the neighbour is interior (its diagonal entry P is 0 otherwise).
+    const double aj_xm = (x > 1) ? coef<double>(wall_yp(g, y)) : 0.0;
+    const double ak_xm = (x > 1) ? coef<double>(wall_zp(g, z)) : 0.0;
+    const double ai_ym = (y > 1) ? coef<double>(wall_xp(g, x)) : 0.0;
+    const double ak_ym = (y > 1) ? coef<double>(wall_zp(g, z)) : 0.0;
+    const double ai_zm = (z > 1) ? coef<double>(wall_xp(g, x)) : 0.0;
+    const double aj_zm = (z > 1) ? coef<double>(wall_yp(g, y)) : 0.0;
+    const double pmini2 = P64[xm] * P64[xm];
+    const double pminj2 = P64[ym] * P64[ym];
+    const double pmink2 = P64[zm] * P64[zm];
+    const double e0 = ai_xm * ai_xm * pmini2 + aj_ym * aj_ym * pminj2 + ak_zm * ak_zm * pmink2;
+    const double e1 = tau * (ai_xm * (aj_xm + ak_xm) * pmini2 + aj_ym * (ai_ym + ak_ym) * pminj2 +
+                             ak_zm * (ai_zm + aj_zm) * pmink2);
+    const double ad = adiag<double>(g, x, y, z);
+    double e = ad - e0 - e1;
+    if (e < sig * ad) e = ad;
+    P64[i] = (fabs(ad) < 0.000001) ? 0.0 : 1.0 / sqrt(e);
+  }
+}
+#endif
+// Builds the FP64 MIC diagonal into P64 (hyperplane launches on `s`).
+cudaError_t build_mic_diagonal(const Grid& g, double* P64, double tau, double sig, cudaStream_t s);
+
+template <typename T>
+__global__ void k_convert_precon(int n, const double* P64, T* P) {
+  PL_GRID_STRIDE(i, n) P[i] = (T)P64[i];
+}
+
+// ---------------------------------------------- MIC sweeps, one hyperplane
+// applyMICPreconditioner (FLUID_3D_MIC.cpp:870-898), each cell evaluated with
+// the reference's expression, so the result is bit-identical to the serial
+// sweep in FP64.  One launch per hyperplane; used at set-up and as the
+// reference path the wavefront kernels are tested against.
+template <typename T>
+__global__ void k_mic_fwd_plane(Grid g, const T* P, const T* r, T* q, int s,
+                                const CgState* st) {
+  if (st && st->done) return;
+  PL_GRID_STRIDE(k, g.ny * g.nz) {
+    const int j = k % g.ny, l = k / g.ny;
+    const int ix = s - j - l;
+    if (ix < 0 || ix >= g.nx) continue;
+    const int x = ix + 1, y = j + 1, z = l + 1;
+    const int i = x + y * g.X + z * g.slab;
+    const int xm = i - 1, ym = i - g.X, zm = i - g.slab;
+    const T t = r[i] - coef<T>(wall_xm(g, x)) * P[xm] * q[xm] -
+                coef<T>(wall_ym(g, y)) * P[ym] * q[ym] - coef<T>(wall_zm(g, z)) * P[zm] * q[zm];
+    q[i] = t * P[i];
+  }
+}
+
+template <typename T>
+__global__ void k_mic_bwd_plane(Grid g, const T* P, const T* q, T* zf, int s,
+                                const CgState* st) {
+  if (st && st->done) return;
+  PL_GRID_STRIDE(k, g.ny * g.nz) {
+    const int j = k % g.ny, l = k / g.ny;
+    const int ix = s - j - l;
+    if (ix < 0 || ix >= g.nx) continue;
+    const int x = ix + 1, y = j + 1, z = l + 1;
+    const int i = x + y * g.X + z * g.slab;
+    const T p = P[i];
+    const T t = q[i] - coef<T>(wall_xp(g, x)) * p * zf[i + 1] -
+                coef<T>(wall_yp(g, y)) * p * zf[i + g.X] -
+                coef<T>(wall_zp(g, z)) * p * zf[i + g.slab];
+    zf[i] = t * p;
+  }
+}
+
+// ------------------------------------------------------------ CG kernels
+// Solve set-up part 1 (lines 921-933): r = b - A x on the interior and b.b.
+template <typename T>
+__global__ void k_cg_init(Grid g, const T* b, const T* x, T* r, CgState* st, double* part,
+                          double tol, int max_iters, int criterion) {
+  __shared__ double sh[32];
+  double bb = 0.0;
+  PL_GRID_STRIDE(k, g.nint) {
+    int cx, cy, cz;
+    const int i = interior_cell(g, k, cx, cy, cz);
+    const T ax = mult_a_cell(g, x, i, cx, cy, cz);
+    r[i] = b[i] - ax;
+    bb += (double)b[i] * (double)b[i];
+  }
+  const double s = block_sum(bb, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (arrive_last(&st->ticket[0])) {
+    const double tot = sum_partials(part, sh);
+    if (threadIdx.x == 0) {
+      st->bb = tot;
+      st->tol = tol;
+      st->max_iters = max_iters;
+      st->criterion = criterion;
+      st->iter = 0;
+      st->done = 0;
+      st->converged = 0;
+      st->broke = 0;
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// Solve set-up part 2 (lines 935-944): d = z, deltaNew = r.z, and the entry
+// test of the loop.
+template <typename T>
+__global__ void k_cg_init2(Grid g, const T* r, const T* z, T* d, CgState* st, double* part) {
+  __shared__ double sh[32];
+  double rz = 0.0, rr = 0.0;
+  PL_GRID_STRIDE(k, g.nint) {
+    int cx, cy, cz;
+    const int i = interior_cell(g, k, cx, cy, cz);
+    const T zi = z[i], ri = r[i];
+    d[i] = zi;
+    rz += (double)ri * (double)zi;
+    rr += (double)ri * (double)ri;
+  }
+  const double s1 = block_sum(rz, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s1;
+  const double s2 = block_sum(rr, sh);
+  if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
+  if (arrive_last(&st->ticket[0])) {
+    const double trz = sum_partials(part, sh);
+    const double trr = sum_partials(part + kRedBlocks, sh);
+    if (threadIdx.x == 0) {
+      st->deltaNew = trz;
+      st->rr = trr;
+      if (st->criterion == 0) {
+        st->maxR = 2.0 * st->tol;  // FLUID_3D_MIC.cpp:946
+        if (!(st->maxR > st->tol) || st->max_iters <= 0) st->done = 1;
+      } else {
+        if (sqrt(trr) <= st->tol * sqrt(st->bb)) {
+          st->done = 1;
+          st->converged = 1;
+        }
+        if (st->max_iters <= 0) st->done = 1;
+      }
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// Iteration part 1 (lines 955-969): q = A d, alpha = deltaNew / d.q.
+template <typename T>
+__global__ void k_cg_spmv(Grid g, const T* d, T* q, CgState* st, double* part) {
+  if (st->done) return;
+  __shared__ double sh[32];
+  double dq = 0.0;
+  PL_GRID_STRIDE(k, g.nint) {
+    int cx, cy, cz;
+    const int i = interior_cell(g, k, cx, cy, cz);
+    const T qi = mult_a_cell(g, d, i, cx, cy, cz);
+    q[i] = qi;
+    dq += (double)d[i] * (double)qi;
+  }
+  const double s = block_sum(dq, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (arrive_last(&st->ticket[0])) {
+    const double t = sum_partials(part, sh);
+    if (threadIdx.x == 0) {
+      st->dq = t;
+      if (fabs(t) > 0.0) {
+        st->alpha = st->deltaNew / t;
+      } else {  // "PCG alpha broke down! Bailing." (lines 962-969)
+        st->done = 1;
+        st->broke = 1;
+      }
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// Iteration part 2 (lines 972-983): x += alpha d, r -= alpha q, then the
+// signed max of r (border cells hold 0) and r.r.
+template <typename T>
+__global__ void k_cg_axpy(Grid g, const T* d, const T* q, T* x, T* r, CgState* st,
+                          double* part) {
+  if (st->done) return;
+  __shared__ double sh[32];
+  const T alpha = (T)st->alpha;
+  double mx = -1.0e308, rr = 0.0;
+  PL_GRID_STRIDE(k, g.nint) {
+    int cx, cy, cz;
+    const int i = interior_cell(g, k, cx, cy, cz);
+    x[i] += alpha * d[i];
+    const T ri = r[i] + (-alpha) * q[i];
+    r[i] = ri;
+    mx = ((double)ri > mx) ? (double)ri : mx;
+    rr += (double)ri * (double)ri;
+  }
+  const double s1 = block_max(mx, sh, -1.0e308);
+  if (threadIdx.x == 0) part[blockIdx.x] = s1;
+  const double s2 = block_sum(rr, sh);
+  if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
+  if (arrive_last(&st->ticket[0])) {
+    const double tm = max_partials(part, sh);
+    const double trr = sum_partials(part + kRedBlocks, sh);
+    if (threadIdx.x == 0) {
+      st->oldMaxR = st->maxR;
+      st->maxR = tm > 0.0 ? tm : 0.0;  // FIELD_3D::max starts at a border cell (0)
+      st->rr = trr;
+      if (st->criterion == 1 && sqrt(trr) <= st->tol * sqrt(st->bb)) {
+        st->iter += 1;
+        st->done = 1;
+        st->converged = 1;
+      }
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// Iteration part 3 (lines 985-991): deltaNew = r.z, beta; and the loop's exit
+// tests (lines 951, 1003-1010).
+template <typename T>
+__global__ void k_cg_rz(Grid g, const T* r, const T* z, CgState* st, double* part) {
+  if (st->done) return;
+  __shared__ double sh[32];
+  double rz = 0.0;
+  PL_GRID_STRIDE(k, g.nint) {
+    int cx, cy, cz;
+    const int i = interior_cell(g, k, cx, cy, cz);
+    rz += (double)r[i] * (double)z[i];
+  }
+  const double s = block_sum(rz, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (arrive_last(&st->ticket[0])) {
+    const double t = sum_partials(part, sh);
+    if (threadIdx.x == 0) {
+      st->deltaOld = st->deltaNew;
+      st->deltaNew = t;
+      st->beta = t / st->deltaOld;
+      st->iter += 1;
+      if (st->criterion == 0) {
+        const double relative = fabs((st->maxR - st->oldMaxR) / st->oldMaxR);
+        if (relative < 1e-7) st->done = 2;            // stagnation bail
+        if (!(st->maxR > st->tol)) st->converged = 1;  // loop condition
+      }
+      if (st->converged || st->iter >= st->max_iters) st->done = st->done ? st->done : 1;
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// Iteration part 4 (lines 995-997): d = d*beta + z.  Runs even when the step
+// above ended the loop; the reference updates d before its exit tests too.
+template <typename T>
+__global__ void k_cg_dir(Grid g, const T* z, T* d, const CgState* st, int skip_if_done) {
+  if (skip_if_done && st->done) return;
+  const T beta = (T)st->beta;
+  PL_GRID_STRIDE(k, g.nint) {
+    int cx, cy, cz;
+    const int i = interior_cell(g, k, cx, cy, cz);
+    d[i] = d[i] * beta + z[i];
+  }
+}
+
+}  // namespace plume

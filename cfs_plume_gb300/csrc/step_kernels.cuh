@@ -1,0 +1,492 @@
+// step_kernels.cuh -- the non-solver stages of FLUID_3D_MIC::step as CUDA
+// kernels, templated on the field type T (double: parity mode, compiled
+// without multiply-add contraction so each cell reproduces the reference's
+// rounding; float: performance mode).
+//
+// Storage is SoA: a vector field is three planes x[N], y[N], z[N]; scalars are
+// one plane.  Interior obstacles are not supported (the plume path has none:
+// obstacles are the wall slabs set from the six BC flags,
+// FLUID_3D_MIC.cpp:105-159), so the obstacle tests of the reference reduce to
+// index tests on the grid faces.
+#pragma once
+#include "common.cuh"
+
+namespace plume {
+
+template <typename T>
+struct V3 {
+  T* x;
+  T* y;
+  T* z;
+};
+
+// Per-step scalar constants, each evaluated in double exactly as the reference
+// evaluates it and rounded once to T.
+template <typename T>
+struct StepConsts {
+  T dt;          // _dt
+  T beta;        // _buoyancy
+  T eps;         // _vorticityEps
+  T dx;          // _dx = 1/maxRes
+  T gridSize;    // 0.5f/_dx   (FLUID_3D_MIC.cpp:529)
+  T oneOverDx;   // 1.0f/_dx   (one-sided vorticity differences, and invDx of project)
+  T dt0;         // _dt/_dx    (advectStam, FLUID_3D_MIC.cpp:622)
+  T divc;        // -_dx*0.5f  (project, FLUID_3D_MIC.cpp:354)
+  T wMinus;      // 1 - w      (damping, FLUID_3D_MIC.cpp:1262)
+  T sixth;       // w/6
+  T xHi, yHi, zHi;  // res - 2.5: upper advection clamps
+  int has_vort;  // eps > 0
+  int has_beta;  // beta != 0
+};
+
+// ---------------------------------------------------------------- sources
+// Box source: density = heat = 1 + noise*(2u-1) on [lo, hi).
+template <typename T>
+__global__ void k_source_box(T* dens, T* heat, Grid g, int x0, int y0, int z0, int bx, int by,
+                             int bz, uint64_t seed, int step, double noise) {
+  const int n = bx * by * bz;
+  PL_GRID_STRIDE(i, n) {
+    const int x = x0 + i % bx;
+    const int t = i / bx;
+    const int y = y0 + t % by;
+    const int z = z0 + t / by;
+    const int64_t c = x + (int64_t)y * g.X + (int64_t)z * g.slab;
+    const T v = (T)source_value(seed, step, c, noise);
+    dens[c] = v;
+    heat[c] = v;
+  }
+}
+
+// Box source with host-supplied values (x fastest over the box).
+template <typename T>
+__global__ void k_source_box_values(T* dens, T* heat, Grid g, int x0, int y0, int z0, int bx,
+                                    int by, int bz, const T* vals) {
+  const int n = bx * by * bz;
+  PL_GRID_STRIDE(i, n) {
+    const int x = x0 + i % bx;
+    const int t = i / bx;
+    const int y = y0 + t % by;
+    const int z = z0 + t / by;
+    const int64_t c = x + (int64_t)y * g.X + (int64_t)z * g.slab;
+    dens[c] = vals[i];
+    heat[c] = vals[i];
+  }
+}
+
+// Column source (FLUID_3D_MIC::addSmokeTestCase): the cell list is computed
+// once on the host with the reference's float arithmetic.
+template <typename T>
+__global__ void k_source_list(T* dens, T* heat, const int* cells, int n) {
+  PL_GRID_STRIDE(i, n) {
+    const int c = cells[i];
+    dens[c] = T(1);
+    heat[c] = T(1);
+  }
+}
+
+// ------------------------------------------------ step start: walls + buoyancy
+// FLUID_3D_MIC::step lines 188-199: force.clear, velocity/density
+// setZeroBorder, addBuoyancy (force.y = beta*heat), velocity += force*dt,
+// prevorticity = velocity.
+template <typename T>
+__global__ void k_forces(Grid g, V3<T> vel, T* dens, const T* heat, V3<T> prevort,
+                         StepConsts<T> c, int cache) {
+  PL_GRID_STRIDE(i, g.N) {
+    const int x = i % g.X;
+    const int t = i / g.X;
+    const int y = t % g.Y;
+    const int z = t / g.Y;
+    T vx = vel.x[i], vy = vel.y[i], vz = vel.z[i];
+    if (on_border(g, x, y, z)) {
+      vx = vy = vz = T(0);
+      dens[i] = T(0);
+    }
+    if (c.has_beta) {
+      const T fy = c.beta * heat[i];
+      vy = vy + fy * c.dt;
+    }
+    vel.x[i] = vx;
+    vel.y[i] = vy;
+    vel.z[i] = vz;
+    if (cache) {
+      prevort.x[i] = vx;
+      prevort.y[i] = vy;
+      prevort.z[i] = vz;
+    }
+  }
+}
+
+// ------------------------------------------------------- vorticity confinement
+// Neighbour choice of FLUID_3D_MIC::addVorticity (lines 533-545): one-sided at
+// the first and last interior index of each axis (the obstacle test there is
+// true exactly on those cells, since only wall slabs are obstacles).
+struct VortStencil {
+  int up, down, out, in, right, left;
+  bool oy, oz, ox;  // one-sided along y, z, x
+};
+__device__ inline VortStencil vort_stencil(const Grid& g, int i, int x, int y, int z) {
+  VortStencil s;
+  s.up = (y == g.Y - 2) ? i : i + g.X;
+  s.down = (y == 1) ? i : i - g.X;
+  s.out = (z == g.Z - 2) ? i : i + g.slab;
+  s.in = (z == 1) ? i : i - g.slab;
+  s.right = (x == g.X - 2) ? i : i + 1;
+  s.left = (x == 1) ? i : i - 1;
+  s.oy = (s.up == i || s.down == i);
+  s.oz = (s.out == i || s.in == i);
+  s.ox = (s.left == i || s.right == i);
+  return s;
+}
+
+// Pass 1: vorticity = curl(velocity) on the interior (lines 530-547) and
+// |vorticity| on every cell (VECTOR3_FIELD_3D::magnitudeField, 353-361).
+template <typename T>
+__global__ void k_vort1(Grid g, V3<T> v, V3<T> w, T* mag, StepConsts<T> c) {
+  PL_GRID_STRIDE(i, g.N) {
+    const int x = i % g.X;
+    const int t = i / g.X;
+    const int y = t % g.Y;
+    const int z = t / g.Y;
+    T wx, wy, wz;
+    if (!on_border(g, x, y, z)) {
+      const VortStencil s = vort_stencil(g, i, x, y, z);
+      const T dy = s.oy ? c.oneOverDx : c.gridSize;
+      const T dz = s.oz ? c.oneOverDx : c.gridSize;
+      const T dx = s.ox ? c.oneOverDx : c.gridSize;
+      wx = (v.z[s.up] - v.z[s.down]) * dy + (-v.y[s.out] + v.y[s.in]) * dz;
+      wy = (v.x[s.out] - v.x[s.in]) * dz + (-v.z[s.right] + v.z[s.left]) * dx;
+      wz = (v.y[s.right] - v.y[s.left]) * dx + (-v.x[s.up] + v.x[s.down]) * dy;
+      w.x[i] = wx;
+      w.y[i] = wy;
+      w.z[i] = wz;
+    } else {
+      wx = w.x[i];
+      wy = w.y[i];
+      wz = w.z[i];
+    }
+    mag[i] = sqrt(wx * wx + wy * wy + wz * wz);
+  }
+}
+
+// Pass 2: N = grad|w| / |grad|w||, force = eps*dx*(N x w) on the interior
+// (lines 552-589), then velocity += force*dt (line 202).
+template <typename T>
+__global__ void k_vort2(Grid g, V3<T> vel, V3<T> w, const T* mag, V3<T> force,
+                        StepConsts<T> c, int cache) {
+  PL_GRID_STRIDE(i, g.N) {
+    const int x = i % g.X;
+    const int t = i / g.X;
+    const int y = t % g.Y;
+    const int z = t / g.Y;
+    T fx = T(0), fy = T(0), fz = T(0);
+    bool has_f = false;
+    if (!on_border(g, x, y, z)) {
+      const VortStencil s = vort_stencil(g, i, x, y, z);
+      const T dy = s.oy ? c.oneOverDx : c.gridSize;
+      const T dz = s.oz ? c.oneOverDx : c.gridSize;
+      const T dx = s.ox ? c.oneOverDx : c.gridSize;
+      T N0 = (mag[s.right] - mag[s.left]) * dx;
+      T N1 = (mag[s.up] - mag[s.down]) * dy;
+      T N2 = (mag[s.out] - mag[s.in]) * dz;
+      T m = sqrt(N0 * N0 + N1 * N1 + N2 * N2);
+      if (m > T(0)) {
+        m = T(1) / m;
+        N0 *= m;
+        N1 *= m;
+        N2 *= m;
+        const T wx = w.x[i], wy = w.y[i], wz = w.z[i];
+        fx = (N1 * wz - N2 * wy) * c.dx * c.eps;
+        fy = -((N0 * wz - N2 * wx) * c.dx * c.eps);
+        fz = (N0 * wy - N1 * wx) * c.dx * c.eps;
+        has_f = true;
+      }
+    }
+    if (has_f) {
+      vel.x[i] = vel.x[i] + fx * c.dt;
+      vel.y[i] = vel.y[i] + fy * c.dt;
+      vel.z[i] = vel.z[i] + fz * c.dt;
+    }
+    if (cache) {
+      force.x[i] = fx;
+      force.y[i] = fy;
+      force.z[i] = fz;
+    }
+  }
+}
+
+// ----------------------------------------------------------- face conditions
+// One component per pair of faces: mode 0 zero (setZeroX/Y/Z), 1 copy from one
+// cell in (copyBorderX/Y/Z), 2 copy from two cells in (setNeumannX/Y/Z)
+// (VECTOR3_FIELD_3D.cpp:2872-3053).  Each face writes only its own axis's
+// component and reads that component from a cell no face of the same axis
+// writes, so all six faces run in one launch.  Threads enumerate the cells of
+// the x faces, then the y faces, then the z faces.
+template <typename T>
+__global__ void k_face_bc(Grid g, V3<T> v, int mode_x, int mode_y, int mode_z) {
+  const int nxf = 2 * g.Y * g.Z, nyf = 2 * g.X * g.Z, nzf = 2 * g.X * g.Y;
+  PL_GRID_STRIDE(i, nxf + nyf + nzf) {
+    if (i < nxf) {
+      const int side = i & 1, r = i >> 1;
+      const int y = r % g.Y, z = r / g.Y;
+      const int x = side ? g.X - 1 : 0;
+      const int c = x + y * g.X + z * g.slab;
+      const int m = mode_x;
+      v.x[c] = (m == 0) ? T(0) : v.x[side ? c - m : c + m];
+    } else if (i < nxf + nyf) {
+      const int j = i - nxf;
+      const int side = j & 1, r = j >> 1;
+      const int x = r % g.X, z = r / g.X;
+      const int y = side ? g.Y - 1 : 0;
+      const int c = x + y * g.X + z * g.slab;
+      const int m = mode_y * g.X;
+      v.y[c] = (mode_y == 0) ? T(0) : v.y[side ? c - m : c + m];
+    } else {
+      const int j = i - nxf - nyf;
+      const int side = j & 1, r = j >> 1;
+      const int x = r % g.X, y = r / g.X;
+      const int z = side ? g.Z - 1 : 0;
+      const int c = x + y * g.X + z * g.slab;
+      const int m = mode_z * g.slab;
+      v.z[c] = (mode_z == 0) ? T(0) : v.z[side ? c - m : c + m];
+    }
+  }
+}
+
+// ---------------------------------------------------------------- advection
+// First-order semi-Lagrangian lookup of VECTOR3_FIELD_3D::advect
+// (VECTOR3_FIELD_3D.cpp:2001-2158): backtrace in index space by dt0*u, clamp
+// to [1.5, res-2.5], trilinear weights, evaluated in the reference's order.
+template <typename T>
+struct Trilinear {
+  int i000, i010, i100, i110, i001, i011, i101, i111;
+  T s0, s1, t0, t1, u0, u1;
+  __device__ inline T apply(const T* f) const {
+    return u0 * (s0 * (t0 * f[i000] + t1 * f[i010]) + s1 * (t0 * f[i100] + t1 * f[i110])) +
+           u1 * (s0 * (t0 * f[i001] + t1 * f[i011]) + s1 * (t0 * f[i101] + t1 * f[i111]));
+  }
+};
+
+template <typename T>
+__device__ inline Trilinear<T> backtrace(const Grid& g, const StepConsts<T>& c, V3<T> vo, int i,
+                                         int x, int y, int z) {
+  T xt = T(x) - c.dt0 * vo.x[i];
+  T yt = T(y) - c.dt0 * vo.y[i];
+  T zt = T(z) - c.dt0 * vo.z[i];
+  xt = (xt < T(1.5)) ? T(1.5) : xt;
+  xt = (xt > c.xHi) ? c.xHi : xt;
+  yt = (yt < T(1.5)) ? T(1.5) : yt;
+  yt = (yt > c.yHi) ? c.yHi : yt;
+  zt = (zt < T(1.5)) ? T(1.5) : zt;
+  zt = (zt > c.zHi) ? c.zHi : zt;
+  const int x0 = (int)xt, y0 = (int)yt, z0 = (int)zt;
+  const int x1 = x0 + 1, y1 = y0 + 1, z1 = z0 + 1;
+  Trilinear<T> w;
+  w.s1 = xt - T(x0);
+  w.s0 = T(1) - w.s1;
+  w.t1 = yt - T(y0);
+  w.t0 = T(1) - w.t1;
+  w.u1 = zt - T(z0);
+  w.u0 = T(1) - w.u1;
+  w.i000 = x0 + y0 * g.X + z0 * g.slab;
+  w.i010 = x0 + y1 * g.X + z0 * g.slab;
+  w.i100 = x1 + y0 * g.X + z0 * g.slab;
+  w.i110 = x1 + y1 * g.X + z0 * g.slab;
+  w.i001 = x0 + y0 * g.X + z1 * g.slab;
+  w.i011 = x0 + y1 * g.X + z1 * g.slab;
+  w.i101 = x1 + y0 * g.X + z1 * g.slab;
+  w.i111 = x1 + y1 * g.X + z1 * g.slab;
+  return w;
+}
+
+// advectStam after its first boundary pass (FLUID_3D_MIC.cpp:621-649): all
+// three fields advected with one backtrace per cell, then the border fix-up
+// (velocity.setZeroBorder, copyBorder on the open axes, density/heat
+// setZeroBorder) folded in: a border cell's final value along an open axis is
+// its interior neighbour's new value, which the border thread recomputes.
+// postadvection (the pre-fix-up velocity) is written when `cache` is set.
+template <typename T>
+__global__ void k_advect(Grid g, StepConsts<T> c, V3<T> vo, const T* dens_o, const T* heat_o,
+                         V3<T> vn, T* dens_n, T* heat_n, V3<T> postadv, int cache,
+                         int open_x, int open_y, int open_z) {
+  PL_GRID_STRIDE(i, g.N) {
+    const int x = i % g.X;
+    const int t = i / g.X;
+    const int y = t % g.Y;
+    const int z = t / g.Y;
+    const Trilinear<T> w = backtrace(g, c, vo, i, x, y, z);
+    const T ux = w.apply(vo.x), uy = w.apply(vo.y), uz = w.apply(vo.z);
+    if (cache) {
+      postadv.x[i] = ux;
+      postadv.y[i] = uy;
+      postadv.z[i] = uz;
+    }
+    if (!on_border(g, x, y, z)) {
+      dens_n[i] = w.apply(dens_o);
+      heat_n[i] = w.apply(heat_o);
+      vn.x[i] = ux;
+      vn.y[i] = uy;
+      vn.z[i] = uz;
+    } else {
+      dens_n[i] = T(0);
+      heat_n[i] = T(0);
+      const bool yin = (y >= 1 && y <= g.Y - 2), zin = (z >= 1 && z <= g.Z - 2),
+                 xin = (x >= 1 && x <= g.X - 2);
+      T bx = T(0), by = T(0), bz = T(0);
+      if (open_x && (x == 0 || x == g.X - 1) && yin && zin) {
+        const int nx = (x == 0) ? 1 : g.X - 2;
+        const int n = nx + y * g.X + z * g.slab;
+        bx = backtrace(g, c, vo, n, nx, y, z).apply(vo.x);
+      }
+      if (open_y && (y == 0 || y == g.Y - 1) && xin && zin) {
+        const int ny = (y == 0) ? 1 : g.Y - 2;
+        const int n = x + ny * g.X + z * g.slab;
+        by = backtrace(g, c, vo, n, x, ny, z).apply(vo.y);
+      }
+      if (open_z && (z == 0 || z == g.Z - 1) && xin && yin) {
+        const int nz = (z == 0) ? 1 : g.Z - 2;
+        const int n = x + y * g.X + nz * g.slab;
+        bz = backtrace(g, c, vo, n, x, y, nz).apply(vo.z);
+      }
+      vn.x[i] = bx;
+      vn.y[i] = by;
+      vn.z[i] = bz;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ damping
+// The peeled damping product (buildPeeledDampingMatrixFull, FLUID_3D_MIC.cpp:
+// 1251-1306, applied through SPARSE_MATRIX operator*, SPARSE_MATRIX.cpp:83-105):
+// out = (1-w) v + (w/6) * (existing peeled neighbours), summed in the map's
+// column order z-1, y-1, x-1, self, x+1, y+1, z+1.  Border cells pass through.
+// Out of place; `preproj` receives a copy of the result when caching.
+template <typename T>
+__device__ inline T damp1(const Grid& g, const T* v, int i, int x, int y, int z, T wm, T s6) {
+  T acc = T(0);
+  if (z != 1) acc += v[i - g.slab] * s6;
+  if (y != 1) acc += v[i - g.X] * s6;
+  if (x != 1) acc += v[i - 1] * s6;
+  acc += v[i] * wm;
+  if (x != g.X - 2) acc += v[i + 1] * s6;
+  if (y != g.Y - 2) acc += v[i + g.X] * s6;
+  if (z != g.Z - 2) acc += v[i + g.slab] * s6;
+  return acc;
+}
+
+template <typename T>
+__global__ void k_damping(Grid g, StepConsts<T> c, V3<T> vin, V3<T> vout, V3<T> preproj,
+                          int cache) {
+  PL_GRID_STRIDE(i, g.N) {
+    const int x = i % g.X;
+    const int t = i / g.X;
+    const int y = t % g.Y;
+    const int z = t / g.Y;
+    T ox, oy, oz;
+    if (on_border(g, x, y, z)) {
+      ox = vin.x[i];
+      oy = vin.y[i];
+      oz = vin.z[i];
+    } else {
+      ox = damp1(g, vin.x, i, x, y, z, c.wMinus, c.sixth);
+      oy = damp1(g, vin.y, i, x, y, z, c.wMinus, c.sixth);
+      oz = damp1(g, vin.z, i, x, y, z, c.wMinus, c.sixth);
+    }
+    vout.x[i] = ox;
+    vout.y[i] = oy;
+    vout.z[i] = oz;
+    if (cache) {
+      preproj.x[i] = ox;
+      preproj.y[i] = oy;
+      preproj.z[i] = oz;
+    }
+  }
+}
+
+// --------------------------------------------------------------- projection
+// Divergence of FLUID_3D_MIC::project (lines 337-361) with the reflection at
+// wall neighbours, and p = 0 on the interior unless the previous pressure is
+// kept as the initial guess.
+template <typename T>
+__global__ void k_divergence(Grid g, StepConsts<T> c, V3<T> v, T* div, T* p, int keep_p) {
+  PL_GRID_STRIDE(k, g.nint) {
+    int x, y, z;
+    const int i = interior_cell(g, k, x, y, z);
+    T xright = v.x[i + 1], xleft = v.x[i - 1];
+    T yup = v.y[i + g.X], ydown = v.y[i - g.X];
+    T ztop = v.z[i + g.slab], zbottom = v.z[i - g.slab];
+    if (wall_xp(g, x)) xright = -v.x[i];
+    if (wall_xm(g, x)) xleft = -v.x[i];
+    if (wall_yp(g, y)) yup = -v.y[i];
+    if (wall_ym(g, y)) ydown = -v.y[i];
+    if (wall_zp(g, z)) ztop = -v.z[i];
+    if (wall_zm(g, z)) zbottom = -v.z[i];
+    div[i] = c.divc * (xright - xleft + yup - ydown + ztop - zbottom);
+    if (!keep_p) p[i] = T(0);
+  }
+}
+
+// FIELD_3D::copyBorderAll (FIELD_3D.cpp:1382-1420): z faces, then y faces, then
+// x faces.  Composed, every border cell takes the value of the cell with each
+// coordinate clamped into the interior.
+template <typename T>
+__global__ void k_copy_border_all(Grid g, T* p) {
+  const int nxf = 2 * g.Y * g.Z, nyf = 2 * g.X * g.Z, nzf = 2 * g.X * g.Y;
+  PL_GRID_STRIDE(i, nxf + nyf + nzf) {
+    int x, y, z;
+    if (i < nxf) {
+      const int r = i >> 1;
+      x = (i & 1) ? g.X - 1 : 0;
+      y = r % g.Y;
+      z = r / g.Y;
+    } else if (i < nxf + nyf) {
+      const int j = i - nxf, r = j >> 1;
+      y = (j & 1) ? g.Y - 1 : 0;
+      x = r % g.X;
+      z = r / g.X;
+    } else {
+      const int j = i - nxf - nyf, r = j >> 1;
+      z = (j & 1) ? g.Z - 1 : 0;
+      x = r % g.X;
+      y = r / g.X;
+    }
+    const int cx = x < 1 ? 1 : (x > g.X - 2 ? g.X - 2 : x);
+    const int cy = y < 1 ? 1 : (y > g.Y - 2 ? g.Y - 2 : y);
+    const int cz = z < 1 ? 1 : (z > g.Z - 2 ? g.Z - 2 : z);
+    p[x + y * g.X + z * g.slab] = p[cx + cy * g.X + cz * g.slab];
+  }
+}
+
+// Pressure-gradient subtraction (lines 372-398): central differences, one-sided
+// at the first and last interior index of each axis.
+template <typename T>
+__global__ void k_gradient(Grid g, StepConsts<T> c, V3<T> v, const T* p) {
+  PL_GRID_STRIDE(k, g.nint) {
+    int x, y, z;
+    const int i = interior_cell(g, k, x, y, z);
+    const T inv = c.oneOverDx;
+    T gx, gy, gz;
+    if (x == 1)
+      gx = (p[i + 1] - p[i]) * inv;
+    else if (x == g.X - 2)
+      gx = (p[i] - p[i - 1]) * inv;
+    else
+      gx = T(0.5) * (p[i + 1] - p[i - 1]) * inv;
+    if (y == 1)
+      gy = (p[i + g.X] - p[i]) * inv;
+    else if (y == g.Y - 2)
+      gy = (p[i] - p[i - g.X]) * inv;
+    else
+      gy = T(0.5) * (p[i + g.X] - p[i - g.X]) * inv;
+    if (z == 1)
+      gz = (p[i + g.slab] - p[i]) * inv;
+    else if (z == g.Z - 2)
+      gz = (p[i] - p[i - g.slab]) * inv;
+    else
+      gz = T(0.5) * (p[i + g.slab] - p[i - g.slab]) * inv;
+    v.x[i] = v.x[i] - gx;
+    v.y[i] = v.y[i] - gy;
+    v.z[i] = v.z[i] - gz;
+  }
+}
+
+}  // namespace plume

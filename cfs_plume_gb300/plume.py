@@ -1,0 +1,303 @@
+"""Python binding of libplume (ctypes over include/plume.h).
+
+`FLUID_3D_MIC` mirrors the public surface of the reference class
+(src/integrators/FLUID_3D_MIC.h:37-120): construct with the resolution and the
+six boundary flags, set `vorticityEps`/`buoyancy`, then per step
+`addSmokeColumn()` (or `add_source(step)`), `step()`, `writeGz(path)`,
+`appendStreams()`.  Field accessors return NumPy copies in the reference
+layout (vector fields as (N, 3) arrays of doubles).
+
+The compute runs in the CUDA library; there is no CPU fallback.  Loading fails
+with an error when cfs_plume_gb300/lib/libplume.so has not been built.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import PlumeParams, PlumeStepStats
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libplume.so")
+_lib = None
+
+
+class PlumeError(RuntimeError):
+    def __init__(self, status, detail):
+        self.status = status
+        super().__init__("plume error %d (%s): %s" % (status, _strerror(status), detail))
+
+
+def load_library(path=LIB_PATH):
+    """Load libplume.so and declare its signatures (idempotent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("libplume.so not built (%s); run `python -m cfs_plume_gb300.build`" % path)
+    lib = C.CDLL(path)
+    H = C.c_void_p
+    P = C.POINTER
+    sig = {
+        "plume_default_params": (None, [P(PlumeParams)]),
+        "plume_create": (C.c_int, [P(PlumeParams), P(H)]),
+        "plume_destroy": (None, [H]),
+        "plume_add_source": (C.c_int, [H, C.c_int32]),
+        "plume_step": (C.c_int, [H, P(PlumeStepStats)]),
+        "plume_add_source_values": (C.c_int, [H, C.c_void_p, C.c_size_t]),
+        "plume_run_timed": (C.c_int, [H, C.c_int32, C.c_int32, P(C.c_double), P(PlumeStepStats)]),
+        "plume_run": (C.c_int, [H, C.c_int32, C.c_int32, P(PlumeStepStats)]),
+        "plume_download": (C.c_int, [H, C.c_int32, C.c_void_p, C.c_size_t]),
+        "plume_upload": (C.c_int, [H, C.c_int32, C.c_void_p, C.c_size_t]),
+        "plume_download_obstacles": (C.c_int, [H, C.c_void_p, C.c_size_t]),
+        "plume_get_info": (C.c_int, [H, P(C.c_int32), P(C.c_int32), P(C.c_double), P(C.c_double)]),
+        "plume_write_state": (C.c_int, [H, C.c_char_p]),
+        "plume_append_streams": (C.c_int, [H, C.c_char_p]),
+        "plume_strerror": (C.c_char_p, [C.c_int]),
+        "plume_last_error": (C.c_char_p, [H]),
+        "plume_solve_poisson": (C.c_int, [H, C.c_void_p, C.c_void_p, P(PlumeStepStats)]),
+        "plume_mic_apply": (C.c_int, [H, C.c_void_p, C.c_void_p, C.c_void_p]),
+        "plume_mic_diagonal": (C.c_int, [H, C.c_void_p]),
+        "plume_sync": (C.c_int, [H]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _strerror(status):
+    try:
+        return load_library().plume_strerror(status).decode()
+    except Exception:  # library not loadable: plain number
+        return str(status)
+
+
+def _check(rc, handle=None):
+    if rc != 0:
+        detail = load_library().plume_last_error(handle).decode(errors="replace")
+        raise PlumeError(rc, detail)
+
+
+class Plume:
+    """One simulation on one GPU (a plume_handle)."""
+
+    def __init__(self, params: PlumeParams):
+        self.lib = load_library()
+        self.params = params
+        h = C.c_void_p()
+        _check(self.lib.plume_create(C.byref(params), C.byref(h)))
+        self.h = h
+        self.res = tuple(params.res)
+        self.N = self.res[0] * self.res[1] * self.res[2]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.plume_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def add_source(self, step_index):
+        _check(self.lib.plume_add_source(self.h, step_index), self.h)
+
+    def add_source_values(self, values):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        _check(self.lib.plume_add_source_values(self.h, v.ctypes.data, v.size), self.h)
+
+    def run_timed(self, first_step, n, stats=True):
+        """n steps between CUDA events on the handle's stream: (ms, stats)."""
+        ms = C.c_double()
+        arr = (PlumeStepStats * n)() if stats else None
+        _check(self.lib.plume_run_timed(self.h, first_step, n, C.byref(ms), arr), self.h)
+        return ms.value, (list(arr) if stats else None)
+
+    def step(self, stats=True):
+        st = PlumeStepStats()
+        _check(self.lib.plume_step(self.h, C.byref(st) if stats else None), self.h)
+        return st if stats else None
+
+    def run(self, first_step, n, stats=False):
+        arr = (PlumeStepStats * n)() if stats else None
+        _check(self.lib.plume_run(self.h, first_step, n, arr), self.h)
+        return list(arr) if stats else None
+
+    def field(self, name):
+        fid = _abi.FIELD_ID[name]
+        vec = name in _abi.VECTOR_FIELDS
+        a = np.empty(3 * self.N if vec else self.N, dtype=np.float64)
+        _check(self.lib.plume_download(self.h, fid, a.ctypes.data, a.size), self.h)
+        return a
+
+    def set_field(self, name, values):
+        a = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        _check(self.lib.plume_upload(self.h, _abi.FIELD_ID[name], a.ctypes.data, a.size), self.h)
+
+    def obstacles(self):
+        a = np.empty(self.N, dtype=np.uint8)
+        _check(self.lib.plume_download_obstacles(self.h, a.ctypes.data, a.size), self.h)
+        return a
+
+    def info(self):
+        res = (C.c_int32 * 3)()
+        ts, tt, dx = C.c_int32(), C.c_double(), C.c_double()
+        _check(self.lib.plume_get_info(self.h, res, C.byref(ts), C.byref(tt), C.byref(dx)), self.h)
+        return dict(res=tuple(res), total_steps=ts.value, total_time=tt.value, dx=dx.value)
+
+    def write_state(self, path):
+        _check(self.lib.plume_write_state(self.h, os.fsencode(path)), self.h)
+
+    def append_streams(self, directory):
+        d = directory if directory.endswith("/") else directory + "/"
+        _check(self.lib.plume_append_streams(self.h, os.fsencode(d)), self.h)
+
+    def solve_poisson(self, b, x0=None):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(self.N) if x0 is None else np.array(x0, dtype=np.float64)
+        st = PlumeStepStats()
+        _check(self.lib.plume_solve_poisson(self.h, b.ctypes.data, x.ctypes.data, C.byref(st)), self.h)
+        return x, st
+
+    def mic_apply(self, r):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = np.zeros(self.N)
+        q = np.zeros(self.N)
+        _check(self.lib.plume_mic_apply(self.h, r.ctypes.data, z.ctypes.data, q.ctypes.data), self.h)
+        return z, q
+
+    def mic_diagonal(self):
+        p = np.zeros(self.N)
+        _check(self.lib.plume_mic_diagonal(self.h, p.ctypes.data), self.h)
+        return p
+
+
+class FLUID_3D_MIC:
+    """Facade with the reference class's names (FLUID_3D_MIC.h:37-120).
+
+    The device state is created on first use so that `vorticityEps` and
+    `buoyancy` can be assigned after construction, as fluid3D.cpp:346 does.
+    """
+
+    def __init__(self, xRes, yRes, zRes, amplify=4, boundaries=None, **params):
+        kw = dict(res=(xRes, yRes, zRes))
+        if boundaries is not None:
+            kw["bc"] = tuple(boundaries)
+        kw.update(params)
+        self._params = _abi.default_params(**kw)
+        self._plume = None
+        self._source_step = 0
+        self.snapshotPath = ""
+
+    # reference accessors that are assignable (Real& vorticityEps(), buoyancy())
+    @property
+    def vorticityEps(self):
+        return self._params.vorticity_eps
+
+    @vorticityEps.setter
+    def vorticityEps(self, v):
+        self._require_fresh()
+        self._params.vorticity_eps = float(v)
+
+    @property
+    def buoyancy(self):
+        return self._params.buoyancy
+
+    @buoyancy.setter
+    def buoyancy(self, v):
+        self._require_fresh()
+        self._params.buoyancy = float(v)
+
+    def _require_fresh(self):
+        if self._plume is not None:
+            raise RuntimeError("parameters must be set before the first step")
+
+    @property
+    def plume(self):
+        if self._plume is None:
+            self._plume = Plume(self._params)
+        return self._plume
+
+    def xRes(self):
+        return self._params.res[0]
+
+    def yRes(self):
+        return self._params.res[1]
+
+    def zRes(self):
+        return self._params.res[2]
+
+    def dx(self):
+        return self.plume.info()["dx"]
+
+    def addSmokeColumn(self):
+        self.plume.add_source(self._source_step)
+        self._source_step += 1
+
+    def step(self):
+        return self.plume.step()
+
+    def writeGz(self, filename):
+        self.plume.write_state(filename)
+
+    def appendStreams(self):
+        if not self.snapshotPath:
+            raise RuntimeError("snapshotPath is empty")
+        self.plume.append_streams(self.snapshotPath)
+
+    def _vec(self, name):
+        return self.plume.field(name).reshape(-1, 3)
+
+    def velocity(self):
+        return self._vec("velocity")
+
+    def velocityOld(self):
+        return self._vec("velocityOld")
+
+    def force(self):
+        return self._vec("force")
+
+    def vorticity(self):
+        return self._vec("vorticity")
+
+    def density(self):
+        return self.plume.field("density")
+
+    def pressure(self):
+        return self.plume.field("pressure")
+
+    def divergence(self):
+        return self.plume.field("divergence")
+
+    def preprojection(self):
+        return self._vec("preprojection")
+
+    def prediffusion(self):
+        return self._vec("prediffusion")
+
+    def prevorticity(self):
+        return self._vec("prevorticity")
+
+    def preadvection(self):
+        return self._vec("preadvection")
+
+    def postadvection(self):
+        return self._vec("postadvection")
+
+    def cachedQuadratic(self):
+        return self._vec("cachedQuadratic")
+
+    def cachedPressure(self):
+        return self.plume.field("cachedPressure")
+
+    def cachedDivergence(self):
+        return self.plume.field("cachedDivergence")

@@ -1,0 +1,125 @@
+"""Generate the golden fixtures under tests/golden/ from the reference itself.
+
+Runs oracle/_ref/fluid3d_ref -- the reference's own FLUID_3D_MIC.cpp, compiled
+unmodified by `make -C oracle ref` (headless driver in oracle/ref/) -- on small
+configurations and stores what it produced:
+
+  ref_<case>.npz        every state field after the last step (read back with
+                        the reference's own FLUID_3D_MIC::readGz) and the PCG
+                        iteration count of every step;
+  ref_cfg1_sampled.npz  the 48x64x48 plume (box source, closed box, FP64,
+                        reference criterion 1e-10), 3 steps: iteration counts,
+                        per-field sums / L2 norms and every 97th value;
+  ref_state_8x10x6/     the reference's own state file (writeGz, gzip level 1)
+                        and appendStreams output after 2 steps, as format
+                        fixtures.
+
+Needs the reference tree (PLUME_REFERENCE_DIR, default /root/reference) and
+writes nothing outside tests/golden/.  Usage: python tests/golden/make_golden.py
+"""
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from cfs_plume_gb300 import _abi  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref", "fluid3d_ref")
+
+# name -> (params kwargs, steps, reference source mode)
+CASES = {
+    "default_16x20x12": (dict(res=(16, 20, 12)), 6, "column"),
+    "vort2_16x20x12": (dict(res=(16, 20, 12), vorticity_eps=2.0), 6, "column"),
+    "closed_box_17x23x13": (dict(res=(17, 23, 13), bc=(1, 1, 1, 1, 1, 1), vorticity_eps=1.0,
+                                 buoyancy=1.0, source=_abi.SRC_BOX, box_lo=(6, 2, 4),
+                                 box_hi=(11, 6, 9), source_noise=0.05, seed=7), 6, "box"),
+    "mixed_bc_16x20x12": (dict(res=(16, 20, 12), bc=(0, 1, 0, 1, 0, 1), vorticity_eps=0.5), 6,
+                          "column"),
+    "open_box_20x16x18": (dict(res=(20, 16, 18), bc=(0, 0, 0, 0, 0, 0), vorticity_eps=1.5,
+                               buoyancy=0.5, source=_abi.SRC_BOX, box_lo=(7, 1, 7),
+                               box_hi=(13, 4, 11), source_noise=0.05, seed=11), 5, "box"),
+}
+
+
+def ref_args(p, steps, src, out):
+    a = [REF, "run", "res=%d,%d,%d" % tuple(p.res), "bc=" + ",".join(str(b) for b in p.bc),
+         "vorticity=%r" % p.vorticity_eps, "steps=%d" % steps, "out=%s/" % out, "dump=1",
+         "source=" + src]
+    if src == "box":
+        a += ["box=%d,%d,%d,%d,%d,%d" % (tuple(p.box_lo) + tuple(p.box_hi)),
+              "noise=%r" % p.source_noise, "seed=%d" % p.seed]
+    if p.buoyancy != _abi.BUOYANCY_REF:
+        a += ["buoyancy=%r" % p.buoyancy]
+    return a
+
+
+def run_ref(p, steps, src, extra=()):
+    d = tempfile.mkdtemp(prefix="plume_golden_")
+    r = subprocess.run(ref_args(p, steps, src, d) + list(extra), capture_output=True, text=True,
+                       check=True)
+    iters = [int(l.split()[0]) for l in r.stdout.splitlines() if "iterations converged" in l]
+    subprocess.run([REF, "readgz", d + "/final.fluid3d.gz", d + "/x"], check=True,
+                   capture_output=True)
+    fields = {n: np.fromfile(d + "/x.%s.f64" % n) for n in _abi.FIELDS}
+    fields["obstacles"] = np.fromfile(d + "/x.obstacles.u8", dtype=np.uint8)
+    return d, iters, fields
+
+
+def params_record(p):
+    return dict(res=np.array(p.res), bc=np.array(p.bc), buoyancy=p.buoyancy,
+                vorticity_eps=p.vorticity_eps, source=p.source, box_lo=np.array(p.box_lo),
+                box_hi=np.array(p.box_hi), source_noise=p.source_noise, seed=p.seed)
+
+
+def main():
+    if not os.path.exists(REF):
+        sys.exit("build the reference first: make -C oracle ref")
+    for name, (kw, steps, src) in CASES.items():
+        p = _abi.default_params(**kw)
+        d, iters, fields = run_ref(p, steps, src)
+        np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % name), iters=np.array(iters),
+                            steps=steps, **params_record(p), **fields)
+        shutil.rmtree(d)
+        print(name, "iters", iters)
+
+    # the benchmark plume at 48x64x48, summarised
+    res = (48, 64, 48)
+    p = _abi.plume_config(res, precision=_abi.PREC_FP64, criterion=_abi.CRIT_REFERENCE, tol=1e-10)
+    d, iters, fields = run_ref(p, 3, "box")
+    out = dict(iters=np.array(iters), steps=3, **params_record(p))
+    for n in _abi.FIELDS:
+        a = fields[n]
+        out["sum_" + n] = a.sum()
+        out["l2_" + n] = np.sqrt((a * a).sum())
+        out["sample_" + n] = a[::97].copy()
+    np.savez_compressed(os.path.join(HERE, "ref_cfg1_sampled.npz"), **out)
+    shutil.rmtree(d)
+    print("cfg1 iters", iters)
+
+    # format fixtures: the reference's own state file and streams
+    fx = os.path.join(HERE, "ref_state_8x10x6")
+    shutil.rmtree(fx, ignore_errors=True)
+    os.makedirs(fx)
+    p = _abi.default_params(res=(8, 10, 6), vorticity_eps=1.0)
+    d = tempfile.mkdtemp(prefix="plume_golden_")
+    subprocess.run(ref_args(p, 2, "column", d) + ["gz=1", "streams=1"], check=True,
+                   capture_output=True)
+    for f in sorted(os.listdir(d)):
+        if f.startswith("fluid.0001") or f.endswith(".dims") or f.endswith(".transpose"):
+            shutil.copy(os.path.join(d, f), fx)
+    subprocess.run([REF, "readgz", d + "/fluid.0001.fluid3d.gz", d + "/x"], check=True,
+                   capture_output=True)
+    fields = {n: np.fromfile(d + "/x.%s.f64" % n) for n in _abi.FIELDS}
+    np.savez_compressed(os.path.join(fx, "fields.npz"), **fields, **params_record(p))
+    shutil.rmtree(d)
+    print("format fixture:", sorted(os.listdir(fx)))
+
+
+if __name__ == "__main__":
+    main()
