@@ -8,6 +8,7 @@
 #pragma once
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <type_traits>
@@ -15,8 +16,10 @@
 
 #include "common.cuh"
 #include "engine.h"
+#include "skew_kernels.cuh"
 #include "solver_kernels.cuh"
 #include "step_kernels.cuh"
+#include "wave.cuh"
 
 namespace plume {
 
@@ -57,6 +60,35 @@ inline std::vector<int> column_cells(int X, int Y, int Z) {
         if (radius < 0.075f * xTotal) cells.push_back(x + y * X + z * X * Y);
       }
   return cells;
+}
+
+template <typename T, int C, bool EXACT>
+cudaError_t launch_wave_c(const WaveArgs<T>& a, int grid, size_t smem, cudaStream_t s) {
+  void (*kf)(WaveArgs<T>) = a.backward ? k_mic_wave<T, C, EXACT, true> : k_mic_wave<T, C, EXACT, false>;
+  static bool attr_set[2] = {false, false};
+  if (!attr_set[a.backward]) {
+    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_set[a.backward] = true;
+  }
+  kf<<<grid, 32 * (a.BZ + 1), smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+// MIC sweep dispatch on the cells-per-lane count C (1..8: up to 256 cells per row).
+template <typename T, bool EXACT>
+cudaError_t launch_wave(const WaveArgs<T>& a, int grid, size_t smem, cudaStream_t s) {
+  switch (a.k.C) {
+    case 1: return launch_wave_c<T, 1, EXACT>(a, grid, smem, s);
+    case 2: return launch_wave_c<T, 2, EXACT>(a, grid, smem, s);
+    case 3: return launch_wave_c<T, 3, EXACT>(a, grid, smem, s);
+    case 4: return launch_wave_c<T, 4, EXACT>(a, grid, smem, s);
+    case 5: return launch_wave_c<T, 5, EXACT>(a, grid, smem, s);
+    case 6: return launch_wave_c<T, 6, EXACT>(a, grid, smem, s);
+    case 7: return launch_wave_c<T, 7, EXACT>(a, grid, smem, s);
+    case 8: return launch_wave_c<T, 8, EXACT>(a, grid, smem, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 template <typename T>
@@ -159,6 +191,8 @@ class EngineT : public Engine {
     PL_TRY(build_mic_diagonal(g_, P64_, p.mic_tau, p.mic_sigma, s_));
     k_convert_precon<T><<<grid_for(g_.N), 256, 0, s_>>>(g_.N, P64_, P_);
     PL_CHECK_LAUNCH();
+    int rc = init_solver();
+    if (rc != PLUME_OK) return rc;
     PL_TRY(cudaStreamSynchronize(s_));
     return PLUME_OK;
   }
@@ -374,8 +408,23 @@ class EngineT : public Engine {
   int mic_apply(const double* r, double* z, double* q) override {
     int rc = put_plane(r_, r, 1, 0);
     if (rc != PLUME_OK) return rc;
-    rc = mic_sweeps(r_, qf_, z_, nullptr);
-    if (rc == PLUME_OK) rc = fetch_plane(z_, z, 1, 0);
+    // a fresh solver state so the sweeps are not skipped
+    PL_TRY(cudaMemsetAsync(st_, 0, sizeof(CgState), s_));
+    const int gK = grid_for(k_.total);
+    k_to_skew<T, T><<<gK, 256, 0, s_>>>(g_, k_, r_, sr_);
+    PL_CHECK_LAUNCH();
+    rc = mic_sweeps(sr_, sqf_, sz_);
+    if (rc != PLUME_OK) return rc;
+    PL_TRY(cudaMemsetAsync(z_, 0, (size_t)g_.N * sizeof(T), s_));
+    PL_TRY(cudaMemsetAsync(qf_, 0, (size_t)g_.N * sizeof(T), s_));
+    k_from_skew<T><<<gK, 256, 0, s_>>>(g_, k_, sz_, z_);
+    PL_CHECK_LAUNCH();
+    k_from_skew<T><<<gK, 256, 0, s_>>>(g_, k_, sqf_, qf_);
+    PL_CHECK_LAUNCH();
+    PL_TRY(cudaMemcpyAsync(st_host_, st_, sizeof(CgState), cudaMemcpyDeviceToHost, s_));
+    PL_TRY(cudaStreamSynchronize(s_));
+    if (st_host_->wave_err) return fail(PLUME_ERR_TIMEOUT, "MIC wavefront wait expired");
+    rc = fetch_plane(z_, z, 1, 0);
     if (rc == PLUME_OK && q) rc = fetch_plane(qf_, q, 1, 0);
     return rc;
   }
@@ -420,44 +469,119 @@ class EngineT : public Engine {
     c_.has_beta = p_.buoyancy != 0.0 ? 1 : 0;
   }
 
-  // MIC forward then backward sweep, one launch per hyperplane.
-  int mic_sweeps(const T* r, T* q, T* z, const CgState* st) {
-    const int planes = g_.nx + g_.ny + g_.nz - 2;
-    const int gp = grid_for((long long)g_.ny * g_.nz);
-    for (int s = 0; s < planes; s++) {
-      k_mic_fwd_plane<T><<<gp, 256, 0, s_>>>(g_, P_, r, q, s, st);
-      PL_CHECK_LAUNCH();
+  // ---------------------------------------------------------------- solver
+  // Skewed interior layout and wavefront configuration (wave.cuh).
+  int init_solver() {
+    k_.nx = g_.nx;
+    k_.ny = g_.ny;
+    k_.nz = g_.nz;
+    k_.C = (g_.nx + 31) / 32;
+    if (k_.C > 8) return fail(PLUME_ERR_UNSUPPORTED, "x resolution above 258 cells");
+    k_.W = 32 * k_.C;
+    k_.R = g_.ny + 31;
+    k_.plane = (long long)k_.R * k_.W;
+    k_.total = (long long)g_.nz * k_.plane;
+    if (k_.total >= (1ll << 31)) return fail(PLUME_ERR_UNSUPPORTED, "grid too large for the solver");
+    const size_t vb = align((size_t)k_.total * sizeof(T));
+    const size_t bytes = 8 * vb + align(4 * sizeof(unsigned)) + align((size_t)g_.nz * sizeof(int));
+    cudaError_t e = cudaMalloc(&spool_, bytes);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return fail(PLUME_ERR_OOM, "device allocation of the solver vectors failed");
     }
-    for (int s = planes - 1; s >= 0; s--) {
-      k_mic_bwd_plane<T><<<gp, 256, 0, s_>>>(g_, P_, q, z, s, st);
-      PL_CHECK_LAUNCH();
+    PL_TRY(cudaMemsetAsync(spool_, 0, bytes, s_));
+    char* cur = spool_;
+    T** v[] = {&sr_, &sd_, &sq_, &sz_, &sqf_, &sx_, &sb_, &sP_};
+    for (T** p : v) {
+      *p = (T*)cur;
+      cur += vb;
+    }
+    wave_ctl_ = (unsigned*)cur;
+    cur += align(4 * sizeof(unsigned));
+    wave_prog_ = (int*)cur;
+    k_to_skew<T, T><<<grid_for(k_.total), 256, 0, s_>>>(g_, k_, P_, sP_);
+    PL_CHECK_LAUNCH();
+    // slab height: as many planes per CTA as shared memory allows, up to 8
+    int dev = 0;
+    PL_TRY(cudaGetDevice(&dev));
+    PL_TRY(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
+    bz_ = 8;
+    while (bz_ > 1 && wave_smem_bytes<T>(bz_, k_.W) > 200 * 1024) bz_ /= 2;
+    if (const char* env = getenv("PLUME_WAVE_BZ")) {
+      const int b = atoi(env);
+      if (b >= 1 && b <= 16 && wave_smem_bytes<T>(b, k_.W) <= 227 * 1024) bz_ = b;
+    }
+    wave_k_ = 8;
+    if (const char* env = getenv("PLUME_WAVE_K")) {
+      const int kk = atoi(env);
+      if (kk >= 1 && kk <= 1024) wave_k_ = kk;
+    }
+    nslabs_ = (g_.nz + bz_ - 1) / bz_;
+    wave_smem_ = wave_smem_bytes<T>(bz_, k_.W);
+    wave_grid_ = nslabs_;  // slabs are handed out by ticket, so any grid size is safe
+    if (wave_grid_ > 2 * num_sms_) wave_grid_ = 2 * num_sms_;
+    if (const char* env = getenv("PLUME_WAVE_GRID")) {  // fewer CTAs than slabs: ticket loop
+      const int gcap = atoi(env);
+      if (gcap >= 1 && gcap < wave_grid_) wave_grid_ = gcap;
     }
     return PLUME_OK;
   }
 
-  // MIC-PCG on device (FLUID_3D_MIC.cpp:918-1015); x holds the initial guess.
+  WaveArgs<T> wave_args(const T* in, T* out, int backward) {
+    WaveArgs<T> a;
+    a.P = sP_;
+    a.in = in;
+    a.out = out;
+    a.k = k_;
+    a.BZ = bz_;
+    a.nslabs = nslabs_;
+    a.K = wave_k_;
+    a.backward = backward;
+    a.ctl = wave_ctl_;
+    a.progress = wave_prog_;
+    a.st = st_;
+    return a;
+  }
+
+  // MIC forward then backward sweep on skewed vectors (wavefront kernels).
+  int mic_sweeps(const T* r, T* q, T* z) {
+    constexpr bool exact = std::is_same<T, double>::value;
+    cudaError_t e = launch_wave<T, exact>(wave_args(r, q, 0), wave_grid_, wave_smem_, s_);
+    PL_TRY(e);
+    ++launches_;
+    e = launch_wave<T, exact>(wave_args(q, z, 1), wave_grid_, wave_smem_, s_);
+    PL_TRY(e);
+    ++launches_;
+    return PLUME_OK;
+  }
+
+  // MIC-PCG (FLUID_3D_MIC.cpp:918-1015); x (natural layout) holds the initial
+  // guess on entry and the solution on return, b is the natural right side.
   int solve_device(const T* b, T* x) {
-    const int crit = p_.criterion;
-    k_cg_init<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, b, x, r_, st_, part_, p_.tol,
-                                                     p_.max_iters, crit);
+    const int gK = grid_for(k_.total);
+    k_to_skew<T, T><<<gK, 256, 0, s_>>>(g_, k_, b, sb_);
     PL_CHECK_LAUNCH();
-    int rc = mic_sweeps(r_, qf_, z_, nullptr);
+    k_to_skew<T, T><<<gK, 256, 0, s_>>>(g_, k_, x, sx_);
+    PL_CHECK_LAUNCH();
+    k_cgs_init<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, k_, sb_, sx_, sr_, st_, part_, p_.tol,
+                                                      p_.max_iters, p_.criterion);
+    PL_CHECK_LAUNCH();
+    int rc = mic_sweeps(sr_, sqf_, sz_);
     if (rc != PLUME_OK) return rc;
-    k_cg_init2<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, r_, z_, d_, st_, part_);
+    k_cgs_init2<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sr_, sz_, sd_, st_, part_);
     PL_CHECK_LAUNCH();
-    const int gI = grid_for(g_.nint);
     int chunk = 4;
     for (int it = 0; it < p_.max_iters + chunk;) {
-      for (int k = 0; k < chunk; k++) {
-        k_cg_spmv<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, d_, q_ad_, st_, part_);
+      for (int kk = 0; kk < chunk; kk++) {
+        k_cgs_spmv<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, k_, sd_, sq_, st_, part_);
         PL_CHECK_LAUNCH();
-        k_cg_axpy<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, d_, q_ad_, x, r_, st_, part_);
+        k_cgs_axpy<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sd_, sq_, sx_, sr_, st_, part_);
         PL_CHECK_LAUNCH();
-        rc = mic_sweeps(r_, qf_, z_, st_);
+        rc = mic_sweeps(sr_, sqf_, sz_);
         if (rc != PLUME_OK) return rc;
-        k_cg_rz<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, r_, z_, st_, part_);
+        k_cgs_rz<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sr_, sz_, st_, part_);
         PL_CHECK_LAUNCH();
-        k_cg_dir<T><<<gI, 256, 0, s_>>>(g_, z_, d_, st_, 1);
+        k_cgs_dir<T><<<gK, 256, 0, s_>>>(k_, sz_, sd_, st_);
         PL_CHECK_LAUNCH();
       }
       it += chunk;
@@ -465,6 +589,15 @@ class EngineT : public Engine {
       PL_TRY(cudaStreamSynchronize(s_));
       if (st_host_->done) break;
       if (chunk < 16) chunk *= 2;
+    }
+    k_from_skew<T><<<gK, 256, 0, s_>>>(g_, k_, sx_, x);
+    PL_CHECK_LAUNCH();
+    PL_TRY(cudaMemcpyAsync(st_host_, st_, sizeof(CgState), cudaMemcpyDeviceToHost, s_));
+    PL_TRY(cudaStreamSynchronize(s_));
+    if (st_host_->wave_err) {
+      char buf[128];
+      snprintf(buf, sizeof(buf), "MIC wavefront wait expired (code %d)", st_host_->wave_err);
+      return fail(PLUME_ERR_TIMEOUT, buf);
     }
     return PLUME_OK;
   }
@@ -554,6 +687,7 @@ class EngineT : public Engine {
   void release() {
     if (s_) cudaStreamSynchronize(s_);
     if (pool_) cudaFree(pool_);
+    if (spool_) cudaFree(spool_);
     if (col_cells_) cudaFree(col_cells_);
     if (src_dev_) cudaFree(src_dev_);
     if (src_host_) cudaFreeHost(src_host_);
@@ -580,6 +714,15 @@ class EngineT : public Engine {
   T *r_ = nullptr, *d_ = nullptr, *q_ad_ = nullptr, *z_ = nullptr, *qf_ = nullptr, *P_ = nullptr;
   V3<T> vel_{}, vel_old_{}, spare_{}, prevort_{}, postadv_{}, preproj_{}, force_{}, vort_{};
   double* P64_ = nullptr;
+  // skewed solver vectors and wavefront configuration
+  Skew k_{};
+  char* spool_ = nullptr;
+  T *sr_ = nullptr, *sd_ = nullptr, *sq_ = nullptr, *sz_ = nullptr, *sqf_ = nullptr, *sx_ = nullptr,
+    *sb_ = nullptr, *sP_ = nullptr;
+  unsigned* wave_ctl_ = nullptr;
+  int* wave_prog_ = nullptr;
+  int bz_ = 8, wave_k_ = 8, nslabs_ = 1, wave_grid_ = 1, num_sms_ = 1;
+  size_t wave_smem_ = 0;
   uint8_t* obst_ = nullptr;
   CgState* st_ = nullptr;
   double* part_ = nullptr;

@@ -1,0 +1,238 @@
+// skew_kernels.cuh -- CG vector kernels on the skewed interior layout used by
+// the wavefront MIC sweeps (wave.cuh).  Same arithmetic as the
+// natural-layout kernels in solver_kernels.cuh (FLUID_3D_MIC.cpp:918-1015);
+// threads run over the stored elements row by row, so loads and stores are
+// contiguous; padding elements are kept at zero.
+#pragma once
+#include "solver_kernels.cuh"
+#include "wave.cuh"
+
+namespace plume {
+
+// Stored element e -> interior cell (ix, iy, iz); false for padding.
+__device__ inline bool skew_cell(const Skew& k, int e, int& ix, int& iy, int& iz) {
+  iz = e / (int)k.plane;
+  const int rem = e - iz * (int)k.plane;
+  const int s = rem / k.W;
+  ix = rem - s * k.W;
+  iy = s - ix / k.C;
+  return ix < k.nx && iy >= 0 && iy < k.ny;
+}
+
+__device__ inline int skew_at(const Skew& k, int ix, int iy, int iz) {
+  return iz * (int)k.plane + (iy + ix / k.C) * k.W + ix;
+}
+
+// multA (FLUID_3D_MIC.cpp:811-822) at interior cell (ix,iy,iz) in skewed
+// storage; neighbours outside the interior are border cells, which hold 0.
+template <typename T>
+__device__ inline T mult_a_skew(const Grid& g, const Skew& k, const T* v, int e, int ix, int iy,
+                                int iz) {
+  const int x = ix + 1, y = iy + 1, z = iz + 1;
+  const T vxm = ix > 0 ? v[skew_at(k, ix - 1, iy, iz)] : T(0);
+  const T vxp = ix + 1 < k.nx ? v[skew_at(k, ix + 1, iy, iz)] : T(0);
+  const T vym = iy > 0 ? v[e - k.W] : T(0);
+  const T vyp = iy + 1 < k.ny ? v[e + k.W] : T(0);
+  const T vzm = iz > 0 ? v[e - (int)k.plane] : T(0);
+  const T vzp = iz + 1 < k.nz ? v[e + (int)k.plane] : T(0);
+  return adiag<T>(g, x, y, z) * v[e] + vxm * coef<T>(wall_xm(g, x)) + vxp * coef<T>(wall_xp(g, x)) +
+         vym * coef<T>(wall_ym(g, y)) + vyp * coef<T>(wall_yp(g, y)) +
+         vzm * coef<T>(wall_zm(g, z)) + vzp * coef<T>(wall_zp(g, z));
+}
+
+// natural full grid -> skewed interior (padding zero)
+template <typename S, typename T>
+__global__ void k_to_skew(Grid g, Skew k, const S* nat, T* sk) {
+  PL_GRID_STRIDE(e, (int)k.total) {
+    int ix, iy, iz;
+    T v = T(0);
+    if (skew_cell(k, e, ix, iy, iz)) v = (T)nat[(ix + 1) + (iy + 1) * g.X + (iz + 1) * g.slab];
+    sk[e] = v;
+  }
+}
+
+// skewed interior -> natural full grid (interior cells only)
+template <typename T>
+__global__ void k_from_skew(Grid g, Skew k, const T* sk, T* nat) {
+  PL_GRID_STRIDE(e, (int)k.total) {
+    int ix, iy, iz;
+    if (skew_cell(k, e, ix, iy, iz)) nat[(ix + 1) + (iy + 1) * g.X + (iz + 1) * g.slab] = sk[e];
+  }
+}
+
+// set-up part 1: r = b - A x, b.b
+template <typename T>
+__global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState* st, double* part,
+                           double tol, int max_iters, int criterion) {
+  __shared__ double sh[32];
+  double bb = 0.0;
+  PL_GRID_STRIDE(e, (int)k.total) {
+    int ix, iy, iz;
+    T v = T(0);
+    if (skew_cell(k, e, ix, iy, iz)) {
+      const T bi = b[e];
+      v = bi - mult_a_skew(g, k, x, e, ix, iy, iz);
+      bb += (double)bi * (double)bi;
+    }
+    r[e] = v;
+  }
+  const double s = block_sum(bb, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (arrive_last(&st->ticket[0])) {
+    const double tot = sum_partials(part, sh);
+    if (threadIdx.x == 0) {
+      st->bb = tot;
+      st->tol = tol;
+      st->max_iters = max_iters;
+      st->criterion = criterion;
+      st->iter = 0;
+      st->done = 0;
+      st->converged = 0;
+      st->broke = 0;
+      st->wave_err = 0;
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// set-up part 2: d = z, deltaNew = r.z, loop entry test
+template <typename T>
+__global__ void k_cgs_init2(Skew k, const T* r, const T* z, T* d, CgState* st, double* part) {
+  __shared__ double sh[32];
+  double rz = 0.0, rr = 0.0;
+  PL_GRID_STRIDE(e, (int)k.total) {
+    const T zi = z[e], ri = r[e];
+    d[e] = zi;
+    rz += (double)ri * (double)zi;
+    rr += (double)ri * (double)ri;
+  }
+  const double s1 = block_sum(rz, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s1;
+  const double s2 = block_sum(rr, sh);
+  if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
+  if (arrive_last(&st->ticket[0])) {
+    const double trz = sum_partials(part, sh);
+    const double trr = sum_partials(part + kRedBlocks, sh);
+    if (threadIdx.x == 0) {
+      st->deltaNew = trz;
+      st->rr = trr;
+      if (st->wave_err) st->done = 3;
+      if (st->criterion == 0) {
+        st->maxR = 2.0 * st->tol;
+        if (!(st->maxR > st->tol) || st->max_iters <= 0) st->done = st->done ? st->done : 1;
+      } else {
+        if (sqrt(trr) <= st->tol * sqrt(st->bb)) {
+          st->done = st->done ? st->done : 1;
+          st->converged = 1;
+        }
+        if (st->max_iters <= 0) st->done = st->done ? st->done : 1;
+      }
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// iteration part 1: q = A d, alpha = deltaNew / d.q
+template <typename T>
+__global__ void k_cgs_spmv(Grid g, Skew k, const T* d, T* q, CgState* st, double* part) {
+  if (st->done) return;
+  __shared__ double sh[32];
+  double dq = 0.0;
+  PL_GRID_STRIDE(e, (int)k.total) {
+    int ix, iy, iz;
+    T v = T(0);
+    if (skew_cell(k, e, ix, iy, iz)) {
+      v = mult_a_skew(g, k, d, e, ix, iy, iz);
+      dq += (double)d[e] * (double)v;
+    }
+    q[e] = v;
+  }
+  const double s = block_sum(dq, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (arrive_last(&st->ticket[0])) {
+    const double t = sum_partials(part, sh);
+    if (threadIdx.x == 0) {
+      st->dq = t;
+      if (fabs(t) > 0.0) {
+        st->alpha = st->deltaNew / t;
+      } else {
+        st->done = 1;
+        st->broke = 1;
+      }
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// iteration part 2: x += alpha d, r -= alpha q, signed max(r), r.r
+template <typename T>
+__global__ void k_cgs_axpy(Skew k, const T* d, const T* q, T* x, T* r, CgState* st, double* part) {
+  if (st->done) return;
+  __shared__ double sh[32];
+  const T alpha = (T)st->alpha;
+  double mx = -1.0e308, rr = 0.0;
+  PL_GRID_STRIDE(e, (int)k.total) {
+    x[e] += alpha * d[e];
+    const T ri = r[e] + (-alpha) * q[e];
+    r[e] = ri;
+    mx = ((double)ri > mx) ? (double)ri : mx;
+    rr += (double)ri * (double)ri;
+  }
+  const double s1 = block_max(mx, sh, -1.0e308);
+  if (threadIdx.x == 0) part[blockIdx.x] = s1;
+  const double s2 = block_sum(rr, sh);
+  if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
+  if (arrive_last(&st->ticket[0])) {
+    const double tm = max_partials(part, sh);
+    const double trr = sum_partials(part + kRedBlocks, sh);
+    if (threadIdx.x == 0) {
+      st->oldMaxR = st->maxR;
+      st->maxR = tm > 0.0 ? tm : 0.0;
+      st->rr = trr;
+      if (st->criterion == 1 && sqrt(trr) <= st->tol * sqrt(st->bb)) {
+        st->iter += 1;
+        st->done = 1;
+        st->converged = 1;
+      }
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// iteration part 3: deltaNew = r.z, beta, exit tests
+template <typename T>
+__global__ void k_cgs_rz(Skew k, const T* r, const T* z, CgState* st, double* part) {
+  if (st->done) return;
+  __shared__ double sh[32];
+  double rz = 0.0;
+  PL_GRID_STRIDE(e, (int)k.total) rz += (double)r[e] * (double)z[e];
+  const double s = block_sum(rz, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (arrive_last(&st->ticket[0])) {
+    const double t = sum_partials(part, sh);
+    if (threadIdx.x == 0) {
+      st->deltaOld = st->deltaNew;
+      st->deltaNew = t;
+      st->beta = t / st->deltaOld;
+      st->iter += 1;
+      if (st->wave_err) st->done = 3;
+      if (st->criterion == 0) {
+        const double relative = fabs((st->maxR - st->oldMaxR) / st->oldMaxR);
+        if (relative < 1e-7) st->done = st->done ? st->done : 2;
+        if (!(st->maxR > st->tol)) st->converged = 1;
+      }
+      if (st->converged || st->iter >= st->max_iters) st->done = st->done ? st->done : 1;
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// iteration part 4: d = d*beta + z
+template <typename T>
+__global__ void k_cgs_dir(Skew k, const T* z, T* d, const CgState* st) {
+  if (st->done) return;
+  const T beta = (T)st->beta;
+  PL_GRID_STRIDE(e, (int)k.total) d[e] = d[e] * beta + z[e];
+}
+
+}  // namespace plume

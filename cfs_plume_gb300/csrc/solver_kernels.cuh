@@ -23,7 +23,7 @@ struct CgState {
   double dq;             // d.(A d)
   double tol;            // absolute (reference) or relative (rel2) tolerance
   int iter, max_iters, criterion, done;
-  int converged, broke, pad0, pad1;
+  int converged, broke, wave_err, pad1;
   unsigned int ticket[4];
 };
 
