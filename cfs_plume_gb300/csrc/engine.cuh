@@ -71,8 +71,68 @@ cudaError_t launch_wave_c(const WaveArgs<T>& a, int grid, size_t smem, cudaStrea
     if (e != cudaSuccess) return e;
     attr_set[a.backward] = true;
   }
-  kf<<<grid, 32 * (a.BZ + 1), smem, s>>>(a);
-  return cudaGetLastError();
+  // launched as explicit one-CTA clusters: the ring hand-off uses
+  // shared::cluster forms (st.async, cluster-scope barrier waits)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid, 1, 1);
+  cfg.blockDim = dim3(32 * (a.BZ + 2), 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 1;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kf, a);
+}
+
+template <typename T, int C, bool EXACT>
+cudaError_t launch_wave_cl_c(const WaveArgs<T>& a, size_t smem, cudaStream_t s, int query,
+                             int* max_clusters) {
+  void (*kf)(WaveArgs<T>) =
+      a.backward ? k_mic_wave_cl<T, C, EXACT, true> : k_mic_wave_cl<T, C, EXACT, false>;
+  static bool attr_set[2] = {false, false};
+  if (!attr_set[a.backward]) {
+    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(kf, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    attr_set[a.backward] = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(a.nslabs, 1, 1);
+  cfg.blockDim = dim3(32 * a.BZ, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = a.nslabs;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (query) return cudaOccupancyMaxActiveClusters(max_clusters, (void*)kf, &cfg);
+  return cudaLaunchKernelEx(&cfg, kf, a);
+}
+
+// Cluster wavefront (one cluster holds every slab of the plume); query != 0
+// only asks how many such clusters fit on the device.
+template <typename T, bool EXACT>
+cudaError_t launch_wave_cl(const WaveArgs<T>& a, size_t smem, cudaStream_t s, int query = 0,
+                           int* max_clusters = nullptr) {
+  switch (a.k.C) {
+    case 1: return launch_wave_cl_c<T, 1, EXACT>(a, smem, s, query, max_clusters);
+    case 2: return launch_wave_cl_c<T, 2, EXACT>(a, smem, s, query, max_clusters);
+    case 3: return launch_wave_cl_c<T, 3, EXACT>(a, smem, s, query, max_clusters);
+    case 4: return launch_wave_cl_c<T, 4, EXACT>(a, smem, s, query, max_clusters);
+    case 5: return launch_wave_cl_c<T, 5, EXACT>(a, smem, s, query, max_clusters);
+    case 6: return launch_wave_cl_c<T, 6, EXACT>(a, smem, s, query, max_clusters);
+    case 7: return launch_wave_cl_c<T, 7, EXACT>(a, smem, s, query, max_clusters);
+    case 8: return launch_wave_cl_c<T, 8, EXACT>(a, smem, s, query, max_clusters);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 // MIC sweep dispatch on the cells-per-lane count C (1..8: up to 256 cells per row).
@@ -516,6 +576,31 @@ class EngineT : public Engine {
       const int kk = atoi(env);
       if (kk >= 1 && kk <= 1024) wave_k_ = kk;
     }
+    // cluster path: every slab of the plume in one cluster of <= 16 CTAs
+    use_cluster_ = false;
+    {
+      int bzc = (g_.nz + 15) / 16;
+      if (bzc < 4) bzc = 4;
+      if (const char* env = getenv("PLUME_WAVE_CL_BZ")) {
+        const int b = atoi(env);
+        if (b >= 1 && b <= 16) bzc = b;
+      }
+      const char* off = getenv("PLUME_WAVE_NO_CLUSTER");
+      if (!(off && atoi(off) != 0) && bzc <= 16 && (g_.nz + bzc - 1) / bzc <= 16 &&
+          wave_smem_bytes<T>(bzc, k_.W) <= 227 * 1024) {
+        WaveArgs<T> q = wave_args(sr_, sqf_, 0);
+        q.BZ = bzc;
+        q.nslabs = (g_.nz + bzc - 1) / bzc;
+        int maxc = 0;
+        constexpr bool exact = std::is_same<T, double>::value;
+        cudaError_t e = launch_wave_cl<T, exact>(q, wave_smem_bytes<T>(bzc, k_.W), s_, 1, &maxc);
+        if (e == cudaSuccess && maxc >= 1) {
+          use_cluster_ = true;
+          bz_ = bzc;
+        }
+        (void)cudaGetLastError();
+      }
+    }
     nslabs_ = (g_.nz + bz_ - 1) / bz_;
     wave_smem_ = wave_smem_bytes<T>(bz_, k_.W);
     wave_grid_ = nslabs_;  // slabs are handed out by ticket, so any grid size is safe
@@ -546,10 +631,12 @@ class EngineT : public Engine {
   // MIC forward then backward sweep on skewed vectors (wavefront kernels).
   int mic_sweeps(const T* r, T* q, T* z) {
     constexpr bool exact = std::is_same<T, double>::value;
-    cudaError_t e = launch_wave<T, exact>(wave_args(r, q, 0), wave_grid_, wave_smem_, s_);
+    cudaError_t e = use_cluster_ ? launch_wave_cl<T, exact>(wave_args(r, q, 0), wave_smem_, s_)
+                                 : launch_wave<T, exact>(wave_args(r, q, 0), wave_grid_, wave_smem_, s_);
     PL_TRY(e);
     ++launches_;
-    e = launch_wave<T, exact>(wave_args(q, z, 1), wave_grid_, wave_smem_, s_);
+    e = use_cluster_ ? launch_wave_cl<T, exact>(wave_args(q, z, 1), wave_smem_, s_)
+                     : launch_wave<T, exact>(wave_args(q, z, 1), wave_grid_, wave_smem_, s_);
     PL_TRY(e);
     ++launches_;
     return PLUME_OK;
@@ -722,6 +809,7 @@ class EngineT : public Engine {
   unsigned* wave_ctl_ = nullptr;
   int* wave_prog_ = nullptr;
   int bz_ = 8, wave_k_ = 8, nslabs_ = 1, wave_grid_ = 1, num_sms_ = 1;
+  bool use_cluster_ = false;
   size_t wave_smem_ = 0;
   uint8_t* obst_ = nullptr;
   CgState* st_ = nullptr;

@@ -9,6 +9,10 @@
 
 namespace plume {
 
+// Per-thread partial sums are kept in the field type T (FP32 in FP32 mode:
+// GB300's FP64 rate is a small fraction of its FP32 rate, so one FP64 operation
+// per element would bound these kernels) and are promoted to FP64 for the
+// block and grid reductions, which run in a fixed order.
 // Stored element e -> interior cell (ix, iy, iz); false for padding.
 __device__ inline bool skew_cell(const Skew& k, int e, int& ix, int& iy, int& iz) {
   iz = e / (int)k.plane;
@@ -65,18 +69,18 @@ template <typename T>
 __global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState* st, double* part,
                            double tol, int max_iters, int criterion) {
   __shared__ double sh[32];
-  double bb = 0.0;
+  T bb = T(0);
   PL_GRID_STRIDE(e, (int)k.total) {
     int ix, iy, iz;
     T v = T(0);
     if (skew_cell(k, e, ix, iy, iz)) {
       const T bi = b[e];
       v = bi - mult_a_skew(g, k, x, e, ix, iy, iz);
-      bb += (double)bi * (double)bi;
+      bb += bi * bi;
     }
     r[e] = v;
   }
-  const double s = block_sum(bb, sh);
+  const double s = block_sum((double)bb, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (arrive_last(&st->ticket[0])) {
     const double tot = sum_partials(part, sh);
@@ -99,16 +103,16 @@ __global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState
 template <typename T>
 __global__ void k_cgs_init2(Skew k, const T* r, const T* z, T* d, CgState* st, double* part) {
   __shared__ double sh[32];
-  double rz = 0.0, rr = 0.0;
+  T rz = T(0), rr = T(0);
   PL_GRID_STRIDE(e, (int)k.total) {
     const T zi = z[e], ri = r[e];
     d[e] = zi;
-    rz += (double)ri * (double)zi;
-    rr += (double)ri * (double)ri;
+    rz += ri * zi;
+    rr += ri * ri;
   }
-  const double s1 = block_sum(rz, sh);
+  const double s1 = block_sum((double)rz, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s1;
-  const double s2 = block_sum(rr, sh);
+  const double s2 = block_sum((double)rr, sh);
   if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
   if (arrive_last(&st->ticket[0])) {
     const double trz = sum_partials(part, sh);
@@ -137,17 +141,17 @@ template <typename T>
 __global__ void k_cgs_spmv(Grid g, Skew k, const T* d, T* q, CgState* st, double* part) {
   if (st->done) return;
   __shared__ double sh[32];
-  double dq = 0.0;
+  T dq = T(0);
   PL_GRID_STRIDE(e, (int)k.total) {
     int ix, iy, iz;
     T v = T(0);
     if (skew_cell(k, e, ix, iy, iz)) {
       v = mult_a_skew(g, k, d, e, ix, iy, iz);
-      dq += (double)d[e] * (double)v;
+      dq += d[e] * v;
     }
     q[e] = v;
   }
-  const double s = block_sum(dq, sh);
+  const double s = block_sum((double)dq, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (arrive_last(&st->ticket[0])) {
     const double t = sum_partials(part, sh);
@@ -170,17 +174,17 @@ __global__ void k_cgs_axpy(Skew k, const T* d, const T* q, T* x, T* r, CgState* 
   if (st->done) return;
   __shared__ double sh[32];
   const T alpha = (T)st->alpha;
-  double mx = -1.0e308, rr = 0.0;
+  T mx = T(-3.0e38), rr = T(0);
   PL_GRID_STRIDE(e, (int)k.total) {
     x[e] += alpha * d[e];
     const T ri = r[e] + (-alpha) * q[e];
     r[e] = ri;
-    mx = ((double)ri > mx) ? (double)ri : mx;
-    rr += (double)ri * (double)ri;
+    mx = (ri > mx) ? ri : mx;
+    rr += ri * ri;
   }
-  const double s1 = block_max(mx, sh, -1.0e308);
+  const double s1 = block_max((double)mx, sh, -1.0e308);
   if (threadIdx.x == 0) part[blockIdx.x] = s1;
-  const double s2 = block_sum(rr, sh);
+  const double s2 = block_sum((double)rr, sh);
   if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
   if (arrive_last(&st->ticket[0])) {
     const double tm = max_partials(part, sh);
@@ -204,9 +208,9 @@ template <typename T>
 __global__ void k_cgs_rz(Skew k, const T* r, const T* z, CgState* st, double* part) {
   if (st->done) return;
   __shared__ double sh[32];
-  double rz = 0.0;
-  PL_GRID_STRIDE(e, (int)k.total) rz += (double)r[e] * (double)z[e];
-  const double s = block_sum(rz, sh);
+  T rz = T(0);
+  PL_GRID_STRIDE(e, (int)k.total) rz += r[e] * z[e];
+  const double s = block_sum((double)rz, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (arrive_last(&st->ticket[0])) {
     const double t = sum_partials(part, sh);

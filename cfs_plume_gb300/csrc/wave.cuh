@@ -43,7 +43,8 @@ __host__ __device__ inline long long skew_index(const Skew& k, int ix, int iy, i
   return (long long)iz * k.plane + (long long)(iy + ix / k.C) * k.W + ix;
 }
 
-constexpr int kWavePF = 8;     // TMA prefetch ring depth (rows)
+constexpr int kWaveKB = 4;     // rows per TMA block (contiguous in the skewed layout)
+constexpr int kWavePF = 4;     // TMA ring depth (blocks)
 constexpr int kWaveD = 8;      // inter-warp ring depth (steps)
 constexpr long long kSpinLimit = 1ll << 24;     // shared-memory polls (~0.3 s)
 constexpr long long kSpinLimitSlow = 1ll << 21; // global-flag polls and TMA waits (~2 s)
@@ -97,21 +98,93 @@ __device__ inline void fence_mbar_init() { asm volatile("fence.mbarrier_init.rel
 __device__ inline int ld_vol(const int* p) { return *((volatile const int*)p); }
 __device__ inline void st_vol(int* p, int v) { *((volatile int*)p) = v; }
 
+// Extra PTX for the ring hand-off: st.async writes a value into (possibly
+// another CTA's) shared memory and signals that CTA's mbarrier with the bytes
+// written (complete_tx); the consumer arms its slot barrier with the expected
+// byte count and waits on the phase.  No fence is needed on the producer side,
+// so a step never waits for its own global stores to drain.
+__device__ inline void mbar_arm(uint64_t* bar, unsigned bytes) { mbar_expect_tx(bar, bytes); }
+__device__ inline bool mbar_try_wait_cluster(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ inline void st_async(unsigned addr, float v, unsigned bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.f32 [%0], %1, [%2];" ::"r"(addr),
+               "f"(v), "r"(bar)
+               : "memory");
+}
+__device__ inline void st_async(unsigned addr, double v, unsigned bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.f64 [%0], %1, [%2];" ::"r"(addr),
+               "d"(v), "r"(bar)
+               : "memory");
+}
+__device__ inline void st_async4(unsigned addr, float a, float b, float c, float d, unsigned bar) {
+  asm volatile(
+      "st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(addr),
+      "f"(a), "f"(b), "f"(c), "f"(d), "r"(bar)
+      : "memory");
+}
+__device__ inline void st_async2(unsigned addr, double a, double b, unsigned bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f64 [%0], {%1, %2}, [%3];" ::"r"(addr),
+               "d"(a), "d"(b), "r"(bar)
+               : "memory");
+}
+// lane's C values -> ring slot at shared::cluster address `dst` (16 B aligned)
+template <typename T, int C>
+__device__ inline void st_async_row(unsigned dst, const T (&v)[C], unsigned bar) {
+  if (sizeof(T) == 4 && C % 4 == 0) {
+#pragma unroll
+    for (int j = 0; j < C; j += 4)
+      st_async4(dst + j * 4, (float)v[j], (float)v[j + 1], (float)v[j + 2], (float)v[j + 3], bar);
+  } else if (sizeof(T) == 8 && C % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < C; j += 2) st_async2(dst + j * 8, (double)v[j], (double)v[j + 1], bar);
+  } else {
+#pragma unroll
+    for (int j = 0; j < C; j++) st_async(dst + j * sizeof(T), v[j], bar);
+  }
+}
+__device__ inline unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ inline void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ inline unsigned mapa_u32(const void* p, unsigned rank) {
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+__device__ inline int ld_remote_relaxed(unsigned raddr) {
+  int v;
+  asm volatile("ld.relaxed.cluster.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(raddr) : "memory");
+  return v;
+}
+
 // Shared-memory layout of one CTA (dynamic): see wave_smem_bytes().
 template <typename T>
 struct WaveSmem {
-  T* tma;          // [BZ][PF][2][W]  in-row, P-row per slot
-  uint64_t* bar;   // [BZ][PF]
+  T* tma;          // [BZ][PF][2][KB][W]  KB input rows, then KB diagonal rows
+  uint64_t* bar;   // [BZ][PF]        TMA slot barriers
   T* ring;         // [BZ][D][W]      ring r is read by compute warp r
-  int* prog;       // [BZ + 1]        steps completed: warps 0..BZ-1, courier (ring 0) at BZ
+  uint64_t* rbar;  // [BZ][D]         ring slot barriers (armed by the reader)
+  int* prog;       // [BZ + 1]        steps consumed per compute warp; [BZ] courier fetch count
   int* misc;       // [4]             slab, failed
 };
 
 template <typename T>
 __host__ __device__ inline size_t wave_smem_bytes(int BZ, int W) {
-  size_t b = (size_t)BZ * kWavePF * 2 * W * sizeof(T);
+  size_t b = (size_t)BZ * kWavePF * 2 * kWaveKB * W * sizeof(T);
   b += (size_t)BZ * kWavePF * sizeof(uint64_t);
   b += (size_t)BZ * kWaveD * W * sizeof(T);
+  b += (size_t)BZ * kWaveD * sizeof(uint64_t);
   b += (size_t)(BZ + 1 + 4) * sizeof(int);
   return b;
 }
@@ -120,11 +193,13 @@ template <typename T>
 __device__ inline WaveSmem<T> wave_carve(char* base, int BZ, int W) {
   WaveSmem<T> s;
   s.tma = (T*)base;
-  base += (size_t)BZ * kWavePF * 2 * W * sizeof(T);
+  base += (size_t)BZ * kWavePF * 2 * kWaveKB * W * sizeof(T);
   s.bar = (uint64_t*)base;
   base += (size_t)BZ * kWavePF * sizeof(uint64_t);
   s.ring = (T*)base;
   base += (size_t)BZ * kWaveD * W * sizeof(T);
+  s.rbar = (uint64_t*)base;
+  base += (size_t)BZ * kWaveD * sizeof(uint64_t);
   s.prog = (int*)base;
   s.misc = s.prog + BZ + 1;
   return s;
@@ -142,13 +217,16 @@ __device__ inline void wave_fail(CgState* st, int code, int* failed) {
 template <typename T, bool EXACT, bool BWD>
 __device__ inline void sweep_cell(T in, T p, T cx, T cy, T cz, T& out, T& pass) {
   if (!BWD) {
-    T t;
-    if (EXACT)
-      t = ((in + cx) + cy) + cz;
-    else
-      t = (in + cy + cz) + cx;
-    out = t * p;
-    pass = p * out;
+    if (EXACT) {
+      const T t = ((in + cx) + cy) + cz;
+      out = t * p;
+      pass = p * out;
+    } else {  // pass = P^2 (b + cx): one multiply-add on the chain
+      const T b = in + cy + cz;
+      const T p2 = p * p;
+      pass = fma(p2, cx, p2 * b);
+      out = p * (b + cx);
+    }
   } else {
     T t;
     if (EXACT)
@@ -160,30 +238,282 @@ __device__ inline void sweep_cell(T in, T p, T cx, T cy, T cz, T& out, T& pass) 
   }
 }
 
+// Where a compute warp sends its per-step values: into ring slot barriers of
+// a consumer in this CTA or in another CTA of the cluster (shared::cluster
+// addresses), whose consumed-step counter gives the back-pressure.
+struct RingDst {
+  unsigned ring;   // shared::cluster address of the consumer ring (slot 0)
+  unsigned rbar;   // shared::cluster address of the consumer's slot barriers
+  unsigned prog;   // shared::cluster address of the consumer's consumed-step counter
+  bool remote;     // counter lives in another CTA
+};
+
+// The per-plane body shared by both kernels: R steps of one compute warp.
+// ring_in/rbar_in: this warp's input ring (zeros and no waiting when
+// `no_input`).  Returns false after a bounded wait expired.
 template <typename T, int C, bool EXACT, bool BWD>
-__global__ void __launch_bounds__(32 * 17) k_mic_wave(WaveArgs<T> a) {
+__device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int lane, int z,
+                            bool no_input, const RingDst dst, bool has_dst, int* failed,
+                            unsigned& tparity, unsigned& rparity, int feed_K, bool feed_fence) {
+  const int W = a.k.W, R = a.k.R;
+  const unsigned rowb = (unsigned)(W * sizeof(T));
+  const int nblocks = (R + kWaveKB - 1) / kWaveKB;
+  const T* inp = a.in + (long long)z * a.k.plane;
+  const T* Pp = a.P + (long long)z * a.k.plane;
+  T* outp = a.out + (long long)z * a.k.plane;
+  T* tma = sm.tma + (size_t)warp * kWavePF * 2 * kWaveKB * W;
+  uint64_t* bar = sm.bar + warp * kWavePF;
+  const T* ring_in = sm.ring + (size_t)warp * kWaveD * W;
+  uint64_t* rbar_in = sm.rbar + warp * kWaveD;
+  // block j = steps [j*KB, j*KB+KB); rows are contiguous in sweep order after
+  // reversing for the backward sweep, so one bulk copy per array per block.
+  auto issue = [&](int j) {
+    const int t0 = j * kWaveKB;
+    const int n = min(kWaveKB, R - t0);
+    const int row0 = BWD ? (R - t0 - n) : t0;  // lowest row of the block
+    uint64_t* bb = &bar[j % kWavePF];
+    T* d = tma + (size_t)(j % kWavePF) * 2 * kWaveKB * W;
+    mbar_expect_tx(bb, 2u * (unsigned)n * rowb);
+    tma_row(d, inp + (size_t)row0 * W, (unsigned)n * rowb, bb);
+    tma_row(d + (size_t)kWaveKB * W, Pp + (size_t)row0 * W, (unsigned)n * rowb, bb);
+  };
+  const int prime = min(kWavePF - 1, nblocks);
+  if (lane == 0) {
+    for (int j = 0; j < prime; j++) issue(j);
+    if (!no_input)  // arm the input ring for steps 0..D-1
+      for (int t = 0; t < kWaveD && t < R; t++) mbar_arm(&rbar_in[t], rowb);
+  }
+  int issued = prime, consumed = 0;
+  T cy[C];
+#pragma unroll
+  for (int j = 0; j < C; j++) cy[j] = T(0);
+  T edge = T(0);
+  int next_seen = 0;
+  bool ok = true;
+  const T* din = tma;
+  for (int t = 0; t < R && ok; t++) {
+    const int tb = t % kWaveKB;
+    if (tb == 0) {
+      // a new block: issue block j+PF-1 into the slot freed by block j-1
+      const int j = t / kWaveKB;
+      if (j + kWavePF - 1 < nblocks) {
+        if (lane == 0) issue(j + kWavePF - 1);
+        issued = j + kWavePF;
+      }
+      const int slot = j % kWavePF;
+      long long spins = 0;
+      while (!mbar_try_wait(&bar[slot], (tparity >> slot) & 1u)) {
+        if (++spins > kSpinLimitSlow) {
+          ok = false;
+          break;
+        }
+      }
+      if (!ok) {
+        if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_TMA, failed);
+        break;
+      }
+      tparity ^= 1u << slot;
+      consumed = j + 1;
+      din = tma + (size_t)slot * 2 * kWaveKB * W;
+    }
+    // row of this step inside the block (the block is stored ascending)
+    const int n_blk = min(kWaveKB, R - (t - tb));
+    const int rib = BWD ? (n_blk - 1 - tb) : tb;
+    T vin[C], vp[C];
+#pragma unroll
+    for (int j = 0; j < C; j++) {
+      vin[j] = din[(size_t)rib * W + lane * C + j];
+      vp[j] = din[(size_t)(kWaveKB + rib) * W + lane * C + j];
+    }
+    // neighbour-plane values of this step
+    T cz[C];
+    const int rs = t % kWaveD;
+    if (no_input) {
+#pragma unroll
+      for (int j = 0; j < C; j++) cz[j] = T(0);
+    } else {
+      long long spins = 0;
+      while (!mbar_try_wait_cluster(&rbar_in[rs], (rparity >> rs) & 1u)) {
+        if (++spins > kSpinLimit || ld_vol(failed)) {
+          ok = false;
+          break;
+        }
+      }
+      if (!ok) {
+        if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_RING, failed);
+        break;
+      }
+      rparity ^= 1u << rs;
+      const T* rin = ring_in + (size_t)rs * W;
+#pragma unroll
+      for (int j = 0; j < C; j++) cz[j] = rin[lane * C + j];
+    }
+    T cx = BWD ? __shfl_down_sync(0xffffffffu, edge, 1) : __shfl_up_sync(0xffffffffu, edge, 1);
+    if (BWD ? (lane == 31) : (lane == 0)) cx = T(0);
+    T vout[C], pass[C];
+    if (!BWD) {
+#pragma unroll
+      for (int j = 0; j < C; j++) {
+        sweep_cell<T, EXACT, false>(vin[j], vp[j], cx, cy[j], cz[j], vout[j], pass[j]);
+        cx = pass[j];
+      }
+      edge = pass[C - 1];
+    } else {
+#pragma unroll
+      for (int j = C - 1; j >= 0; j--) {
+        sweep_cell<T, EXACT, true>(vin[j], vp[j], cx, cy[j], cz[j], vout[j], pass[j]);
+        cx = pass[j];
+      }
+      edge = pass[0];
+    }
+#pragma unroll
+    for (int j = 0; j < C; j++) cy[j] = pass[j];
+    // hand this step to the consumer plane (bounded back-pressure on its ring)
+    if (has_dst) {
+      if (next_seen <= t - kWaveD) {
+        long long spins = 0;
+        for (;;) {
+          next_seen = ld_remote_relaxed(dst.prog);  // a shared::cta address is valid here too
+          if (next_seen > t - kWaveD) break;
+          if (++spins > kSpinLimit || ld_vol(failed)) {
+            ok = false;
+            break;
+          }
+        }
+        if (!ok) {
+          if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_RING, failed);
+          break;
+        }
+      }
+      const unsigned off = (unsigned)(((size_t)rs * W + lane * C) * sizeof(T));
+      st_async_row<T, C>(dst.ring + off, pass, dst.rbar + (unsigned)(rs * sizeof(uint64_t)));
+    }
+    // output row
+    T* orow = outp + (size_t)(BWD ? (R - 1 - t) : t) * W + lane * C;
+    if (sizeof(T) == 4 && C % 4 == 0) {
+#pragma unroll
+      for (int j = 0; j < C; j += 4)
+        *reinterpret_cast<float4*>(orow + j) = make_float4(vout[j], vout[j + 1], vout[j + 2], vout[j + 3]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < C; j++) orow[j] = vout[j];
+    }
+    // every 4 steps: report consumption and re-arm the consumed ring slots
+    if ((t & 3) == 3 || t + 1 == R) {
+      __syncwarp();
+      if (lane == 0) {
+        st_vol(&sm.prog[warp], t + 1);
+        if (!no_input)
+          for (int u = (t & ~3); u <= t; u++)
+            if (u + kWaveD < R) mbar_arm(&rbar_in[u % kWaveD], rowb);
+      }
+    }
+    // boundary plane of the courier path: make rows visible GPU-wide every K
+    if (feed_fence && ((t + 1) % feed_K == 0 || t + 1 == R)) {
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) st_vol(&sm.misc[2], t + 1);
+    }
+  }
+  // every issued TMA block must land before its slot is reused or the CTA exits
+  for (int j = consumed; j < issued; j++) {
+    const int k = j % kWavePF;
+    long long spins = 0;
+    while (!mbar_try_wait(&bar[k], (tparity >> k) & 1u)) {
+      if (++spins > kSpinLimitSlow) {
+        if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_TMA, failed);
+        break;
+      }
+    }
+    tparity ^= 1u << k;
+  }
+  __syncwarp();
+  return ok;
+}
+
+// ------------------------------------------------------------ cluster path
+// One thread-block cluster per plume: CTA rank r owns slab r (BZ planes), so
+// the plume's whole z-extent lives in one cluster (nslabs <= 16).  The last
+// compute warp of a slab st.async-writes its per-step values into ring 0 of
+// the next slab's CTA over distributed shared memory.  No global flags.
+template <typename T, int C, bool EXACT, bool BWD>
+__global__ void __launch_bounds__(32 * 16) k_mic_wave_cl(WaveArgs<T> a) {
+  if (a.st->done) return;
+  extern __shared__ __align__(128) char smem_raw[];
+  const int BZ = a.BZ, W = a.k.W;
+  WaveSmem<T> sm = wave_carve<T>(smem_raw, BZ, W);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned rank = cluster_rank();
+  const int z0 = (int)rank * BZ;
+  const int zend = min(z0 + BZ, a.k.nz);
+  const int nw = max(zend - z0, 0);
+  const bool has_up = BWD ? (zend < a.k.nz) : (z0 > 0);
+  const bool has_down = BWD ? (z0 > 0) : (zend < a.k.nz);
+  const unsigned down_rank = BWD ? rank - 1 : rank + 1;
+  int* failed = &sm.misc[1];
+  if (lane == 0 && warp < BZ) {
+    for (int k = 0; k < kWavePF; k++) mbar_init(&sm.bar[warp * kWavePF + k], 1);
+    for (int k = 0; k < kWaveD; k++) mbar_init(&sm.rbar[warp * kWaveD + k], 1);
+  }
+  if (threadIdx.x == 0) {
+    sm.misc[1] = 0;
+    for (int w = 0; w <= BZ; w++) sm.prog[w] = 0;
+  }
+  fence_mbar_init();
+  __syncthreads();
+  cluster_sync_all();  // every CTA's barriers exist before any remote st.async
+  if (warp < nw) {
+    const int z = BWD ? (zend - 1 - warp) : (z0 + warp);
+    RingDst d{0u, 0u, 0u, false};
+    bool has_dst = false;
+    if (warp + 1 < nw) {
+      d.ring = smem_u32(sm.ring + (size_t)(warp + 1) * kWaveD * W);
+      d.rbar = smem_u32(sm.rbar + (warp + 1) * kWaveD);
+      d.prog = smem_u32(&sm.prog[warp + 1]);
+      has_dst = true;
+    } else if (has_down) {
+      d.ring = mapa_u32(sm.ring, down_rank);
+      d.rbar = mapa_u32(sm.rbar, down_rank);
+      d.prog = mapa_u32(&sm.prog[0], down_rank);
+      d.remote = true;
+      has_dst = true;
+    }
+    unsigned tpar = 0u, rpar = 0u;
+    sweep_plane<T, C, EXACT, BWD>(a, sm, warp, lane, z, warp == 0 && !has_up, d, has_dst, failed, tpar,
+                                  rpar, 1, false);
+  }
+  __syncthreads();
+  cluster_sync_all();  // no CTA leaves while a neighbour may still write into it
+}
+
+// ------------------------------------------------------------ courier path
+// For plumes too tall for one cluster: slabs are handed to CTAs in sweep
+// order by a ticket (a CTA only waits on slabs already running, so any grid
+// size is deadlock-free); per CTA a fetch courier feeds ring 0 from the
+// upstream slab's boundary plane in global memory, and a publish courier
+// advertises this slab's boundary progress every K steps.
+template <typename T, int C, bool EXACT, bool BWD>
+__global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
   if (a.st->done) return;
   extern __shared__ __align__(128) char smem_raw[];
   const int BZ = a.BZ, W = a.k.W, R = a.k.R;
   WaveSmem<T> sm = wave_carve<T>(smem_raw, BZ, W);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const bool courier = (warp == BZ);
   int* failed = &sm.misc[1];
   const unsigned rowb = (unsigned)(W * sizeof(T));
-
-  // per-warp TMA slot barriers, initialised once per CTA
-  if (!courier && lane == 0)
+  if (lane == 0 && warp < BZ) {
     for (int k = 0; k < kWavePF; k++) mbar_init(&sm.bar[warp * kWavePF + k], 1);
+    for (int k = 0; k < kWaveD; k++) mbar_init(&sm.rbar[warp * kWaveD + k], 1);
+  }
   if (threadIdx.x == 0) sm.misc[1] = 0;
   fence_mbar_init();
   __syncthreads();
-  // bit k = phase parity expected next on TMA slot k (same in every lane)
-  unsigned parity = 0u;
-
+  unsigned tpar = 0u, rpar = 0u;  // barrier phases carry over between slabs
   for (;;) {
     if (threadIdx.x == 0) {
       const unsigned tk = atomicAdd(&a.ctl[0], 1u);
       sm.misc[0] = (tk < (unsigned)a.nslabs) ? (int)tk : -1;
+      sm.misc[2] = 0;
       for (int w = 0; w <= BZ; w++) sm.prog[w] = 0;
     }
     __syncthreads();
@@ -191,208 +521,93 @@ __global__ void __launch_bounds__(32 * 17) k_mic_wave(WaveArgs<T> a) {
     if (ticket < 0 || ld_vol(failed) || ld_vol(&a.st->wave_err)) break;
     const int slab = a.backward ? (a.nslabs - 1 - ticket) : ticket;
     const int z0 = slab * BZ;
-    const int zend = min(z0 + BZ, a.k.nz);  // planes [z0, zend)
-    const int nw = zend - z0;                // compute warps with a plane
+    const int zend = min(z0 + BZ, a.k.nz);
+    const int nw = zend - z0;
     const bool has_up = a.backward ? (zend < a.k.nz) : (z0 > 0);
     const bool has_down = a.backward ? (z0 > 0) : (zend < a.k.nz);
-    const int z_up = a.backward ? zend : z0 - 1;  // neighbour plane feeding warp 0
-    const int z_last = a.backward ? z0 : zend - 1;  // plane the next slab reads
-
-    if (courier) {
-      // ---------------- courier: bridge to the neighbouring slabs ----------
-      int in_next = 0;  // steps of plane z_up copied into ring 0
-      int pub = has_down ? 0 : R;  // steps of plane z_last published
-      if (!has_up) {
-        // no neighbour plane: ring 0 holds zeros for the whole slab
-        for (int e = lane; e < kWaveD * W; e += 32) sm.ring[e] = T(0);
-        __syncwarp();
-        __threadfence_block();
-        in_next = R;
-        if (lane == 0) st_vol(&sm.prog[BZ], R);
-      }
-      long long spins = 0;
-      while ((in_next < R || pub < R) && !ld_vol(failed)) {
-        bool moved = false;
-        if (in_next < R) {
+    const int z_up = a.backward ? zend : z0 - 1;
+    const int z_last = a.backward ? z0 : zend - 1;
+    if (warp == BZ) {
+      // fetch courier: upstream boundary plane -> ring 0 (st.async, local)
+      if (has_up) {
+        int in_next = 0;
+        long long spins = 0;
+        const unsigned ring0 = smem_u32(sm.ring), rbar0 = smem_u32(sm.rbar);
+        while (in_next < R && !ld_vol(failed)) {
           const int avail = ld_vol(&a.progress[z_up]);
           const int space = ld_vol(&sm.prog[0]) + kWaveD - in_next;
           const int n = min(min(avail - in_next, space), 4);
-          if (n > 0) {
-            __threadfence();
-            for (int i = 0; i < n; i++) {
+          if (n <= 0) {
+            if (++spins > kSpinLimitSlow) {
+              if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_FLAG, failed);
+              break;
+            }
+            __nanosleep(32);
+            continue;
+          }
+          spins = 0;
+          __threadfence();
+          T o[4][C], pv[4][C];
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            if (i < n) {
               const int t = in_next + i;
               const int row = a.backward ? (R - 1 - t) : t;
-              const long long base = (long long)z_up * a.k.plane + (long long)row * W;
-              T* slot = sm.ring + (size_t)(t % kWaveD) * W;  // ring 0
+              const long long base = (long long)z_up * a.k.plane + (long long)row * W + lane * C;
 #pragma unroll
               for (int j = 0; j < C; j++) {
-                const int c = lane * C + j;
-                const T o = __ldcg(a.out + base + c);
-                slot[c] = BWD ? o : (__ldcg(a.P + base + c) * o);
+                o[i][j] = __ldcg(a.out + base + j);
+                pv[i][j] = BWD ? T(1) : __ldcg(a.P + base + j);
               }
             }
-            __syncwarp();
-            __threadfence_block();
-            in_next += n;
-            if (lane == 0) st_vol(&sm.prog[BZ], in_next);
-            moved = true;
           }
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            if (i < n) {
+              const int rs = (in_next + i) % kWaveD;
+              T v[C];
+#pragma unroll
+              for (int j = 0; j < C; j++) v[j] = BWD ? o[i][j] : pv[i][j] * o[i][j];
+              st_async_row<T, C>(ring0 + (unsigned)(((size_t)rs * W + lane * C) * sizeof(T)), v,
+                                 rbar0 + (unsigned)(rs * sizeof(uint64_t)));
+            }
+          }
+          in_next += n;
         }
-        if (pub < R) {
-          const int p = ld_vol(&sm.prog[nw - 1]);
-          if (p >= min(pub + a.K, R)) {
-            __threadfence();
+      }
+    } else if (warp == BZ + 1) {
+      // publish courier: this slab's boundary progress -> global flag
+      if (has_down) {
+        int pub = 0;
+        long long spins = 0;
+        while (pub < R && !ld_vol(failed)) {
+          const int p = ld_vol(&sm.misc[2]);  // rows the boundary warp has fenced
+          if (p > pub) {
             if (lane == 0) st_vol(&a.progress[z_last], p);
             pub = p;
-            moved = true;
+            spins = 0;
+          } else if (++spins > kSpinLimitSlow) {
+            if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_FLAG, failed);
+            break;
+          } else {
+            __nanosleep(32);
           }
-        }
-        if (moved) {
-          spins = 0;
-        } else if (++spins > kSpinLimitSlow) {
-          if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_FLAG, failed);
-          break;
-        } else {
-          __nanosleep(32);
         }
       }
     } else if (warp < nw) {
-      // ---------------- compute warp: one plane, R steps -------------------
       const int z = a.backward ? (zend - 1 - warp) : (z0 + warp);
-      const T* inp = a.in + (long long)z * a.k.plane;
-      const T* Pp = a.P + (long long)z * a.k.plane;
-      T* outp = a.out + (long long)z * a.k.plane;
-      T* tma = sm.tma + (size_t)warp * kWavePF * 2 * W;
-      uint64_t* bar = sm.bar + warp * kWavePF;
-      const T* ring_in = sm.ring + (size_t)warp * kWaveD * W;   // filled by warp-1 / courier
-      T* ring_out = sm.ring + (size_t)(warp + 1) * kWaveD * W;  // read by warp+1
-      const int* prog_in = (warp == 0) ? &sm.prog[BZ] : &sm.prog[warp - 1];
-      const bool has_next = (warp + 1 < nw);
-      const int* prog_next = &sm.prog[warp + 1];
-      // the boundary warp makes its rows visible GPU-wide before counting them
-      const bool feeds_slab = has_down && (warp == nw - 1);
-      int issued = 0, consumed = 0;
-      auto issue = [&](int tn) {  // lane 0 only
-        uint64_t* b = &bar[tn % kWavePF];
-        T* d = tma + (size_t)(tn % kWavePF) * 2 * W;
-        const int row = a.backward ? (R - 1 - tn) : tn;
-        fence_proxy_async();
-        mbar_expect_tx(b, 2 * rowb);
-        tma_row(d, inp + (size_t)row * W, rowb, b);
-        tma_row(d + W, Pp + (size_t)row * W, rowb, b);
-      };
-      const int prime = min(kWavePF - 1, R);
-      if (lane == 0)
-        for (int t = 0; t < prime; t++) issue(t);
-      issued = prime;
-      T cy[C];  // value from the previous step (the -y / +y neighbour)
-#pragma unroll
-      for (int j = 0; j < C; j++) cy[j] = T(0);
-      T edge = T(0);  // this lane's outermost value of the previous step
-      bool ok = true;
-      for (int t = 0; t < R && ok; t++) {
-        const int slot = t % kWavePF;
-        // issue step t+PF-1 into the slot consumed at step t-1
-        if (t + kWavePF - 1 < R) {
-          if (lane == 0) issue(t + kWavePF - 1);
-          issued = t + kWavePF;
-        }
-        // neighbour plane values for this step
-        long long spins = 0;
-        while (ld_vol(prog_in) <= t) {
-          if (++spins > kSpinLimit || ld_vol(failed)) {
-            if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_RING, failed);
-            ok = false;
-            break;
-          }
-        }
-        if (!ok) break;
-        __threadfence_block();
-        const T* rin = ring_in + (size_t)(t % kWaveD) * W;
-        T cz[C];
-#pragma unroll
-        for (int j = 0; j < C; j++) cz[j] = rin[lane * C + j];
-        // this step's input row and diagonal
-        spins = 0;
-        while (!mbar_try_wait(&bar[slot], (parity >> slot) & 1u)) {
-          if (++spins > kSpinLimitSlow) {
-            if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_TMA, failed);
-            ok = false;
-            break;
-          }
-        }
-        if (!ok) break;
-        parity ^= 1u << slot;
-        consumed = t + 1;
-        const T* din = tma + (size_t)slot * 2 * W;
-        T vin[C], vp[C];
-#pragma unroll
-        for (int j = 0; j < C; j++) {
-          vin[j] = din[lane * C + j];
-          vp[j] = din[W + lane * C + j];
-        }
-        // x-neighbour across the lane boundary: previous step of lane-1
-        // (forward) or lane+1 (backward)
-        T cx = BWD ? __shfl_down_sync(0xffffffffu, edge, 1) : __shfl_up_sync(0xffffffffu, edge, 1);
-        if (BWD ? (lane == 31) : (lane == 0)) cx = T(0);
-        T vout[C], pass[C];
-        if (!BWD) {
-#pragma unroll
-          for (int j = 0; j < C; j++) {
-            sweep_cell<T, EXACT, false>(vin[j], vp[j], cx, cy[j], cz[j], vout[j], pass[j]);
-            cx = pass[j];
-          }
-          edge = pass[C - 1];
-        } else {
-#pragma unroll
-          for (int j = C - 1; j >= 0; j--) {
-            sweep_cell<T, EXACT, true>(vin[j], vp[j], cx, cy[j], cz[j], vout[j], pass[j]);
-            cx = pass[j];
-          }
-          edge = pass[0];
-        }
-        // output row
-        T* orow = outp + (size_t)(a.backward ? (R - 1 - t) : t) * W + lane * C;
-#pragma unroll
-        for (int j = 0; j < C; j++) {
-          orow[j] = vout[j];
-          cy[j] = pass[j];
-        }
-        // hand this step to the next warp (bounded back-pressure on its ring)
-        if (has_next) {
-          spins = 0;
-          while (ld_vol(prog_next) <= t - kWaveD) {
-            if (++spins > kSpinLimit || ld_vol(failed)) {
-              if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_RING, failed);
-              ok = false;
-              break;
-            }
-          }
-          if (!ok) break;
-          T* rout = ring_out + (size_t)(t % kWaveD) * W;
-#pragma unroll
-          for (int j = 0; j < C; j++) rout[lane * C + j] = pass[j];
-        }
-        if (feeds_slab && ((t + 1) % a.K == 0 || t + 1 == R)) __threadfence();
-        __syncwarp();
-        __threadfence_block();
-        if (lane == 0) st_vol(&sm.prog[warp], t + 1);
+      RingDst d{0u, 0u, 0u, false};
+      const bool has_dst = warp + 1 < nw;
+      if (has_dst) {
+        d.ring = smem_u32(sm.ring + (size_t)(warp + 1) * kWaveD * W);
+        d.rbar = smem_u32(sm.rbar + (warp + 1) * kWaveD);
+        d.prog = smem_u32(&sm.prog[warp + 1]);
       }
-      // every issued copy must land before its slot is reused by the next
-      // slab or the CTA exits: wait (bounded) for steps consumed..issued-1
-      for (int t = consumed; t < issued; t++) {
-        const int k = t % kWavePF;
-        long long spins = 0;
-        while (!mbar_try_wait(&bar[k], (parity >> k) & 1u)) {
-          if (++spins > kSpinLimitSlow) {
-            if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_TMA, failed);
-            break;
-          }
-        }
-        parity ^= 1u << k;
-      }
-      __syncwarp();
+      const bool boundary = has_down && warp == nw - 1;
+      sweep_plane<T, C, EXACT, BWD>(a, sm, warp, lane, z, warp == 0 && !has_up, d, has_dst, failed,
+                                    tpar, rpar, a.K, boundary);
     }
+    (void)rowb;
     __syncthreads();
     if (ld_vol(failed)) break;
   }

@@ -202,19 +202,25 @@ def test_streams_are_reference_format(tmp_path):
         assert rel_l2(ra, rb) < 1e-9 if rb.size else True, name
 
 
-WAVE_SHAPES = [  # (BZ, grid cap) exercising 1..many slabs and the ticket loop
-    ("1", None), ("3", None), ("8", None), ("2", "3"),
+WAVE_SHAPES = [  # (path, planes per CTA, CTA cap): cluster (DSMEM) and courier paths
+    ("cluster", "1", None), ("cluster", "2", None), ("cluster", "4", None),
+    ("courier", "1", None), ("courier", "3", None), ("courier", "8", None), ("courier", "2", "3"),
 ]
 
 
-@pytest.mark.parametrize("bz,grid", WAVE_SHAPES)
+@pytest.mark.parametrize("path,bz,grid", WAVE_SHAPES)
 @pytest.mark.parametrize("kw", [SMALL[0], SMALL[2], dict(res=(40, 12, 21), bc=(1, 1, 1, 1, 1, 1)),
                                 dict(res=(70, 9, 11), bc=(0, 0, 0, 0, 0, 0))])
-def test_wavefront_sweeps_bit_exact_fp64(kw, bz, grid, monkeypatch):
-    """The persistent wavefront sweeps (skewed layout, one warp per plane,
-    slabs linked through the courier warp) reproduce the serial sweep bit for
-    bit in FP64 for any slab height and CTA count."""
-    monkeypatch.setenv("PLUME_WAVE_BZ", bz)
+def test_wavefront_sweeps_bit_exact_fp64(kw, path, bz, grid, monkeypatch):
+    """The persistent wavefront sweeps (skewed layout, one warp per plane)
+    reproduce the serial sweep bit for bit in FP64, whether the slabs are
+    linked through a thread-block cluster's shared memory or through the
+    courier warps, for any slab height and CTA count."""
+    if path == "cluster":
+        monkeypatch.setenv("PLUME_WAVE_CL_BZ", bz)
+    else:
+        monkeypatch.setenv("PLUME_WAVE_NO_CLUSTER", "1")
+        monkeypatch.setenv("PLUME_WAVE_BZ", bz)
     if grid:
         monkeypatch.setenv("PLUME_WAVE_GRID", grid)
     p = _abi.default_params(**kw)
@@ -229,6 +235,24 @@ def test_wavefront_sweeps_bit_exact_fp64(kw, bz, grid, monkeypatch):
         z, q = g.mic_apply(r)
         assert np.array_equal(q, qo)
         assert np.array_equal(z, zo)
+
+
+@pytest.mark.parametrize("path", ["cluster", "courier"])
+def test_solve_paths_agree_fp64(path, monkeypatch):
+    """A full FP64 solve is identical whichever sweep path runs."""
+    if path == "courier":
+        monkeypatch.setenv("PLUME_WAVE_NO_CLUSTER", "1")
+    p = _abi.plume_config((24, 32, 36), precision=_abi.PREC_FP64, criterion=_abi.CRIT_REL2,
+                          tol=1e-9)
+    o = oracle.Oracle(p)
+    for s in range(2):
+        o.add_source(s)
+        o.step()
+    b = o.field("divergence")
+    xo, so = oracle.solve_poisson(p, b)
+    xg, sg = Plume(p).solve_poisson(b)
+    assert abs(sg.iterations - so.iterations) <= 1
+    assert rel_l2(xg, xo) < 1e-9
 
 
 def test_wavefront_sweeps_fp32():
