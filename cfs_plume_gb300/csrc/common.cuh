@@ -44,6 +44,11 @@ __device__ inline bool wall_yp(const Grid& g, int y) { return y == g.Y - 2 && g.
 __device__ inline bool wall_zm(const Grid& g, int z) { return z == 1 && g.wall[0] == 1; }
 __device__ inline bool wall_zp(const Grid& g, int z) { return z == g.Z - 2 && g.wall[1] == 1; }
 
+// Explicitly typed square root for the field type (the FP32 path must not
+// widen to FP64).
+__device__ inline float sqrt_t(float v) { return sqrtf(v); }
+__device__ inline double sqrt_t(double v) { return sqrt(v); }
+
 // Deterministic block reduction (fixed shuffle tree, fixed smem order).
 template <typename A>
 __device__ inline A warp_sum(A v) {

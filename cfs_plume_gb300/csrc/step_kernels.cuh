@@ -164,7 +164,7 @@ __global__ void k_vort1(Grid g, V3<T> v, V3<T> w, T* mag, StepConsts<T> c) {
       wy = w.y[i];
       wz = w.z[i];
     }
-    mag[i] = sqrt(wx * wx + wy * wy + wz * wz);
+    mag[i] = sqrt_t(wx * wx + wy * wy + wz * wz);
   }
 }
 
@@ -188,7 +188,7 @@ __global__ void k_vort2(Grid g, V3<T> vel, V3<T> w, const T* mag, V3<T> force,
       T N0 = (mag[s.right] - mag[s.left]) * dx;
       T N1 = (mag[s.up] - mag[s.down]) * dy;
       T N2 = (mag[s.out] - mag[s.in]) * dz;
-      T m = sqrt(N0 * N0 + N1 * N1 + N2 * N2);
+      T m = sqrt_t(N0 * N0 + N1 * N1 + N2 * N2);
       if (m > T(0)) {
         m = T(1) / m;
         N0 *= m;

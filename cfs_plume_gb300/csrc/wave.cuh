@@ -43,8 +43,8 @@ __host__ __device__ inline long long skew_index(const Skew& k, int ix, int iy, i
   return (long long)iz * k.plane + (long long)(iy + ix / k.C) * k.W + ix;
 }
 
-constexpr int kWaveKB = 4;     // rows per TMA block (contiguous in the skewed layout)
-constexpr int kWavePF = 4;     // TMA ring depth (blocks)
+constexpr int kWaveKB = 8;     // rows per TMA block (contiguous in the skewed layout)
+constexpr int kWavePF = 3;     // TMA ring depth (blocks)
 constexpr int kWaveD = 8;      // inter-warp ring depth (steps)
 constexpr long long kSpinLimit = 1ll << 24;     // shared-memory polls (~0.3 s)
 constexpr long long kSpinLimitSlow = 1ll << 21; // global-flag polls and TMA waits (~2 s)
@@ -104,6 +104,14 @@ __device__ inline void st_vol(int* p, int v) { *((volatile int*)p) = v; }
 // byte count and waits on the phase.  No fence is needed on the producer side,
 // so a step never waits for its own global stores to drain.
 __device__ inline void mbar_arm(uint64_t* bar, unsigned bytes) { mbar_expect_tx(bar, bytes); }
+// One arrival plus the expected byte count on a slot barrier at a
+// shared::cluster address (this CTA or another), relaxed: it orders nothing,
+// it only opens the phase that the following st.async bytes complete.
+__device__ inline void mbar_arm_remote(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.relaxed.cluster.shared::cluster.b64 _, [%0], %1;" ::"r"(bar),
+               "r"(bytes)
+               : "memory");
+}
 __device__ inline bool mbar_try_wait_cluster(uint64_t* bar, unsigned parity) {
   unsigned ok;
   asm volatile(
@@ -179,13 +187,17 @@ struct WaveSmem {
   int* misc;       // [4]             slab, failed
 };
 
+// Every region starts on a 128-byte boundary (16-byte vector accesses and
+// bulk copies need at least 16; mbarrier counts differ in size per region).
+__host__ __device__ inline size_t wave_al(size_t b) { return (b + 127) & ~(size_t)127; }
+
 template <typename T>
 __host__ __device__ inline size_t wave_smem_bytes(int BZ, int W) {
-  size_t b = (size_t)BZ * kWavePF * 2 * kWaveKB * W * sizeof(T);
-  b += (size_t)BZ * kWavePF * sizeof(uint64_t);
-  b += (size_t)BZ * kWaveD * W * sizeof(T);
-  b += (size_t)BZ * kWaveD * sizeof(uint64_t);
-  b += (size_t)(BZ + 1 + 4) * sizeof(int);
+  size_t b = wave_al((size_t)BZ * kWavePF * 2 * kWaveKB * W * sizeof(T));
+  b += wave_al((size_t)BZ * kWavePF * sizeof(uint64_t));
+  b += wave_al((size_t)BZ * kWaveD * W * sizeof(T));
+  b += wave_al((size_t)BZ * kWaveD * sizeof(uint64_t));
+  b += wave_al((size_t)(BZ + 1 + 4) * sizeof(int));
   return b;
 }
 
@@ -193,13 +205,13 @@ template <typename T>
 __device__ inline WaveSmem<T> wave_carve(char* base, int BZ, int W) {
   WaveSmem<T> s;
   s.tma = (T*)base;
-  base += (size_t)BZ * kWavePF * 2 * kWaveKB * W * sizeof(T);
+  base += wave_al((size_t)BZ * kWavePF * 2 * kWaveKB * W * sizeof(T));
   s.bar = (uint64_t*)base;
-  base += (size_t)BZ * kWavePF * sizeof(uint64_t);
+  base += wave_al((size_t)BZ * kWavePF * sizeof(uint64_t));
   s.ring = (T*)base;
-  base += (size_t)BZ * kWaveD * W * sizeof(T);
+  base += wave_al((size_t)BZ * kWaveD * W * sizeof(T));
   s.rbar = (uint64_t*)base;
-  base += (size_t)BZ * kWaveD * sizeof(uint64_t);
+  base += wave_al((size_t)BZ * kWaveD * sizeof(uint64_t));
   s.prog = (int*)base;
   s.misc = s.prog + BZ + 1;
   return s;
@@ -209,6 +221,37 @@ __device__ inline void wave_fail(CgState* st, int code, int* failed) {
   atomicCAS(&st->wave_err, 0, code);
   st_vol(failed, 1);
 }
+
+// A lane's C consecutive values from shared memory (16-byte loads when the
+// row slice allows it).
+template <typename T, int C>
+__device__ inline void lds_row(const T* src, T (&v)[C]) {
+  if (sizeof(T) == 4 && C % 4 == 0) {
+#pragma unroll
+    for (int j = 0; j < C; j += 4) {
+      const float4 f = *reinterpret_cast<const float4*>(src + j);
+      v[j] = (T)f.x;
+      v[j + 1] = (T)f.y;
+      v[j + 2] = (T)f.z;
+      v[j + 3] = (T)f.w;
+    }
+  } else if (sizeof(T) == 8 && C % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < C; j += 2) {
+      const double2 d = *reinterpret_cast<const double2*>(src + j);
+      v[j] = (T)d.x;
+      v[j + 1] = (T)d.y;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < C; j++) v[j] = src[j];
+  }
+}
+
+// Explicitly typed multiply-add: the generic overload set must never pick the
+// FP64 form for FP32 operands (FP64 is a small fraction of FP32 on GB300).
+__device__ inline float madd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ inline double madd(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 // One cell of the sweep.  Forward: t = ((r + wx) + wy) + wz, q = t*P, and the
 // value handed to the +x/+y/+z neighbours is w = P*q, because the reference
@@ -224,7 +267,7 @@ __device__ inline void sweep_cell(T in, T p, T cx, T cy, T cz, T& out, T& pass) 
     } else {  // pass = P^2 (b + cx): one multiply-add on the chain
       const T b = in + cy + cz;
       const T p2 = p * p;
-      pass = fma(p2, cx, p2 * b);
+      pass = madd(p2, cx, p2 * b);
       out = p * (b + cx);
     }
   } else {
@@ -265,67 +308,77 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
   uint64_t* bar = sm.bar + warp * kWavePF;
   const T* ring_in = sm.ring + (size_t)warp * kWaveD * W;
   uint64_t* rbar_in = sm.rbar + warp * kWaveD;
-  // block j = steps [j*KB, j*KB+KB); rows are contiguous in sweep order after
-  // reversing for the backward sweep, so one bulk copy per array per block.
+  // block j = steps [j*KB, j*KB+KB); its rows are contiguous, so one bulk
+  // copy per array per block (rows stored ascending in the slot).
   auto issue = [&](int j) {
     const int t0 = j * kWaveKB;
     const int n = min(kWaveKB, R - t0);
-    const int row0 = BWD ? (R - t0 - n) : t0;  // lowest row of the block
+    const int row0 = BWD ? (R - t0 - n) : t0;
     uint64_t* bb = &bar[j % kWavePF];
     T* d = tma + (size_t)(j % kWavePF) * 2 * kWaveKB * W;
     mbar_expect_tx(bb, 2u * (unsigned)n * rowb);
     tma_row(d, inp + (size_t)row0 * W, (unsigned)n * rowb, bb);
     tma_row(d + (size_t)kWaveKB * W, Pp + (size_t)row0 * W, (unsigned)n * rowb, bb);
   };
-  const int prime = min(kWavePF - 1, nblocks);
-  if (lane == 0) {
-    for (int j = 0; j < prime; j++) issue(j);
-    if (!no_input)  // arm the input ring for steps 0..D-1
-      for (int t = 0; t < kWaveD && t < R; t++) mbar_arm(&rbar_in[t], rowb);
-  }
-  int issued = prime, consumed = 0;
+  int issued = min(kWavePF - 1, nblocks), consumed = 0;
+  if (lane == 0)
+    for (int j = 0; j < issued; j++) issue(j);
+  bool ok = true;
+  const T* din = tma;
+  // make step t's block current (issue ahead, wait for it); false on timeout
+  auto enter_block = [&](int t) -> bool {
+    const int j = t / kWaveKB;
+    if (j + kWavePF - 1 < nblocks) {
+      if (lane == 0) issue(j + kWavePF - 1);
+      issued = j + kWavePF;
+    }
+    const int slot = j % kWavePF;
+    long long spins = 0;
+    while (!mbar_try_wait(&bar[slot], (tparity >> slot) & 1u)) {
+      if (++spins > kSpinLimitSlow) {
+        if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_TMA, failed);
+        return false;
+      }
+    }
+    tparity ^= 1u << slot;
+    consumed = j + 1;
+    din = tma + (size_t)slot * 2 * kWaveKB * W;
+    return true;
+  };
+  T vin[C], vp[C];
+  auto load_step = [&](int t) {
+    const int tb = t % kWaveKB;
+    const int n_blk = min(kWaveKB, R - (t - tb));
+    const int rib = BWD ? (n_blk - 1 - tb) : tb;
+    lds_row<T, C>(din + (size_t)rib * W + lane * C, vin);
+    lds_row<T, C>(din + (size_t)(kWaveKB + rib) * W + lane * C, vp);
+  };
+  // the consumer may be at most D steps behind; arm its slot for step t
+  int next_seen = 0;
+  auto open_dst = [&](int t) -> bool {
+    if (next_seen <= t - kWaveD) {
+      long long spins = 0;
+      for (;;) {
+        next_seen = ld_remote_relaxed(dst.prog);  // a shared::cta address is valid here too
+        if (next_seen > t - kWaveD) break;
+        if (++spins > kSpinLimit || ld_vol(failed)) {
+          if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_RING, failed);
+          return false;
+        }
+      }
+    }
+    if (lane == 0) mbar_arm_remote(dst.rbar + (unsigned)((t % kWaveD) * sizeof(uint64_t)), rowb);
+    return true;
+  };
+  if (!enter_block(0)) ok = false;
+  if (ok) load_step(0);
+  if (ok && has_dst) ok = open_dst(0);
   T cy[C];
 #pragma unroll
   for (int j = 0; j < C; j++) cy[j] = T(0);
   T edge = T(0);
-  int next_seen = 0;
-  bool ok = true;
-  const T* din = tma;
   for (int t = 0; t < R && ok; t++) {
-    const int tb = t % kWaveKB;
-    if (tb == 0) {
-      // a new block: issue block j+PF-1 into the slot freed by block j-1
-      const int j = t / kWaveKB;
-      if (j + kWavePF - 1 < nblocks) {
-        if (lane == 0) issue(j + kWavePF - 1);
-        issued = j + kWavePF;
-      }
-      const int slot = j % kWavePF;
-      long long spins = 0;
-      while (!mbar_try_wait(&bar[slot], (tparity >> slot) & 1u)) {
-        if (++spins > kSpinLimitSlow) {
-          ok = false;
-          break;
-        }
-      }
-      if (!ok) {
-        if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_TMA, failed);
-        break;
-      }
-      tparity ^= 1u << slot;
-      consumed = j + 1;
-      din = tma + (size_t)slot * 2 * kWaveKB * W;
-    }
-    // row of this step inside the block (the block is stored ascending)
-    const int n_blk = min(kWaveKB, R - (t - tb));
-    const int rib = BWD ? (n_blk - 1 - tb) : tb;
-    T vin[C], vp[C];
-#pragma unroll
-    for (int j = 0; j < C; j++) {
-      vin[j] = din[(size_t)rib * W + lane * C + j];
-      vp[j] = din[(size_t)(kWaveKB + rib) * W + lane * C + j];
-    }
-    // neighbour-plane values of this step
+    // ---- critical chain: neighbour value -> cell updates -> hand-off ----
     T cz[C];
     const int rs = t % kWaveD;
     if (no_input) {
@@ -344,9 +397,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
         break;
       }
       rparity ^= 1u << rs;
-      const T* rin = ring_in + (size_t)rs * W;
-#pragma unroll
-      for (int j = 0; j < C; j++) cz[j] = rin[lane * C + j];
+      lds_row<T, C>(ring_in + (size_t)rs * W + lane * C, cz);
     }
     T cx = BWD ? __shfl_down_sync(0xffffffffu, edge, 1) : __shfl_up_sync(0xffffffffu, edge, 1);
     if (BWD ? (lane == 31) : (lane == 0)) cx = T(0);
@@ -366,29 +417,13 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
       }
       edge = pass[0];
     }
-#pragma unroll
-    for (int j = 0; j < C; j++) cy[j] = pass[j];
-    // hand this step to the consumer plane (bounded back-pressure on its ring)
     if (has_dst) {
-      if (next_seen <= t - kWaveD) {
-        long long spins = 0;
-        for (;;) {
-          next_seen = ld_remote_relaxed(dst.prog);  // a shared::cta address is valid here too
-          if (next_seen > t - kWaveD) break;
-          if (++spins > kSpinLimit || ld_vol(failed)) {
-            ok = false;
-            break;
-          }
-        }
-        if (!ok) {
-          if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_RING, failed);
-          break;
-        }
-      }
       const unsigned off = (unsigned)(((size_t)rs * W + lane * C) * sizeof(T));
       st_async_row<T, C>(dst.ring + off, pass, dst.rbar + (unsigned)(rs * sizeof(uint64_t)));
     }
-    // output row
+    // ---- off the chain: output, next step's inputs, bookkeeping ----
+#pragma unroll
+    for (int j = 0; j < C; j++) cy[j] = pass[j];
     T* orow = outp + (size_t)(BWD ? (R - 1 - t) : t) * W + lane * C;
     if (sizeof(T) == 4 && C % 4 == 0) {
 #pragma unroll
@@ -398,21 +433,26 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
 #pragma unroll
       for (int j = 0; j < C; j++) orow[j] = vout[j];
     }
-    // every 4 steps: report consumption and re-arm the consumed ring slots
-    if ((t & 3) == 3 || t + 1 == R) {
+    if ((t & 3) == 3 || t + 1 == R) {  // report consumed ring steps (back-pressure)
       __syncwarp();
-      if (lane == 0) {
-        st_vol(&sm.prog[warp], t + 1);
-        if (!no_input)
-          for (int u = (t & ~3); u <= t; u++)
-            if (u + kWaveD < R) mbar_arm(&rbar_in[u % kWaveD], rowb);
-      }
+      if (lane == 0) st_vol(&sm.prog[warp], t + 1);
     }
-    // boundary plane of the courier path: make rows visible GPU-wide every K
     if (feed_fence && ((t + 1) % feed_K == 0 || t + 1 == R)) {
+      // boundary plane of the courier path: rows visible GPU-wide every K
       __threadfence();
       __syncwarp();
       if (lane == 0) st_vol(&sm.misc[2], t + 1);
+    }
+    if (t + 1 < R) {
+      if ((t + 1) % kWaveKB == 0 && !enter_block(t + 1)) {
+        ok = false;
+        break;
+      }
+      load_step(t + 1);
+      if (has_dst && !open_dst(t + 1)) {
+        ok = false;
+        break;
+      }
     }
   }
   // every issued TMA block must land before its slot is reused or the CTA exits
@@ -568,6 +608,7 @@ __global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
               T v[C];
 #pragma unroll
               for (int j = 0; j < C; j++) v[j] = BWD ? o[i][j] : pv[i][j] * o[i][j];
+              if (lane == 0) mbar_arm_remote(rbar0 + (unsigned)(rs * sizeof(uint64_t)), rowb);
               st_async_row<T, C>(ring0 + (unsigned)(((size_t)rs * W + lane * C) * sizeof(T)), v,
                                  rbar0 + (unsigned)(rs * sizeof(uint64_t)));
             }
