@@ -543,7 +543,7 @@ class EngineT : public Engine {
     k_.total = (long long)g_.nz * k_.plane;
     if (k_.total >= (1ll << 31)) return fail(PLUME_ERR_UNSUPPORTED, "grid too large for the solver");
     const size_t vb = align((size_t)k_.total * sizeof(T));
-    const size_t bytes = 8 * vb + align(4 * sizeof(unsigned)) + align((size_t)g_.nz * sizeof(int));
+    const size_t bytes = 9 * vb + align(4 * sizeof(unsigned)) + align((size_t)g_.nz * sizeof(int));
     cudaError_t e = cudaMalloc(&spool_, bytes);
     if (e != cudaSuccess) {
       (void)cudaGetLastError();
@@ -551,7 +551,7 @@ class EngineT : public Engine {
     }
     PL_TRY(cudaMemsetAsync(spool_, 0, bytes, s_));
     char* cur = spool_;
-    T** v[] = {&sr_, &sd_, &sq_, &sz_, &sqf_, &sx_, &sb_, &sP_};
+    T** v[] = {&sr_, &sd_, &sq_, &sz_, &sqf_, &sx_, &sb_, &sP_, &sd2_};
     for (T** p : v) {
       *p = (T*)cur;
       cur += vb;
@@ -612,6 +612,30 @@ class EngineT : public Engine {
     return PLUME_OK;
   }
 
+  // fused direction update + SpMV (skew_kernels.cuh), dispatched on C
+  int launch_spmv_dir(const T* z, const T* d_old, T* d_new, T* q) {
+    switch (k_.C) {
+#define PL_SPMV_CASE(CC)                                                                         \
+  case CC:                                                                                       \
+    k_cgs_spmv_dir<T, CC><<<kRedBlocks, SkewRows<CC>::THREADS, 0, s_>>>(g_, k_, z, d_old, d_new, q, \
+                                                                       st_, part_);             \
+    break;
+      PL_SPMV_CASE(1)
+      PL_SPMV_CASE(2)
+      PL_SPMV_CASE(3)
+      PL_SPMV_CASE(4)
+      PL_SPMV_CASE(5)
+      PL_SPMV_CASE(6)
+      PL_SPMV_CASE(7)
+      PL_SPMV_CASE(8)
+#undef PL_SPMV_CASE
+      default:
+        return fail(PLUME_ERR_UNSUPPORTED, "cells per lane");
+    }
+    PL_CHECK_LAUNCH();
+    return PLUME_OK;
+  }
+
   WaveArgs<T> wave_args(const T* in, T* out, int backward) {
     WaveArgs<T> a;
     a.P = sP_;
@@ -655,21 +679,25 @@ class EngineT : public Engine {
     PL_CHECK_LAUNCH();
     int rc = mic_sweeps(sr_, sqf_, sz_);
     if (rc != PLUME_OK) return rc;
-    k_cgs_init2<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sr_, sz_, sd_, st_, part_);
+    k_cgs_init2<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sr_, sz_, (T*)nullptr, st_, part_);
     PL_CHECK_LAUNCH();
+    // zeroed so that 0 * d_old on the first iteration can never see stale
+    // non-finite values
+    PL_TRY(cudaMemsetAsync(sd_, 0, (size_t)k_.total * sizeof(T), s_));
     int chunk = 4;
+    T* dcur = sd_;  // direction of the previous iteration (beta = 0 on the first)
+    T* dnext = sd2_;
     for (int it = 0; it < p_.max_iters + chunk;) {
       for (int kk = 0; kk < chunk; kk++) {
-        k_cgs_spmv<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, k_, sd_, sq_, st_, part_);
-        PL_CHECK_LAUNCH();
-        k_cgs_axpy<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sd_, sq_, sx_, sr_, st_, part_);
+        rc = launch_spmv_dir(sz_, dcur, dnext, sq_);
+        if (rc != PLUME_OK) return rc;
+        k_cgs_axpy_v<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, dnext, sq_, sx_, sr_, st_, part_);
         PL_CHECK_LAUNCH();
         rc = mic_sweeps(sr_, sqf_, sz_);
         if (rc != PLUME_OK) return rc;
-        k_cgs_rz<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sr_, sz_, st_, part_);
+        k_cgs_rz_v<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sr_, sz_, st_, part_);
         PL_CHECK_LAUNCH();
-        k_cgs_dir<T><<<gK, 256, 0, s_>>>(k_, sz_, sd_, st_);
-        PL_CHECK_LAUNCH();
+        std::swap(dcur, dnext);
       }
       it += chunk;
       PL_TRY(cudaMemcpyAsync(st_host_, st_, sizeof(CgState), cudaMemcpyDeviceToHost, s_));
@@ -805,7 +833,7 @@ class EngineT : public Engine {
   Skew k_{};
   char* spool_ = nullptr;
   T *sr_ = nullptr, *sd_ = nullptr, *sq_ = nullptr, *sz_ = nullptr, *sqf_ = nullptr, *sx_ = nullptr,
-    *sb_ = nullptr, *sP_ = nullptr;
+    *sb_ = nullptr, *sP_ = nullptr, *sd2_ = nullptr;
   unsigned* wave_ctl_ = nullptr;
   int* wave_prog_ = nullptr;
   int bz_ = 8, wave_k_ = 8, nslabs_ = 1, wave_grid_ = 1, num_sms_ = 1;

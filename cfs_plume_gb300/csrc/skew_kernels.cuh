@@ -106,7 +106,7 @@ __global__ void k_cgs_init2(Skew k, const T* r, const T* z, T* d, CgState* st, d
   T rz = T(0), rr = T(0);
   PL_GRID_STRIDE(e, (int)k.total) {
     const T zi = z[e], ri = r[e];
-    d[e] = zi;
+    if (d) d[e] = zi;
     rz += ri * zi;
     rr += ri * ri;
   }
@@ -120,6 +120,7 @@ __global__ void k_cgs_init2(Skew k, const T* r, const T* z, T* d, CgState* st, d
     if (threadIdx.x == 0) {
       st->deltaNew = trz;
       st->rr = trr;
+      st->beta = 0.0;  // the first direction is z itself
       if (st->wave_err) st->done = 3;
       if (st->criterion == 0) {
         st->maxR = 2.0 * st->tol;
@@ -237,6 +238,201 @@ __global__ void k_cgs_dir(Skew k, const T* z, T* d, const CgState* st) {
   if (st->done) return;
   const T beta = (T)st->beta;
   PL_GRID_STRIDE(e, (int)k.total) d[e] = d[e] * beta + z[e];
+}
+
+// ----------------------------------------------------- fused fast path
+// Rows of the skewed layout are walked whole: thread (row, ix) with the row
+// width W = 32*C known at compile time, so no per-element division.
+template <int C>
+struct SkewRows {
+  static constexpr int W = 32 * C;
+  static constexpr int RPB = (256 / W) > 0 ? (256 / W) : 1;  // rows per block pass
+  static constexpr int THREADS = RPB * W;
+};
+
+// Iteration part 1 with the direction update folded in:
+//   d = z + beta * d_old   (FLUID_3D_MIC.cpp:995-996, `_direction *= beta;
+//                           _direction += _z`, same rounding order)
+//   q = A d, d.q, alpha = deltaNew / d.q
+// Each cell rebuilds its neighbours' new direction values instead of reading
+// a separately written d, so the update costs no extra pass.  beta = 0 on the
+// first iteration (d = z).  d is double-buffered: reads d_old, writes d_new.
+template <typename T, int C>
+__global__ void __launch_bounds__(SkewRows<C>::THREADS) k_cgs_spmv_dir(Grid g, Skew k, const T* z,
+                                                                        const T* d_old, T* d_new,
+                                                                        T* q, CgState* st,
+                                                                        double* part) {
+  if (st->done) return;
+  __shared__ double sh[32];
+  constexpr int W = SkewRows<C>::W, RPB = SkewRows<C>::RPB;
+  const int ix = threadIdx.x % W, lr = threadIdx.x / W;
+  const int lb = ix / C, jb = ix - lb * C;
+  const T beta = (T)st->beta;
+  const int plane = (int)k.plane;
+  const int nrows = k.nz * k.R;
+  T dq = T(0);
+  for (int row = blockIdx.x * RPB + lr; row < nrows; row += gridDim.x * RPB) {
+    const int iz = row / k.R;
+    const int sr = row - iz * k.R;
+    const int iy = sr - lb;
+    const int e = row * W + ix;
+    T dn = T(0), qq = T(0);
+    if (ix < k.nx && iy >= 0 && iy < k.ny) {
+      const int x = ix + 1, y = iy + 1, zz = iz + 1;
+      dn = d_old[e] * beta + z[e];
+      const T vxm = ix > 0 ? (jb > 0 ? d_old[e - 1] * beta + z[e - 1]
+                                     : d_old[e - W - 1] * beta + z[e - W - 1])
+                           : T(0);
+      const T vxp = ix + 1 < k.nx ? (jb < C - 1 ? d_old[e + 1] * beta + z[e + 1]
+                                                : d_old[e + W + 1] * beta + z[e + W + 1])
+                                  : T(0);
+      const T vym = iy > 0 ? d_old[e - W] * beta + z[e - W] : T(0);
+      const T vyp = iy + 1 < k.ny ? d_old[e + W] * beta + z[e + W] : T(0);
+      const T vzm = iz > 0 ? d_old[e - plane] * beta + z[e - plane] : T(0);
+      const T vzp = iz + 1 < k.nz ? d_old[e + plane] * beta + z[e + plane] : T(0);
+      qq = adiag<T>(g, x, y, zz) * dn + vxm * coef<T>(wall_xm(g, x)) + vxp * coef<T>(wall_xp(g, x)) +
+           vym * coef<T>(wall_ym(g, y)) + vyp * coef<T>(wall_yp(g, y)) +
+           vzm * coef<T>(wall_zm(g, zz)) + vzp * coef<T>(wall_zp(g, zz));
+      dq += dn * qq;
+    }
+    d_new[e] = dn;
+    q[e] = qq;
+  }
+  const double sblk = block_sum((double)dq, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = sblk;
+  if (arrive_last(&st->ticket[0])) {
+    const double t = sum_partials(part, sh);
+    if (threadIdx.x == 0) {
+      st->dq = t;
+      if (fabs(t) > 0.0) {
+        st->alpha = st->deltaNew / t;
+      } else {  // "PCG alpha broke down! Bailing." (FLUID_3D_MIC.cpp:962-969)
+        st->done = 1;
+        st->broke = 1;
+      }
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// 16-byte vector type of T
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  typedef float4 type;
+  static constexpr int n = 4;
+};
+template <>
+struct Vec16<double> {
+  typedef double2 type;
+  static constexpr int n = 2;
+};
+template <typename T>
+__device__ inline T vget(const typename Vec16<T>::type& v, int i);
+template <>
+__device__ inline float vget<float>(const float4& v, int i) {
+  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+template <>
+__device__ inline double vget<double>(const double2& v, int i) {
+  return i == 0 ? v.x : v.y;
+}
+template <typename T>
+__device__ inline void vset(typename Vec16<T>::type& v, int i, T x);
+template <>
+__device__ inline void vset<float>(float4& v, int i, float x) {
+  if (i == 0) v.x = x; else if (i == 1) v.y = x; else if (i == 2) v.z = x; else v.w = x;
+}
+template <>
+__device__ inline void vset<double>(double2& v, int i, double x) {
+  if (i == 0) v.x = x; else v.y = x;
+}
+
+// Iteration part 2, vectorised: x += alpha d, r -= alpha q, signed max(r), r.r
+template <typename T>
+__global__ void k_cgs_axpy_v(Skew k, const T* d, const T* q, T* x, T* r, CgState* st, double* part) {
+  if (st->done) return;
+  typedef typename Vec16<T>::type V;
+  constexpr int NV = Vec16<T>::n;
+  __shared__ double sh[32];
+  const T alpha = (T)st->alpha;
+  T mx = T(-3.0e38), rr = T(0);
+  const int nvec = (int)(k.total / NV);
+  const V* dv = reinterpret_cast<const V*>(d);
+  const V* qv = reinterpret_cast<const V*>(q);
+  V* xv = reinterpret_cast<V*>(x);
+  V* rv = reinterpret_cast<V*>(r);
+  PL_GRID_STRIDE(i, nvec) {
+    const V dd = dv[i], qq = qv[i];
+    V xx = xv[i], ri = rv[i];
+#pragma unroll
+    for (int c = 0; c < NV; c++) {
+      vset<T>(xx, c, vget<T>(xx, c) + alpha * vget<T>(dd, c));
+      const T rn = vget<T>(ri, c) + (-alpha) * vget<T>(qq, c);
+      vset<T>(ri, c, rn);
+      mx = (rn > mx) ? rn : mx;
+      rr += rn * rn;
+    }
+    xv[i] = xx;
+    rv[i] = ri;
+  }
+  const double s1 = block_max((double)mx, sh, -1.0e308);
+  if (threadIdx.x == 0) part[blockIdx.x] = s1;
+  const double s2 = block_sum((double)rr, sh);
+  if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
+  if (arrive_last(&st->ticket[0])) {
+    const double tm = max_partials(part, sh);
+    const double trr = sum_partials(part + kRedBlocks, sh);
+    if (threadIdx.x == 0) {
+      st->oldMaxR = st->maxR;
+      st->maxR = tm > 0.0 ? tm : 0.0;  // FIELD_3D::max starts at a border cell (0)
+      st->rr = trr;
+      if (st->criterion == 1 && sqrt(trr) <= st->tol * sqrt(st->bb)) {
+        st->iter += 1;
+        st->done = 1;
+        st->converged = 1;
+      }
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// Iteration part 3, vectorised: deltaNew = r.z, beta, exit tests
+template <typename T>
+__global__ void k_cgs_rz_v(Skew k, const T* r, const T* z, CgState* st, double* part) {
+  if (st->done) return;
+  typedef typename Vec16<T>::type V;
+  constexpr int NV = Vec16<T>::n;
+  __shared__ double sh[32];
+  T rz = T(0);
+  const int nvec = (int)(k.total / NV);
+  const V* rv = reinterpret_cast<const V*>(r);
+  const V* zv = reinterpret_cast<const V*>(z);
+  PL_GRID_STRIDE(i, nvec) {
+    const V a = rv[i], b = zv[i];
+#pragma unroll
+    for (int c = 0; c < NV; c++) rz += vget<T>(a, c) * vget<T>(b, c);
+  }
+  const double s = block_sum((double)rz, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (arrive_last(&st->ticket[0])) {
+    const double t = sum_partials(part, sh);
+    if (threadIdx.x == 0) {
+      st->deltaOld = st->deltaNew;
+      st->deltaNew = t;
+      st->beta = t / st->deltaOld;
+      st->iter += 1;
+      if (st->wave_err) st->done = 3;
+      if (st->criterion == 0) {
+        const double relative = fabs((st->maxR - st->oldMaxR) / st->oldMaxR);
+        if (relative < 1e-7) st->done = st->done ? st->done : 2;  // stagnation bail
+        if (!(st->maxR > st->tol)) st->converged = 1;
+      }
+      if (st->converged || st->iter >= st->max_iters) st->done = st->done ? st->done : 1;
+      st->ticket[0] = 0;
+    }
+  }
 }
 
 }  // namespace plume
