@@ -1,0 +1,189 @@
+// fluid3d_main.cpp -- `fluid3D <cfg>`: the full-rank snapshot stage of the
+// pipeline, as a drop-in for the reference's projects/fluid3D/fluid3D.cpp
+// (main 300-353, runEverytime 357-398) without the GLUT window and movie.
+//
+// Same command line, same cfg keys and defaults, same outputs:
+//   <snapshot path>fluid.%04i.fluid3d.gz        FLUID_3D_MIC::writeGz format
+//   <snapshot path>velocity.*.matrix.transpose  FLUID_3D_MIC::appendStreams rows
+//   <snapshot path>pressure.matrix.transpose    (+ the .dims files)
+// so svdOutOfCoreMultiple and cubatureGeneratorStamStaged read them unchanged.
+//
+// Keys read by the reference (fluid3D.cpp:313-343): xres yres zres vorticity
+// front back left right top bottom, snapshot path, simulation snapshots.
+// Additional keys, whose defaults reproduce the reference:
+//   buoyancy (0.1f), source (column | box), source box = x0 y0 z0 x1 y1 z1,
+//   source noise (0), seed (0), precision (fp64 | fp32), solver criterion
+//   (reference | rel2), solver tolerance (1e-10), solver max iterations (1000),
+//   mic tau (0.97), mic sigma (0.25), damping (0.9), warm start (zero |
+//   previous), write state (1), write streams (1), device (0).
+#include <sys/stat.h>
+
+#include <cctype>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/plume.h"
+
+namespace {
+
+// Config reader with the reference parser's rules (SIMPLE_PARSER.cpp:53-195):
+// `key = value` lines of at most 511 characters, '#' comments only at
+// column 0, keys lower-cased and trimmed, values trimmed, numbers via atof,
+// unknown keys ignored, a non-empty line without '=' is an error.
+class Config {
+ public:
+  bool load(const std::string& path, std::string& err) {
+    std::ifstream f(path.c_str());
+    if (!f.good()) {
+      err = "Failed to open file " + path;
+      return false;
+    }
+    char buffer[512];
+    int line_no = 1;
+    while (!f.eof()) {
+      f.getline(buffer, 512);
+      if (f.fail() && !f.eof()) f.clear();  // over-long line: keep the first 511 chars
+      std::string line(buffer);
+      if (line.empty() || line[0] == '#') continue;
+      const size_t pos = line.find('=');
+      if (pos != std::string::npos) {
+        std::string lhs = trim(line.substr(0, pos));
+        const std::string rhs = trim(line.substr(pos + 1));
+        for (char& c : lhs) c = (char)tolower((unsigned char)c);
+        vals_[lhs] = rhs;
+      } else if (!trim(line).empty()) {
+        err = "Unable to parse, error in line " + std::to_string(line_no) + ": '" + line + "'";
+        return false;
+      }
+      line_no++;
+    }
+    return true;
+  }
+  bool has(const std::string& k) const { return vals_.count(lower(k)) != 0; }
+  double num(const std::string& k, double def) const {
+    auto it = vals_.find(lower(k));
+    return it == vals_.end() ? def : atof(it->second.c_str());
+  }
+  int integer(const std::string& k, int def) const { return (int)num(k, def); }
+  std::string str(const std::string& k, const std::string& def) const {
+    auto it = vals_.find(lower(k));
+    return it == vals_.end() ? def : it->second;
+  }
+
+ private:
+  static std::string trim(const std::string& in) {
+    size_t s = 0, e = in.size();
+    while (s < in.size() && isspace((unsigned char)in[s])) s++;
+    while (e > s && isspace((unsigned char)in[e - 1])) e--;
+    return in.substr(s, e - s);
+  }
+  static std::string lower(std::string k) {
+    for (char& c : k) c = (char)tolower((unsigned char)c);
+    return k;
+  }
+  std::map<std::string, std::string> vals_;
+};
+
+// fluid3D.cpp:40-47: create every prefix of the path
+void ensure_directory(const std::string& path) {
+  std::string built;
+  for (size_t i = 0; i < path.size(); i++) {
+    built += path[i];
+    if (path[i] == '/' || i == path.size() - 1) mkdir(built.c_str(), 0755);
+  }
+}
+
+int check(int rc, plume_handle* h, const char* what) {
+  if (rc != PLUME_OK) {
+    std::cerr << " " << what << " failed: " << plume_strerror(rc) << " (" << plume_last_error(h)
+              << ")" << std::endl;
+  }
+  return rc;
+}
+
+}  // namespace
+
+int main(int argc, char* argv[]) {
+  if (argc != 2) {  // fluid3D.cpp:303-307
+    std::cout << " Usage: " << argv[0] << " *.cfg" << std::endl;
+    return 0;
+  }
+  Config cfg;
+  std::string err;
+  if (!cfg.load(argv[1], err)) {
+    std::cerr << " " << err << std::endl;
+    return 1;
+  }
+  plume_params p;
+  plume_default_params(&p);
+  p.res[0] = cfg.integer("xRes", 48);
+  p.res[1] = cfg.integer("yRes", 64);
+  p.res[2] = cfg.integer("zRes", 48);
+  p.vorticity_eps = cfg.num("vorticity", 0);
+  const char* names[6] = {"front", "back", "left", "right", "top", "bottom"};
+  const int defaults[6] = {1, 1, 1, 1, 0, 0};
+  for (int k = 0; k < 6; k++) p.bc[k] = cfg.integer(names[k], defaults[k]);
+  p.buoyancy = cfg.num("buoyancy", (double)0.1f);
+  const std::string source = cfg.str("source", "column");
+  if (source == "box") {
+    p.source = PLUME_SRC_BOX;
+    std::istringstream box(cfg.str("source box", ""));
+    for (int k = 0; k < 3; k++) box >> p.box_lo[k];
+    for (int k = 0; k < 3; k++) box >> p.box_hi[k];
+    p.source_noise = cfg.num("source noise", 0.0);
+    p.seed = (uint64_t)cfg.num("seed", 0);
+  } else if (source == "none") {
+    p.source = PLUME_SRC_NONE;
+  }
+  if (cfg.str("precision", "fp64") == "fp32") p.precision = PLUME_PREC_FP32;
+  if (cfg.str("solver criterion", "reference") == "rel2") {
+    p.criterion = PLUME_CRIT_REL2;
+    p.tol = 1e-6;
+  }
+  p.tol = cfg.num("solver tolerance", p.tol);
+  p.max_iters = cfg.integer("solver max iterations", 1000);
+  p.mic_tau = cfg.num("mic tau", 0.97);
+  p.mic_sigma = cfg.num("mic sigma", 0.25);
+  p.damping_w = cfg.num("damping", 0.9);
+  if (cfg.str("warm start", "zero") == "previous") p.warm_start = PLUME_WARM_PREVIOUS;
+  p.device = cfg.integer("device", 0);
+  const bool write_state = cfg.integer("write state", 1) != 0;
+  const bool write_streams = cfg.integer("write streams", 1) != 0;
+  std::string snapshot_path = cfg.str("snapshot path", "./data/dummy/");
+  const int snapshots = cfg.integer("simulation snapshots", 20);
+
+  std::cout << " Using resoluion: " << p.res[0] << " " << p.res[1] << " " << p.res[2] << std::endl;
+  std::cout << " Using vorticity: " << p.vorticity_eps << std::endl;
+  for (int k = 0; k < 6; k++)
+    std::cout << " Boundary on " << names[k] << "\tis set to "
+              << (p.bc[k] == 0 ? "Neumann " : "Dirichlet ") << std::endl;
+  ensure_directory(snapshot_path);
+
+  plume_handle* h = nullptr;
+  if (check(plume_create(&p, &h), nullptr, "plume_create") != PLUME_OK) return 1;
+  int rc = PLUME_OK;
+  for (int step = 0; step < snapshots && rc == PLUME_OK; step++) {  // fluid3D.cpp:357-398
+    std::cout << " Simulation step " << 1 + step << " of " << snapshots << std::endl;
+    plume_step_stats st;
+    rc = check(plume_add_source(h, step), h, "add_source");
+    if (rc == PLUME_OK) rc = check(plume_step(h, &st), h, "step");
+    if (rc != PLUME_OK) break;
+    std::cout << "   " << st.iterations << " iterations converged to inf norm: " << st.max_residual
+              << " relative two norm: " << st.rel_residual << "  (" << st.ms_total << " ms)"
+              << std::endl;
+    if (write_state) {
+      char buffer[1024];
+      snprintf(buffer, sizeof(buffer), "%sfluid.%04i.fluid3d", snapshot_path.c_str(), step);
+      rc = check(plume_write_state(h, buffer), h, "write_state");
+    }
+    if (rc == PLUME_OK && write_streams) rc = check(plume_append_streams(h, snapshot_path.c_str()), h, "append_streams");
+  }
+  plume_destroy(h);
+  return rc == PLUME_OK ? 0 : 1;
+}
