@@ -132,6 +132,12 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+# DRAM bytes (read + write) of one sweep launch from an ncu capture of this
+# workload (profiles/mic_wave_and_cg_kernels_plume_128x192x128_fp32.md), keyed
+# by grid and field bytes.
+SWEEP_DRAM_BYTES = {((128, 192, 128), 4): 28.529152e6 + 35.84e3}
+
+
 def bytes_per_step(nint, iters, S, P):
     """Algorithmic HBM bytes of one step: each pass reads its operands once and
     writes its results once; 1 byte of cell flags per stencil pass."""
@@ -192,7 +198,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--res", default=None, help="X,Y,Z (default 128,192,128)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
-    ap.add_argument("--cpu-steps", type=int, default=1, help="oracle steps for cpu_baseline (0: skip)")
+    ap.add_argument("--cpu-steps", type=int, default=3, help="oracle steps for cpu_baseline (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=None)
     a = ap.parse_args()
     rank, world, local = dist_env()
@@ -217,10 +223,13 @@ def main():
     g.run_timed(0, a.warmup)
     clocks = ClockSampler(local)
     dist.barrier()
+    g.profile_sweeps(True)  # CUDA events around every MIC sweep launch, on the solver's stream
     g.lib.plume_sync(g.h)
     clocks.start()
     ms, stats = g.run_timed(a.warmup, a.steps)
     clk = clocks.stop()
+    sweep_ms, sweep_launches = g.sweep_times()
+    g.profile_sweeps(False)
     dist.barrier()
     ms_max = dist.max(ms)
     iters = [s.iterations for s in stats]
@@ -253,6 +262,12 @@ def main():
     step_bytes = bytes_per_step(nint, mean_iters, S, P)
     solve_bytes = sum(nint * (5 * S + 2 * P + 2) + it * bytes_per_iteration(nint, S, P) for it in iters)
     achieved_solve = solve_bytes / (ms_solve / 1000.0) / 1e9 if ms_solve > 0 else None
+    # dominant kernel: one MIC sweep launch reads r (or q) and the diagonal and
+    # writes q (or z) once per interior cell
+    sweep_bytes = nint * (2 * S + P)
+    sweep_avg_ms = sweep_ms / sweep_launches if sweep_launches else None
+    achieved_sweep = sweep_bytes / (sweep_avg_ms / 1000.0) / 1e9 if sweep_avg_ms else None
+    traffic = SWEEP_DRAM_BYTES.get((res, S))
 
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": a.steps,
@@ -269,11 +284,17 @@ def main():
         "pcg_iters_per_step": mean_iters,
         "achieved_gbs_step": step_bytes / (ms_max / a.steps / 1000.0) / 1e9,
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "poisson solve (MIC-PCG)",
-                     "achieved": achieved_solve, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved_solve / peak) if achieved_solve else None,
-                     "peak_kind": peak_kind, "traffic": None,
-                     "bytes_model": "N_int*(5S+2P+2 + iters*(16S+2P+3)) per solve"},
+        "roofline": {"bound": "hbm", "kernel": "k_mic_wave_cl (MIC(0) forward/backward sweep)",
+                     "achieved": achieved_sweep, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved_sweep / peak) if achieved_sweep else None,
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "bytes_per_launch": sweep_bytes, "ms_per_launch": sweep_avg_ms,
+                     "launches_timed": sweep_launches,
+                     "bytes_model": "N_int*(2S+P) per sweep launch",
+                     "note": "latency-bound dependency chain (i+j+k wavefront); HBM roof for reference"},
+        "solve_roofline": {"kernel": "poisson solve (all MIC-PCG kernels)", "achieved": achieved_solve,
+                           "unit": "GB/s", "frac": (achieved_solve / peak) if achieved_solve else None,
+                           "bytes_model": "N_int*(5S+2P+2 + iters*(16S+2P+3)) per solve"},
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": nbox * 8,
                 "d2h_bytes_per_step": 3 * g.N * 8},
         "clocks": clk,

@@ -473,6 +473,7 @@ class EngineT : public Engine {
     const int gK = grid_for(k_.total);
     k_to_skew<T, T><<<gK, 256, 0, s_>>>(g_, k_, r_, sr_);
     PL_CHECK_LAUNCH();
+    prof_it_ = -1;
     rc = mic_sweeps(sr_, sqf_, sz_);
     if (rc != PLUME_OK) return rc;
     PL_TRY(cudaMemsetAsync(z_, 0, (size_t)g_.N * sizeof(T), s_));
@@ -483,6 +484,10 @@ class EngineT : public Engine {
     PL_CHECK_LAUNCH();
     PL_TRY(cudaMemcpyAsync(st_host_, st_, sizeof(CgState), cudaMemcpyDeviceToHost, s_));
     PL_TRY(cudaStreamSynchronize(s_));
+    if (prof_on_) {
+      rc = prof_harvest(prof_cur_);
+      if (rc != PLUME_OK) return rc;
+    }
     if (st_host_->wave_err) return fail(PLUME_ERR_TIMEOUT, "MIC wavefront wait expired");
     rc = fetch_plane(z_, z, 1, 0);
     if (rc == PLUME_OK && q) rc = fetch_plane(qf_, q, 1, 0);
@@ -653,17 +658,66 @@ class EngineT : public Engine {
   }
 
   // MIC forward then backward sweep on skewed vectors (wavefront kernels).
+  // With sweep profiling on, CUDA events on the handle's stream bracket each
+  // of the two launches.
   int mic_sweeps(const T* r, T* q, T* z) {
     constexpr bool exact = std::is_same<T, double>::value;
+    cudaEvent_t* ev = nullptr;
+    if (prof_on_ && prof_n_[prof_cur_] + 3 <= kProfEvents) {
+      ev = &prof_ev_[prof_cur_][prof_n_[prof_cur_]];
+      prof_idx_[prof_cur_][prof_n_[prof_cur_] / 3] = prof_it_;
+      prof_n_[prof_cur_] += 3;
+      PL_TRY(cudaEventRecord(ev[0], s_));
+    }
     cudaError_t e = use_cluster_ ? launch_wave_cl<T, exact>(wave_args(r, q, 0), wave_smem_, s_)
                                  : launch_wave<T, exact>(wave_args(r, q, 0), wave_grid_, wave_smem_, s_);
     PL_TRY(e);
     ++launches_;
+    if (ev) PL_TRY(cudaEventRecord(ev[1], s_));
     e = use_cluster_ ? launch_wave_cl<T, exact>(wave_args(q, z, 1), wave_smem_, s_)
                      : launch_wave<T, exact>(wave_args(q, z, 1), wave_grid_, wave_smem_, s_);
     PL_TRY(e);
     ++launches_;
+    if (ev) PL_TRY(cudaEventRecord(ev[2], s_));
     return PLUME_OK;
+  }
+
+  // Adds up the sweep timings recorded in event buffer b, counting only the
+  // pairs of PCG iterations below `ran` (later launches of a chunk return at
+  // once because the solve had finished); every event in the buffer must have
+  // completed (the stream was synchronized after they were queued).
+  int prof_harvest(int b, int ran = 1 << 30) {
+    for (int i = 0; i + 2 < prof_n_[b]; i += 3) {
+      if (prof_idx_[b][i / 3] >= ran) continue;
+      float f = 0.f, g = 0.f;
+      PL_TRY(cudaEventElapsedTime(&f, prof_ev_[b][i], prof_ev_[b][i + 1]));
+      PL_TRY(cudaEventElapsedTime(&g, prof_ev_[b][i + 1], prof_ev_[b][i + 2]));
+      prof_ms_ += (double)f + (double)g;
+      prof_launches_ += 2;
+    }
+    prof_n_[b] = 0;
+    return PLUME_OK;
+  }
+
+  int profile_sweeps(int on) override {
+    PL_TRY(cudaStreamSynchronize(s_));
+    if (on && !prof_ev_[0][0])
+      for (auto& buf : prof_ev_)
+        for (auto& e : buf) PL_TRY(cudaEventCreate(&e));
+    prof_on_ = on != 0;
+    prof_n_[0] = prof_n_[1] = 0;
+    prof_ms_ = 0;
+    prof_launches_ = 0;
+    return PLUME_OK;
+  }
+
+  int sweep_times(double* ms, int64_t* launches) override {
+    PL_TRY(cudaStreamSynchronize(s_));
+    int rc = prof_harvest(0);
+    if (rc == PLUME_OK) rc = prof_harvest(1);
+    if (ms) *ms = prof_ms_;
+    if (launches) *launches = prof_launches_;
+    return rc;
   }
 
   // MIC-PCG (FLUID_3D_MIC.cpp:918-1015); x (natural layout) holds the initial
@@ -677,6 +731,7 @@ class EngineT : public Engine {
     k_cgs_init<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, k_, sb_, sx_, sr_, st_, part_, p_.tol,
                                                       p_.max_iters, p_.criterion);
     PL_CHECK_LAUNCH();
+    prof_it_ = -1;
     int rc = mic_sweeps(sr_, sqf_, sz_);
     if (rc != PLUME_OK) return rc;
     k_cgs_init2<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sr_, sz_, (T*)nullptr, st_, part_);
@@ -693,6 +748,7 @@ class EngineT : public Engine {
         if (rc != PLUME_OK) return rc;
         k_cgs_axpy_v<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, dnext, sq_, sx_, sr_, st_, part_);
         PL_CHECK_LAUNCH();
+        prof_it_ = it + kk;
         rc = mic_sweeps(sr_, sqf_, sz_);
         if (rc != PLUME_OK) return rc;
         k_cgs_rz_v<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sr_, sz_, st_, part_);
@@ -700,8 +756,15 @@ class EngineT : public Engine {
         std::swap(dcur, dnext);
       }
       it += chunk;
+      // the other event buffer was filled before the last synchronize: read
+      // it while this chunk runs, then fill the other one next
+      if (prof_on_) {
+        rc = prof_harvest(prof_cur_ ^ 1);
+        if (rc != PLUME_OK) return rc;
+      }
       PL_TRY(cudaMemcpyAsync(st_host_, st_, sizeof(CgState), cudaMemcpyDeviceToHost, s_));
       PL_TRY(cudaStreamSynchronize(s_));
+      prof_cur_ ^= 1;
       if (st_host_->done) break;
       if (chunk < 16) chunk *= 2;
     }
@@ -709,6 +772,14 @@ class EngineT : public Engine {
     PL_CHECK_LAUNCH();
     PL_TRY(cudaMemcpyAsync(st_host_, st_, sizeof(CgState), cudaMemcpyDeviceToHost, s_));
     PL_TRY(cudaStreamSynchronize(s_));
+    if (prof_on_) {
+      // iterations whose sweeps ran: all counted ones, less the last when the
+      // rel-L2 test stopped the solve before its sweeps (k_cgs_axpy_v)
+      int ran = st_host_->iter;
+      if (st_host_->criterion == 1 && st_host_->converged) ran -= 1;
+      rc = prof_harvest(prof_cur_ ^ 1, ran);
+      if (rc != PLUME_OK) return rc;
+    }
     if (st_host_->wave_err) {
       char buf[128];
       snprintf(buf, sizeof(buf), "MIC wavefront wait expired (code %d)", st_host_->wave_err);
@@ -810,6 +881,9 @@ class EngineT : public Engine {
     if (stage_) cudaFreeHost(stage_);
     for (auto e : ev_)
       if (e) cudaEventDestroy(e);
+    for (auto& buf : prof_ev_)
+      for (auto e : buf)
+        if (e) cudaEventDestroy(e);
     if (s_) cudaStreamDestroy(s_);
     pool_ = nullptr;
     s_ = nullptr;
@@ -848,6 +922,17 @@ class EngineT : public Engine {
   int n_col_ = 0;
   CgState* st_host_ = nullptr;
   void* stage_ = nullptr;
+  // sweep profiling: two event buffers, one filled while the other is read
+  // (three events per forward+backward pair; a chunk holds at most 17 pairs)
+  static constexpr int kProfEvents = 64;
+  bool prof_on_ = false;
+  cudaEvent_t prof_ev_[2][kProfEvents] = {};
+  int prof_n_[2] = {0, 0};
+  int prof_idx_[2][kProfEvents / 3] = {};  // PCG iteration of each pair (-1: set-up)
+  int prof_cur_ = 0;
+  int prof_it_ = -1;
+  double prof_ms_ = 0;
+  int64_t prof_launches_ = 0;
   std::string err_;
 };
 

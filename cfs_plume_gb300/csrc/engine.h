@@ -33,6 +33,11 @@ class Engine {
   virtual int mic_apply(const double* r, double* z, double* q) = 0;
   virtual int mic_precon(double* precon) = 0;
   virtual int sync() = 0;
+  // CUDA-event timing of every MIC sweep launch: on != 0 clears the totals
+  // and starts recording, 0 stops; sweep_times returns the summed device ms
+  // and the number of timed launches.
+  virtual int profile_sweeps(int on) = 0;
+  virtual int sweep_times(double* ms, int64_t* launches) = 0;
   virtual int32_t total_steps() const = 0;
   virtual double total_time() const = 0;
   virtual double dx() const = 0;

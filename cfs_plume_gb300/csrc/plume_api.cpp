@@ -231,4 +231,14 @@ int plume_sync(plume_handle* h) {
   return from_engine(h, h->eng->sync());
 }
 
+int plume_profile_sweeps(plume_handle* h, int on) {
+  if (!h) return PLUME_ERR_INVALID;
+  return from_engine(h, h->eng->profile_sweeps(on));
+}
+
+int plume_sweep_times(plume_handle* h, double* ms_total, int64_t* launches) {
+  if (!h || !ms_total || !launches) return PLUME_ERR_INVALID;
+  return from_engine(h, h->eng->sweep_times(ms_total, launches));
+}
+
 }  // extern "C"

@@ -60,6 +60,8 @@ def load_library(path=LIB_PATH):
         "plume_mic_apply": (C.c_int, [H, C.c_void_p, C.c_void_p, C.c_void_p]),
         "plume_mic_diagonal": (C.c_int, [H, C.c_void_p]),
         "plume_sync": (C.c_int, [H]),
+        "plume_profile_sweeps": (C.c_int, [H, C.c_int]),
+        "plume_sweep_times": (C.c_int, [H, P(C.c_double), P(C.c_int64)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -174,6 +176,16 @@ class Plume:
         q = np.zeros(self.N)
         _check(self.lib.plume_mic_apply(self.h, r.ctypes.data, z.ctypes.data, q.ctypes.data), self.h)
         return z, q
+
+    def profile_sweeps(self, on=True):
+        """Start (clearing the totals) or stop CUDA-event timing of every MIC sweep launch."""
+        _check(self.lib.plume_profile_sweeps(self.h, 1 if on else 0), self.h)
+
+    def sweep_times(self):
+        """(summed device ms, number of timed sweep launches) since profiling started."""
+        ms, n = C.c_double(), C.c_int64()
+        _check(self.lib.plume_sweep_times(self.h, C.byref(ms), C.byref(n)), self.h)
+        return ms.value, n.value
 
     def mic_diagonal(self):
         p = np.zeros(self.N)

@@ -34,6 +34,16 @@ int plume_mic_diagonal(plume_handle* h, double* precon);
 /* Wait for all work queued on the handle's stream. */
 int plume_sync(plume_handle* h);
 
+/* Per-launch device timing of the MIC sweep kernels (the reference's TIMER
+   around applyMICPreconditioner, FLUID_3D_MIC.cpp:866, made per launch):
+   on != 0 clears the totals and brackets every later forward and backward
+   sweep launch with CUDA events on the handle's stream; 0 stops. */
+int plume_profile_sweeps(plume_handle* h, int on);
+
+/* Totals since profiling was switched on: summed device milliseconds of the
+   timed sweep launches and their number.  Waits for the handle's stream. */
+int plume_sweep_times(plume_handle* h, double* ms_total, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

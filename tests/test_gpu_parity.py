@@ -265,3 +265,21 @@ def test_wavefront_sweeps_fp32():
     zo, _ = oracle.mic_apply(p.res, tuple(p.bc), oracle.mic_precon(p.res, tuple(p.bc)), r)
     z, _ = g.mic_apply(r)
     assert rel_l2(z, zo) < 1e-5
+
+
+@pytest.mark.gpu
+def test_sweep_profiling_counts_every_sweep_launch():
+    """plume_profile_sweeps / plume_sweep_times: one forward and one backward
+    sweep per PCG iteration plus the pair that starts the solve; under the
+    rel-L2 test the last counted iteration stops before its sweeps."""
+    p = _abi.plume_config((24, 32, 24))
+    h = Plume(p)
+    h.run_timed(0, 2)
+    h.profile_sweeps(True)
+    _, stats = h.run_timed(2, 3)
+    ms, n = h.sweep_times()
+    h.profile_sweeps(False)
+    assert all(s.converged for s in stats)
+    assert n == sum(2 * s.iterations for s in stats)
+    assert 0 < ms < sum(s.ms_solve for s in stats)
+    h.close()
