@@ -79,6 +79,7 @@ def build(verbose=False, ptxas_info=False):
         ("engine_f64.cu", [nvcc] + common_nv + ["-fmad=false"]),
         ("engine_f32.cu", [nvcc] + common_nv),
         ("noalloc.cu", [nvcc] + common_nv + ["-fmad=false"]),
+        ("unet.cu", [nvcc] + common_nv),
         ("plume_api.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-I" + os.path.join(cuda, "include")]),
         ("snapshot.cpp", ["g++", "-O2", "-std=c++17", "-fPIC"] + zc),
     ]

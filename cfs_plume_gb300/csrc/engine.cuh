@@ -17,6 +17,7 @@
 #include "common.cuh"
 #include "engine.h"
 #include "skew_kernels.cuh"
+#include "unet.h"
 #include "solver_kernels.cuh"
 #include "step_kernels.cuh"
 #include "wave.cuh"
@@ -172,8 +173,9 @@ class EngineT : public Engine {
       for (int k = 0; k < 3; k++)
         if (p.box_lo[k] < 0 || p.box_hi[k] > p.res[k] || p.box_lo[k] > p.box_hi[k])
           return fail(PLUME_ERR_INVALID, "source box outside the grid");
-    if (p.warm_start == PLUME_WARM_LEARNED)
-      return fail(PLUME_ERR_UNSUPPORTED, "learned warm start is not available in this engine");
+    if (p.warm_start != PLUME_WARM_ZERO && p.warm_start != PLUME_WARM_PREVIOUS &&
+        p.warm_start != PLUME_WARM_LEARNED)
+      return fail(PLUME_ERR_INVALID, "unknown warm start");
     g_.X = p.res[0];
     g_.Y = p.res[1];
     g_.Z = p.res[2];
@@ -354,8 +356,24 @@ class EngineT : public Engine {
     k_copy_border_all<T><<<gF, 256, 0, s_>>>(g_, pres_);
     PL_CHECK_LAUNCH();
     PL_TRY(cudaEventRecord(ev_[1], s_));
+    const bool learned = p_.warm_start == PLUME_WARM_LEARNED;
+    last_fallback_ = 0;
+    if (learned) {
+      // the network's guess on the interior; the border keeps the reference's
+      // copied zeros
+      if (!net_) return fail(PLUME_ERR_STATE, "learned warm start without an attached network");
+      const int prc = net_->predict(net_ws_, div_, pres_, std::is_same<T, double>::value ? 1 : 0, s_, err_);
+      if (prc != PLUME_OK) return prc;
+    }
     int rc = solve_device(div_, pres_);
     if (rc != PLUME_OK) return rc;
+    if (learned && !st_host_->converged) {
+      // the guess did not lead to convergence: plain MIC-PCG from p = 0
+      last_fallback_ = 1;
+      PL_TRY(cudaMemsetAsync(pres_, 0, (size_t)g_.N * sizeof(T), s_));
+      rc = solve_device(div_, pres_);
+      if (rc != PLUME_OK) return rc;
+    }
     PL_TRY(cudaEventRecord(ev_[2], s_));
     k_gradient<T><<<gI, 256, 0, s_>>>(g_, c_, vel_, pres_);
     PL_CHECK_LAUNCH();
@@ -504,6 +522,20 @@ class EngineT : public Engine {
 
   int sync() override {
     PL_TRY(cudaStreamSynchronize(s_));
+    return PLUME_OK;
+  }
+
+  const void* device_field(int field) override { return scalar_ptr(field); }
+  void* stream_handle() override { return (void*)s_; }
+  int attach_net(NetRuntime* net) override {
+    PL_TRY(cudaStreamSynchronize(s_));
+    if (net_ws_) net_->free_workspace(net_ws_);
+    net_ = nullptr;
+    net_ws_ = nullptr;
+    if (!net) return PLUME_OK;
+    net_ws_ = net->new_workspace(p_.res, err_);
+    if (!net_ws_) return fail(PLUME_ERR_INVALID, err_.empty() ? "network workspace" : err_.c_str());
+    net_ = net;
     return PLUME_OK;
   }
   int32_t total_steps() const override { return total_steps_; }
@@ -795,6 +827,7 @@ class EngineT : public Engine {
     st->iterations = st_host_->iter;
     st->launches = launches_;
     st->converged = st_host_->converged;
+    st->fallback = last_fallback_;
     st->max_residual = st_host_->maxR;
     st->rhs_norm = sqrt(st_host_->bb);
     st->rel_residual = st_host_->bb > 0 ? sqrt(st_host_->rr) / sqrt(st_host_->bb) : 0.0;
@@ -872,6 +905,8 @@ class EngineT : public Engine {
 
   void release() {
     if (s_) cudaStreamSynchronize(s_);
+    if (net_ws_) net_->free_workspace(net_ws_);
+    net_ws_ = nullptr;
     if (pool_) cudaFree(pool_);
     if (spool_) cudaFree(spool_);
     if (col_cells_) cudaFree(col_cells_);
@@ -924,6 +959,9 @@ class EngineT : public Engine {
   void* stage_ = nullptr;
   // sweep profiling: two event buffers, one filled while the other is read
   // (three events per forward+backward pair; a chunk holds at most 17 pairs)
+  NetRuntime* net_ = nullptr;
+  void* net_ws_ = nullptr;
+  int last_fallback_ = 0;
   static constexpr int kProfEvents = 64;
   bool prof_on_ = false;
   cudaEvent_t prof_ev_[2][kProfEvents] = {};

@@ -13,6 +13,8 @@
 
 namespace plume {
 
+class NetRuntime;
+
 class Engine {
  public:
   virtual ~Engine() {}
@@ -38,6 +40,12 @@ class Engine {
   // and the number of timed launches.
   virtual int profile_sweeps(int on) = 0;
   virtual int sweep_times(double* ms, int64_t* launches) = 0;
+  // Device pointer of a scalar field (field type: float or double as the
+  // engine's precision), the engine's cudaStream_t, and the network used by
+  // PLUME_WARM_LEARNED solves (nullptr detaches).
+  virtual const void* device_field(int field) = 0;
+  virtual void* stream_handle() = 0;
+  virtual int attach_net(NetRuntime* net) = 0;
   virtual int32_t total_steps() const = 0;
   virtual double total_time() const = 0;
   virtual double dx() const = 0;
@@ -47,5 +55,10 @@ class Engine {
 
 Engine* make_engine_f64();
 Engine* make_engine_f32();
+
+// C ABI helpers (plume_api.cpp): a handle's engine, and the calling thread's
+// error text for calls that have no handle.
+Engine* engine_of(plume_handle* h);
+std::string& global_error();
 
 }  // namespace plume

@@ -17,8 +17,15 @@ struct plume_handle {
   std::string err;
 };
 
+namespace plume {
+Engine* engine_of(plume_handle* h) { return h->eng; }
+std::string& global_error() {
+  static thread_local std::string e;
+  return e;
+}
+}  // namespace plume
+
 namespace {
-thread_local std::string g_create_error;
 
 int set_err(plume_handle* h, int code, const std::string& msg) {
   if (h) h->err = msg;
@@ -61,15 +68,15 @@ int plume_create(const plume_params* p, plume_handle** out) {
   if (!out) return PLUME_ERR_INVALID;
   *out = nullptr;
   if (!p) {
-    g_create_error = "null params";
+    plume::global_error() = "null params";
     return PLUME_ERR_INVALID;
   }
   if (p->abi_version != PLUME_ABI_VERSION) {
-    g_create_error = "abi_version mismatch";
+    plume::global_error() = "abi_version mismatch";
     return PLUME_ERR_INVALID;
   }
   if (p->precision != PLUME_PREC_FP64 && p->precision != PLUME_PREC_FP32) {
-    g_create_error = "unknown precision";
+    plume::global_error() = "unknown precision";
     return PLUME_ERR_INVALID;
   }
   plume_handle* h = new (std::nothrow) plume_handle();
@@ -77,7 +84,7 @@ int plume_create(const plume_params* p, plume_handle** out) {
   h->eng = (p->precision == PLUME_PREC_FP64) ? plume::make_engine_f64() : plume::make_engine_f32();
   const int rc = h->eng->init(*p);
   if (rc != PLUME_OK) {
-    g_create_error = h->eng->last_error();
+    plume::global_error() = h->eng->last_error();
     delete h->eng;
     delete h;
     return rc;
@@ -206,7 +213,7 @@ const char* plume_strerror(int status) {
 }
 
 const char* plume_last_error(plume_handle* h) {
-  if (!h) return g_create_error.c_str();
+  if (!h) return plume::global_error().c_str();
   return h->err.c_str();
 }
 
