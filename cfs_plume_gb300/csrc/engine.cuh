@@ -200,7 +200,7 @@ class EngineT : public Engine {
     const size_t n = (size_t)g_.N;
     const size_t aT = align(n * sizeof(T));
     const size_t bytes = 37 * aT + align(n * sizeof(double)) + align(n) +
-                         align(sizeof(CgState)) + align(2 * kRedBlocks * sizeof(double));
+                         align(sizeof(CgState)) + align(3 * kRedBlocks * sizeof(double));
     cudaError_t e = cudaMalloc(&pool_, bytes);
     if (e != cudaSuccess) {
       (void)cudaGetLastError();
@@ -221,7 +221,7 @@ class EngineT : public Engine {
     P64_ = (double*)take(n * sizeof(double));
     obst_ = (uint8_t*)take(n);
     st_ = (CgState*)take(sizeof(CgState));
-    part_ = (double*)take(2 * kRedBlocks * sizeof(double));
+    part_ = (double*)take(3 * kRedBlocks * sizeof(double));
 
     // obstacle slabs (FLUID_3D_MIC.cpp:105-159), kept for download and the
     // state file; kernels derive walls from the flags.
@@ -364,6 +364,11 @@ class EngineT : public Engine {
       if (!net_) return fail(PLUME_ERR_STATE, "learned warm start without an attached network");
       const int prc = net_->predict(net_ws_, div_, pres_, std::is_same<T, double>::value ? 1 : 0, s_, err_);
       if (prc != PLUME_OK) return prc;
+      // Galerkin scaling: the guess is never worse than p = 0 in the A-norm
+      k_guess_scale_dots<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, pres_, div_, st_, part_);
+      PL_CHECK_LAUNCH();
+      k_guess_scale_apply<T><<<gI, 256, 0, s_>>>(g_, pres_, st_);
+      PL_CHECK_LAUNCH();
     }
     int rc = solve_device(div_, pres_);
     if (rc != PLUME_OK) return rc;

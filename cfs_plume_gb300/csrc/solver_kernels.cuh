@@ -22,6 +22,8 @@ struct CgState {
   double rr, bb;         // r.r and b.b
   double dq;             // d.(A d)
   double tol;            // absolute (reference) or relative (rel2) tolerance
+  double guess_scale;    // Galerkin factor of the last learned initial guess
+  double guess_mean;     // interior mean removed from it (closed boxes)
   int iter, max_iters, criterion, done;
   int converged, broke, wave_err, pad1;
   unsigned int ticket[4];
@@ -85,6 +87,64 @@ __device__ inline double max_partials(const double* part, double* sh) {
     s = v > s ? v : s;
   }
   return block_max(s, sh, -1.0e308);
+}
+
+// ------------------------------------------------- scaled initial guess
+// alpha = (x.b) / (x.A x) over the interior minimises the A-norm error of
+// alpha * x among multiples of a guess x, so alpha * x is never further from
+// the solution than x = 0 in that norm (the norm CG's error bound starts
+// from).  With all six walls closed the constant vector is in A's null space:
+// the A-norm does not see it, but a large constant offset in an FP32 guess
+// sets a rounding floor under the residual, so the guess's interior mean is
+// removed (x.A x is unchanged by it and x.b only through sum(b), which the
+// closed-box divergence keeps at round-off).  Writes st->guess_scale = alpha
+// (0 when x.A x is not positive or a sum is not finite) and st->guess_mean;
+// st->ticket[3] is left at 0.  Grid: kRedBlocks blocks; part holds
+// 3 * gridDim.x doubles.
+template <typename T>
+__global__ void k_guess_scale_dots(Grid g, const T* x, const T* b, CgState* st, double* part) {
+  __shared__ double sh[32];
+  double xb = 0.0, xax = 0.0, xs = 0.0;
+  PL_GRID_STRIDE(k, g.nint) {
+    int cx, cy, cz;
+    const int i = interior_cell(g, k, cx, cy, cz);
+    const double xi = (double)x[i];
+    xb += xi * (double)b[i];
+    xax += xi * (double)mult_a_cell(g, x, i, cx, cy, cz);
+    xs += xi;
+  }
+  const double s1 = block_sum(xb, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s1;
+  const double s2 = block_sum(xax, sh);
+  if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = s2;
+  const double s3 = block_sum(xs, sh);
+  if (threadIdx.x == 0) part[2 * gridDim.x + blockIdx.x] = s3;
+  if (arrive_last(&st->ticket[3])) {
+    const double t1 = sum_partials(part, sh);
+    const double t2 = sum_partials(part + gridDim.x, sh);
+    const double t3 = sum_partials(part + 2 * gridDim.x, sh);
+    if (threadIdx.x == 0) {
+      const bool closed = g.wall[0] && g.wall[1] && g.wall[2] && g.wall[3] && g.wall[4] && g.wall[5];
+      const double mean = closed ? t3 / (double)g.nint : 0.0;
+      const double a = t2 > 0.0 ? t1 / t2 : 0.0;
+      const bool ok = isfinite(a) && isfinite(mean);
+      st->guess_scale = ok ? a : 0.0;
+      st->guess_mean = ok ? mean : 0.0;
+      st->ticket[3] = 0;
+    }
+  }
+}
+
+// x = alpha * (x - mean) on the interior; exactly 0 when alpha is 0 (so a
+// non-finite guess never survives)
+template <typename T>
+__global__ void k_guess_scale_apply(Grid g, T* x, const CgState* st) {
+  const double a = st->guess_scale, m = st->guess_mean;
+  PL_GRID_STRIDE(k, g.nint) {
+    int cx, cy, cz;
+    const int i = interior_cell(g, k, cx, cy, cz);
+    x[i] = a == 0.0 ? T(0) : (T)(a * ((double)x[i] - m));
+  }
 }
 
 // ------------------------------------------------------------ MIC diagonal

@@ -181,7 +181,7 @@ struct Workspace {
   bf16 *g_p1 = nullptr, *g_d2b = nullptr, *g_d2a = nullptr, *g_cat2 = nullptr, *g_e2b = nullptr,
        *g_e2a = nullptr;
   bf16 *g_p2 = nullptr, *g_b3b = nullptr, *g_b3a = nullptr;
-  float *y = nullptr, *t = nullptr, *gy = nullptr, *host_in = nullptr;
+  float *y = nullptr, *t = nullptr, *gy = nullptr, *host_in = nullptr, *ebuf = nullptr;
   float* part = nullptr;  // weight-gradient partial sums
   float* misc = nullptr;  // bias / loss / output-layer partial sums
   double* dpart = nullptr;
@@ -246,6 +246,7 @@ struct Workspace {
       act(&g_b3a, 64, 2);
       req.push_back({(void**)&t, al(n1 * 4)});
       req.push_back({(void**)&gy, al(n1 * 4)});
+      req.push_back({(void**)&ebuf, al(n1 * 4)});
       req.push_back({(void**)&part, al(wgrad_part_floats() * 4)});
       req.push_back({(void**)&misc, al((size_t)kMaxBlocks * 64 * 4)});
       req.push_back({(void**)&idx, al((size_t)nb * 4)});
@@ -390,20 +391,36 @@ class Net : public NetRuntime {
     return PLUME_OK;
   }
 
-  // loss against ws.t (added to ws.loss_acc as a sum of squares) and the
-  // gradient of the mean loss in g_ (every parameter written)
-  int backward(Workspace& ws, int nb, double inv_count, cudaStream_t s, std::string& err) {
+  // Loss of ws.y against ws.t over interior cells, its sum added to
+  // ws.loss_acc and d(sum * inv_count)/dy in ws.gy.  kind 0: squared error;
+  // kind 1: energy norm e^T A e of the error (+ 1e-4 e^T e, which pins the
+  // constant mode the closed-box operator does not see).
+  int loss(Workspace& ws, int nb, int kind, double inv_count, cudaStream_t s, std::string& err) {
     const Dims* d = ws.d;
     const long long n1 = d[0].cells * nb;
     const int lb = blocks_for(n1);
-    k_loss<<<lb, kThreads, 0, s>>>(d[0], nb, ws.y, ws.t, ws.gy, (float)inv_count, ws.misc);
-    NT_LAUNCH();
-    {  // loss_acc += sum of the block partials (double)
-      k_sum_parts<<<1, 32, 0, s>>>(ws.misc, lb, 1, ws.misc + kMaxBlocks * 64 - 1, 0);
+    if (kind == 1) {
+      k_err<<<lb, kThreads, 0, s>>>(d[0], nb, ws.y, ws.t, ws.ebuf);
       NT_LAUNCH();
-      k_add_to_double<<<1, 1, 0, s>>>(ws.misc + kMaxBlocks * 64 - 1, ws.loss_acc);
-      NT_LAUNCH();
+      k_loss_energy<<<lb, kThreads, 0, s>>>(d[0], nb, ws.ebuf, ws.gy, (float)inv_count, 1e-4f, ws.misc);
+    } else {
+      k_loss<<<lb, kThreads, 0, s>>>(d[0], nb, ws.y, ws.t, ws.gy, (float)inv_count, ws.misc);
     }
+    NT_LAUNCH();
+    k_sum_parts<<<1, 32, 0, s>>>(ws.misc, lb, 1, ws.misc + kMaxBlocks * 64 - 1, 0);
+    NT_LAUNCH();
+    k_add_to_double<<<1, 1, 0, s>>>(ws.misc + kMaxBlocks * 64 - 1, ws.loss_acc);
+    NT_LAUNCH();
+    return PLUME_OK;
+  }
+
+  // loss (see loss()) and the gradient of the mean loss in g_ (every
+  // parameter written)
+  int backward(Workspace& ws, int nb, int kind, double inv_count, cudaStream_t s, std::string& err) {
+    const Dims* d = ws.d;
+    const long long n1 = d[0].cells * nb;
+    int lrc = loss(ws, nb, kind, inv_count, s, err);
+    if (lrc != PLUME_OK) return lrc;
     const int ob = blocks_for(n1);
     k_out_bwd<<<ob, kThreads, 0, s>>>(d[0].cells, nb, view(ws.d1b, 16, d[0]), w_ + woff_[NCONV], ws.gy,
                                       view(ws.g_d1b, 16, d[0]), ws.misc);
@@ -695,9 +712,9 @@ int plume_net_forward(plume_net* net, const int32_t res[3], int32_t batch, const
   return PLUME_OK;
 }
 
-int plume_net_loss_grad(plume_net* net, const int32_t res[3], int32_t batch, const float* input,
-                        const float* target, double* loss, float* grad) {
-  if (!net || !res || !input || !target || !loss || !grad || batch < 1)
+int plume_net_loss_grad(plume_net* net, const int32_t res[3], int32_t batch, int32_t loss_kind,
+                        const float* input, const float* target, double* loss, float* grad) {
+  if (!net || !res || !input || !target || !loss || !grad || batch < 1 || loss_kind < 0 || loss_kind > 1)
     return fail(PLUME_ERR_INVALID, "bad argument");
   std::string err;
   Net& m = net->net;
@@ -709,7 +726,7 @@ int plume_net_loss_grad(plume_net* net, const int32_t res[3], int32_t batch, con
   NT(cudaMemcpyAsync(ws.t, target, d.cells * batch * 4, cudaMemcpyHostToDevice, m.s_));
   NT(cudaMemsetAsync(ws.loss_acc, 0, 8, m.s_));
   const double count = (double)batch * (d.X - 2) * (d.Y - 2) * (d.Z - 2);
-  rc = m.backward(ws, batch, 1.0 / count, m.s_, err);
+  rc = m.backward(ws, batch, loss_kind, 1.0 / count, m.s_, err);
   if (rc != PLUME_OK) return fail(rc, err);
   double sum = 0;
   NT(cudaMemcpyAsync(&sum, ws.loss_acc, 8, cudaMemcpyDeviceToHost, m.s_));
@@ -894,8 +911,9 @@ int plume_net_train(plume_net* net, plume_dataset* dsh, const plume_train_spec* 
   const plume_train_spec& sp = *spec;
   const Dataset& ds = dsh->ds;
   const int ntrain = ds.pairs - sp.val_pairs;
-  if (sp.epochs < 1 || sp.batch < 1 || sp.val_pairs < 0 || ntrain < sp.batch || !(sp.lr > 0.f))
-    return fail(PLUME_ERR_INVALID, "epochs, batch, val_pairs or lr out of range");
+  if (sp.epochs < 1 || sp.batch < 1 || sp.val_pairs < 0 || ntrain < sp.batch || !(sp.lr > 0.f) ||
+      sp.loss < 0 || sp.loss > 1)
+    return fail(PLUME_ERR_INVALID, "epochs, batch, val_pairs, lr or loss out of range");
   std::string err;
   Net& m = net->net;
   NT(cudaSetDevice(m.device_));
@@ -937,7 +955,7 @@ int plume_net_train(plume_net* net, plume_dataset* dsh, const plume_train_spec* 
       k_gather_batch<<<blocks_for(ws.d[0].cells * sp.batch), kThreads, 0, s>>>(
           ws.d[0].cells, sp.batch, ds.in, ds.tgt, ws.idx, inv_scale, view(ws.xin, 16, ws.d[0]), ws.t);
       rc = m.forward(ws, sp.batch, s, err);
-      if (rc == PLUME_OK) rc = m.backward(ws, sp.batch, 1.0 / (interior * sp.batch), s, err);
+      if (rc == PLUME_OK) rc = m.backward(ws, sp.batch, sp.loss, 1.0 / (interior * sp.batch), s, err);
       t += 1;
       const double frac = total_steps > 1 ? (double)(t - 1) / (double)(total_steps - 1) : 1.0;
       const float lr = sp.lr_final + 0.5f * (sp.lr - sp.lr_final) * (float)(1.0 + std::cos(3.141592653589793 * frac));
@@ -962,10 +980,8 @@ int plume_net_train(plume_net* net, plume_dataset* dsh, const plume_train_spec* 
         rc = m.forward(ws, sp.batch, s, err);
         if (rc != PLUME_OK) return fail_free(rc, err);
         cudaMemsetAsync(ws.loss_acc, 0, 8, s);
-        const int lb = blocks_for(ws.d[0].cells * sp.batch);
-        k_loss<<<lb, kThreads, 0, s>>>(ws.d[0], sp.batch, ws.y, ws.t, ws.gy, 0.f, ws.misc);
-        k_sum_parts<<<1, 32, 0, s>>>(ws.misc, lb, 1, ws.misc + kMaxBlocks * 64 - 1, 0);
-        k_add_to_double<<<1, 1, 0, s>>>(ws.misc + kMaxBlocks * 64 - 1, ws.loss_acc);
+        rc = m.loss(ws, sp.batch, sp.loss, 0.0, s, err);
+        if (rc != PLUME_OK) return fail_free(rc, err);
         double v = 0;
         cudaMemcpyAsync(&v, ws.loss_acc, 8, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return fail_free(PLUME_ERR_CUDA, "validation loss");

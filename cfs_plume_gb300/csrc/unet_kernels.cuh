@@ -572,6 +572,49 @@ __global__ void __launch_bounds__(256) k_loss(Dims d, int batch, const float* y,
   if (threadIdx.x == 0) part[blockIdx.x] = tot;
 }
 
+// e = y - t on interior cells, 0 elsewhere
+__global__ void k_err(Dims d, int batch, const float* y, const float* t, float* e) {
+  const long long n = d.cells * batch;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    e[i] = interior(d, i % d.cells) ? y[i] - t[i] : 0.f;
+}
+
+// Energy norm of the error, the quantity CG's error bound starts from:
+// loss = (e^T A e + w e^T e) / count with A the 7-point operator of a closed
+// box (diagonal = number of interior neighbours, -1 per interior neighbour);
+// gy = 2 (A e + w e) / count.  e must be 0 outside the interior.
+__global__ void __launch_bounds__(256) k_loss_energy(Dims d, int batch, const float* e, float* gy, float inv_count,
+                                                     float w, float* part) {
+  __shared__ float sh[8];
+  const long long n = d.cells * batch;
+  const long long sy = d.X, sz = (long long)d.X * d.Y;
+  float s = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long cell = i % d.cells;
+    const int x = (int)(cell % d.X), y = (int)((cell / d.X) % d.Y), z = (int)(cell / sz);
+    float g = 0.f;
+    if (x > 0 && x < d.X - 1 && y > 0 && y < d.Y - 1 && z > 0 && z < d.Z - 1) {
+      const float ei = e[i];
+      float q = 0.f;
+      int cnt = 0;
+      if (x > 1) { q -= e[i - 1]; cnt++; }
+      if (x < d.X - 2) { q -= e[i + 1]; cnt++; }
+      if (y > 1) { q -= e[i - sy]; cnt++; }
+      if (y < d.Y - 2) { q -= e[i + sy]; cnt++; }
+      if (z > 1) { q -= e[i - sz]; cnt++; }
+      if (z < d.Z - 2) { q -= e[i + sz]; cnt++; }
+      q += (float)cnt * ei;
+      s += ei * q + w * ei * ei;
+      g = 2.f * (q + w * ei) * inv_count;
+    }
+    gy[i] = g;
+  }
+  const float tot = block_sum_f<256>(s, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = tot;
+}
+
 // output-layer backward: gx = [x > 0] * w * gy (BF16); per-block partial
 // sums of dW (16) and db (1) in part[block][17]
 __global__ void __launch_bounds__(256) k_out_bwd(long long cells, int batch, View x, const float* __restrict__ w,

@@ -11,6 +11,7 @@ import numpy as np
 from .plume import PlumeError, load_library
 
 _signed = False
+LOSS_MSE, LOSS_ENERGY = 0, 1
 
 
 class PlumeDatasetSpec(C.Structure):
@@ -19,7 +20,7 @@ class PlumeDatasetSpec(C.Structure):
 
 
 class PlumeTrainSpec(C.Structure):
-    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("val_pairs", C.c_int32), ("reserved", C.c_int32),
+    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("val_pairs", C.c_int32), ("loss", C.c_int32),
                 ("lr", C.c_float), ("lr_final", C.c_float), ("seed", C.c_uint64)]
 
 
@@ -39,7 +40,7 @@ def _lib():
             "plume_net_save": (C.c_int, [V, C.c_char_p]),
             "plume_net_load": (C.c_int, [V, C.c_char_p]),
             "plume_net_forward": (C.c_int, [V, P(C.c_int32), C.c_int32, V, V]),
-            "plume_net_loss_grad": (C.c_int, [V, P(C.c_int32), C.c_int32, V, V, P(C.c_double), V]),
+            "plume_net_loss_grad": (C.c_int, [V, P(C.c_int32), C.c_int32, C.c_int32, V, V, P(C.c_double), V]),
             "plume_dataset_generate": (C.c_int, [P(PlumeDatasetSpec), P(V)]),
             "plume_dataset_destroy": (None, [V]),
             "plume_dataset_info": (C.c_int, [V, P(C.c_int32), P(C.c_double), P(C.c_double)]),
@@ -123,18 +124,18 @@ class PlumeNet:
         _check(self.lib.plume_net_forward(self.h, _res(res), batch, inp.ctypes.data, out.ctypes.data))
         return out
 
-    def loss_grad(self, inp, tgt, res):
+    def loss_grad(self, inp, tgt, res, loss=LOSS_MSE):
         inp = np.ascontiguousarray(inp, dtype=np.float32)
         tgt = np.ascontiguousarray(tgt, dtype=np.float32)
         batch = inp.size // int(np.prod(res))
-        loss = C.c_double()
+        value = C.c_double()
         grad = np.empty(self.num_params, dtype=np.float32)
-        _check(self.lib.plume_net_loss_grad(self.h, _res(res), batch, inp.ctypes.data, tgt.ctypes.data,
-                                            C.byref(loss), grad.ctypes.data))
-        return loss.value, grad
+        _check(self.lib.plume_net_loss_grad(self.h, _res(res), batch, int(loss), inp.ctypes.data,
+                                            tgt.ctypes.data, C.byref(value), grad.ctypes.data))
+        return value.value, grad
 
-    def train(self, dataset, epochs=1, batch=4, val_pairs=0, lr=1e-3, lr_final=1e-4, seed=0):
-        sp = PlumeTrainSpec(epochs=epochs, batch=batch, val_pairs=val_pairs, reserved=0, lr=lr,
+    def train(self, dataset, epochs=1, batch=4, val_pairs=0, lr=1e-3, lr_final=1e-4, seed=0, loss=LOSS_ENERGY):
+        sp = PlumeTrainSpec(epochs=epochs, batch=batch, val_pairs=val_pairs, loss=loss, lr=lr,
                             lr_final=lr_final, seed=seed)
         tl = np.zeros(epochs, dtype=np.float32)
         vl = np.zeros(epochs, dtype=np.float32)

@@ -58,10 +58,20 @@ int plume_net_load(plume_net* net, const char* path);
 int plume_net_forward(plume_net* net, const int32_t res[3], int32_t batch, const float* input,
                       float* output);
 
-/* Loss (mean squared error over interior cells of every sample) and its
-   gradient with respect to every parameter (plume_net_num_params floats). */
-int plume_net_loss_grad(plume_net* net, const int32_t res[3], int32_t batch, const float* input,
-                        const float* target, double* loss, float* grad);
+/* Training losses, averaged over the interior cells of every sample, of the
+   error e = y - target: */
+enum {
+  PLUME_LOSS_MSE = 0,    /* e^T e                                              */
+  PLUME_LOSS_ENERGY = 1  /* e^T A e + 1e-4 e^T e, A the closed-box 7-point
+                            operator: the error norm CG's convergence bound
+                            starts from; the small e^T e term pins the constant
+                            mode A does not see */
+};
+
+/* A loss and its gradient with respect to every parameter
+   (plume_net_num_params floats). */
+int plume_net_loss_grad(plume_net* net, const int32_t res[3], int32_t batch, int32_t loss_kind,
+                        const float* input, const float* target, double* loss, float* grad);
 
 typedef struct plume_dataset_spec {
   int32_t res[3];
@@ -89,7 +99,7 @@ typedef struct plume_train_spec {
   int32_t epochs;
   int32_t batch;
   int32_t val_pairs; /* the last val_pairs pairs are held out */
-  int32_t reserved;
+  int32_t loss;      /* PLUME_LOSS_MSE or PLUME_LOSS_ENERGY */
   float lr;          /* Adam step size, cosine-decayed to lr_final */
   float lr_final;
   uint64_t seed;     /* shuffle order */

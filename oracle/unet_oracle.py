@@ -14,7 +14,8 @@ rounding points the C header documents:
 * 2x2x2 mean pooling (rounded to BF16), nearest upsampling, skip
   concatenation [upsampled, skip];
 * 1x1x1 output convolution 16 -> 1 with FP32 weights;
-* loss = mean over interior cells of (y - t)^2;
+* loss = mean over interior cells of (y - t)^2, or of the energy norm
+  e (A e) + 1e-4 e^2 of the error e = y - t (A the closed-box 7-point operator);
 * gradient tensors are rounded to BF16 where the GPU stores them.
 
 With bf16=False every rounding is skipped and the arithmetic is float64, which
@@ -128,6 +129,18 @@ def interior_mask(res):
     return m
 
 
+def closed_box_operator(e, m):
+    """A e on interior cells: (number of interior neighbours) * e minus the
+    sum of the interior neighbours; e and the result are 0 outside the
+    interior (m is the interior mask, shape (Z, Y, X))."""
+    q = np.zeros_like(e)
+    for ax in (1, 2, 3):
+        for s in (1, -1):
+            nb = np.roll(m, s, ax - 1)
+            q += nb * (e - np.roll(e, s, ax))
+    return q * m
+
+
 class UNetOracle:
     def __init__(self, params, bf16=True):
         self.p = unpack(params)
@@ -165,15 +178,25 @@ class UNetOracle:
         a["y"] = y
         return y.reshape(batch, -1), a
 
-    def loss_grad(self, inp, tgt, res, batch):
+    def loss_grad(self, inp, tgt, res, batch, loss="mse"):
+        """loss "mse": mean of e^2; "energy": mean of e (A e) + 1e-4 e^2 with A
+        the closed-box 7-point operator on interior cells (e = y - t)."""
         X, Y, Z = res
         y, a = self.forward(inp, res, batch)
         t = np.asarray(tgt, dtype=np.float64).reshape(batch, Z, Y, X)
         m = interior_mask(res)
         count = batch * (X - 2) * (Y - 2) * (Z - 2)
         e = (a["y"] - t) * m
-        loss = float((e * e).sum() / count)
-        gy = 2.0 * e / count
+        if loss == "energy":
+            if self.bf16:  # the GPU forms e and A e in FP32
+                e = e.astype(np.float32).astype(np.float64)
+            ae = closed_box_operator(e, m)
+            w = 1e-4
+            loss = float((e * ae + w * e * e).sum() / count)
+            gy = 2.0 * (ae + w * e) / count
+        else:
+            loss = float((e * e).sum() / count)
+            gy = 2.0 * e / count
         r, w, g = self.r, self.w, {}
         relu_mask = lambda act: (act > 0).astype(np.float64)
 

@@ -46,7 +46,8 @@ def test_param_count_and_layout():
     np.testing.assert_array_equal(uo.pack(uo.unpack(p)), p.astype(np.float64))
 
 
-def test_oracle_gradient_matches_finite_differences():
+@pytest.mark.parametrize("loss", ["mse", "energy"])
+def test_oracle_gradient_matches_finite_differences(loss):
     """The restated backward pass (float64, no rounding) against central
     differences of the restated forward pass."""
     res, batch = (8, 8, 8), 2
@@ -55,7 +56,8 @@ def test_oracle_gradient_matches_finite_differences():
     inp = smooth_field(rng, res, batch)
     tgt = smooth_field(rng, res, batch)
     o = uo.UNetOracle(params, bf16=False)
-    loss, grad = o.loss_grad(inp, tgt, res, batch)
+    L = lambda q: uo.UNetOracle(q, bf16=False).loss_grad(inp, tgt, res, batch, loss=loss)[0]
+    _, grad = o.loss_grad(inp, tgt, res, batch, loss=loss)
     # parameters spread over every layer, each with a gradient well above round-off
     checked = 0
     offsets = np.cumsum([0] + [27 * ci * co + co for _, ci, co, _ in uo.LAYERS])
@@ -71,9 +73,7 @@ def test_oracle_gradient_matches_finite_differences():
             pp, pm = params.copy(), params.copy()
             pp[k] += h
             pm[k] -= h
-            lp, _ = uo.UNetOracle(pp, bf16=False).loss_grad(inp, tgt, res, batch)
-            lm, _ = uo.UNetOracle(pm, bf16=False).loss_grad(inp, tgt, res, batch)
-            fd = (lp - lm) / (2 * h)
+            fd = (L(pp) - L(pm)) / (2 * h)
             assert abs(fd - grad[k]) <= 1e-4 * abs(grad[k]) + 1e-9, (name, int(k - lo), fd, grad[k])
             checked += 1
     for k in (offsets[-1], offsets[-1] + 16):  # output layer weight and bias
@@ -81,8 +81,7 @@ def test_oracle_gradient_matches_finite_differences():
         pp, pm = params.copy(), params.copy()
         pp[k] += h
         pm[k] -= h
-        fd = (uo.UNetOracle(pp, bf16=False).loss_grad(inp, tgt, res, batch)[0] -
-              uo.UNetOracle(pm, bf16=False).loss_grad(inp, tgt, res, batch)[0]) / (2 * h)
+        fd = (L(pp) - L(pm)) / (2 * h)
         assert abs(fd - grad[k]) <= 1e-4 * abs(grad[k]) + 1e-9
         checked += 1
     assert checked == 32
@@ -113,7 +112,8 @@ def test_forward_matches_oracle(net):
 
 
 @pytest.mark.gpu
-def test_gradients_match_oracle(net):
+@pytest.mark.parametrize("loss", ["mse", "energy"])
+def test_gradients_match_oracle(net, loss):
     """Loss and every layer's weight and bias gradient of the CUDA backward
     pass against the restatement with the same BF16 rounding points: relative
     L2 per tensor <= 1e-2, and closer to it than BF16 rounding itself moves the
@@ -124,16 +124,19 @@ def test_gradients_match_oracle(net):
     rng = np.random.default_rng(9)
     inp = smooth_field(rng, RES, batch).astype(np.float32)
     tgt = smooth_field(rng, RES, batch).astype(np.float32)
-    loss, grad = net.loss_grad(inp, tgt, RES)
-    lref, gref = uo.UNetOracle(params).loss_grad(inp, tgt, RES, batch)
-    _, gexact = uo.UNetOracle(params, bf16=False).loss_grad(inp, tgt, RES, batch)
-    assert abs(loss - lref) <= 1e-4 * lref
+    from cfs_plume_gb300.net import LOSS_ENERGY, LOSS_MSE
+    value, grad = net.loss_grad(inp, tgt, RES, loss=LOSS_ENERGY if loss == "energy" else LOSS_MSE)
+    lref, gref = uo.UNetOracle(params).loss_grad(inp, tgt, RES, batch, loss=loss)
+    _, gexact = uo.UNetOracle(params, bf16=False).loss_grad(inp, tgt, RES, batch, loss=loss)
+    assert abs(value - lref) <= 1e-4 * lref
     k = 0
     for name, ci, co, _ in uo.LAYERS:
         nw = 27 * ci * co
         for part, s in (("w", slice(k, k + nw)), ("b", slice(k + nw, k + nw + co))):
             err = rel(grad[s], gref[s])
-            assert err < 1e-2, (name, part, err)
+            # the energy loss weights high frequencies, where the gradient is a
+            # difference of large terms and rounding flips count for more
+            assert err < (1e-2 if loss == "mse" else 5e-2), (name, part, err)
             assert err < rel(gref[s], gexact[s]), (name, part)
         k += nw + co
     assert rel(grad[k:], gref[k:]) < 1e-3, "out"
@@ -237,3 +240,25 @@ def test_learned_start_falls_back_to_plain(net):
     vp, vl, sp, sl = _step_pair((32, 48, 32), net, 2, max_iters=3)
     assert all(s.fallback for s in sl) and not any(s.fallback for s in sp)
     np.testing.assert_array_equal(vl, vp)
+
+
+WEIGHTS = __import__("os").path.join(__import__("os").path.dirname(__import__("os").path.dirname(
+    __import__("os").path.abspath(__file__))), "cfs_plume_gb300", "weights", "unet_warmstart.bin")
+
+
+@pytest.mark.gpu
+def test_trained_network_saves_iterations():
+    """The committed network (trained on 20k pairs of 64x96x64 plumes with
+    the energy loss) against the zero start on an unseen 64x96x64 plume: fewer
+    PCG iterations per step, every solve meeting the same rel-L2 1e-6 test
+    without fallback, velocity within 1e-4 relative L2."""
+    from cfs_plume_gb300.net import PlumeNet
+    n = PlumeNet(path=WEIGHTS)
+    vp, vl, sp, sl = _step_pair((64, 96, 64), n, 12)
+    n.close()
+    ip = np.mean([s.iterations for s in sp[2:]])
+    il = np.mean([s.iterations for s in sl[2:]])
+    assert not any(s.fallback for s in sl)
+    assert all(s.converged and s.rel_residual <= 1e-6 for s in sl)
+    assert il < 0.93 * ip, (il, ip)
+    assert rel(vl, vp) < 1e-4
