@@ -8,6 +8,12 @@ PCG to a relative residual of 1e-6.  A "step" is one FLUID_3D_MIC::step
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+Two arms run on the same plume: plain MIC(0)-PCG from p = 0 (the reference's
+solve) and the learned warm start (the committed U-Net's guess, Galerkin
+scaled, then the same MIC-PCG to the same stop test).  The metric compares
+them; `value`, `e2e` and the roofline describe the learned arm, `arms` gives
+both.
+
 Prints one JSON line.  `value` is steps/s from CUDA events on the library's
 stream around the K timed steps (state resident in HBM); `e2e` is steps/s
 through the public API with the source values copied from pinned host memory
@@ -190,6 +196,42 @@ def run_reference(args, rank, world):
     return 0
 
 
+def measure_arm(g, a, dist, nbox, box_values_seed):
+    """Warm-up, then K device-timed steps (CUDA events on the library stream,
+    MIC sweep launches bracketed by events), then the end-to-end loop through
+    the public API with host buffers.  Returns a dict of raw measurements."""
+    import numpy as np
+    from cfs_plume_gb300 import _abi
+    g.run_timed(0, a.warmup)
+    dist.barrier()
+    g.profile_sweeps(True)
+    g.lib.plume_sync(g.h)
+    ms, stats = g.run_timed(a.warmup, a.steps)
+    sweep_ms, sweep_launches = g.sweep_times()
+    g.profile_sweeps(False)
+    dist.barrier()
+    ms_max = dist.max(ms)
+    n_e2e = a.e2e_steps if a.e2e_steps is not None else max(3, min(a.steps, 10))
+    rng = np.random.default_rng(box_values_seed)
+    src = [1.0 + 0.05 * (2.0 * rng.random(nbox) - 1.0) for _ in range(n_e2e)]
+    vel = np.empty(3 * g.N)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for k in range(n_e2e):
+        g.add_source_values(src[k])
+        g.step(stats=False)
+        g.lib.plume_download(g.h, _abi.FIELD_ID["velocity"], vel.ctypes.data, vel.size)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    dist.barrier()
+    iters = [s.iterations for s in stats]
+    return {"ms": ms_max, "value": dist.sum(a.steps) / (ms_max / 1000.0), "iters": iters,
+            "launches": sum(s.launches for s in stats), "ms_solve": sum(s.ms_solve for s in stats),
+            "fallbacks": sum(s.fallback for s in stats),
+            "max_rel_residual": max(s.rel_residual for s in stats),
+            "sweep_ms": sweep_ms, "sweep_launches": sweep_launches,
+            "e2e": dist.sum(n_e2e) / e2e_s, "n_e2e": n_e2e}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -200,6 +242,9 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--cpu-steps", type=int, default=3, help="oracle steps for cpu_baseline (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--arms", default="both", choices=["both", "plain"],
+                    help="both: plain MIC-PCG and the learned warm start (the headline value)")
+    ap.add_argument("--weights", default=None, help="warm-start network (default: the committed one)")
     a = ap.parse_args()
     rank, world, local = dist_env()
     if a.impl == "reference":
@@ -216,46 +261,36 @@ def main():
     P = S
     dist = Dist(world)
     p = _abi.plume_config(res, precision=prec, seed=rank, device=local)
-    g = Plume(p)
     nint = (res[0] - 2) * (res[1] - 2) * (res[2] - 2)
-
-    # warm-up (not timed)
-    g.run_timed(0, a.warmup)
-    clocks = ClockSampler(local)
-    dist.barrier()
-    g.profile_sweeps(True)  # CUDA events around every MIC sweep launch, on the solver's stream
-    g.lib.plume_sync(g.h)
-    clocks.start()
-    ms, stats = g.run_timed(a.warmup, a.steps)
-    clk = clocks.stop()
-    sweep_ms, sweep_launches = g.sweep_times()
-    g.profile_sweeps(False)
-    dist.barrier()
-    ms_max = dist.max(ms)
-    iters = [s.iterations for s in stats]
-    launches = sum(s.launches for s in stats)
-    ms_solve = sum(s.ms_solve for s in stats)
-    steps_total = dist.sum(a.steps)
-    value = steps_total / (ms_max / 1000.0)
-
-    # end to end through the public API with host buffers
-    n_e2e = a.e2e_steps if a.e2e_steps is not None else max(3, min(a.steps, 10))
     lo, hi = p.box_lo, p.box_hi
     nbox = (hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2])
-    rng = np.random.default_rng(rank)
-    src = [1.0 + 0.05 * (2.0 * rng.random(nbox) - 1.0) for _ in range(n_e2e)]
-    vel = np.empty(3 * g.N)
-    dist.barrier()
-    t0 = time.perf_counter()
-    base = a.warmup + a.steps
-    for k in range(n_e2e):
-        g.add_source_values(src[k])
-        g.step(stats=False)
-        g.lib.plume_download(g.h, _abi.FIELD_ID["velocity"], vel.ctypes.data, vel.size)
-    e2e_s = time.perf_counter() - t0
-    dist.barrier()
-    e2e_s = dist.max(e2e_s)
-    e2e = dist.sum(n_e2e) / e2e_s
+    weights = a.weights if a.weights else os.path.join(ROOT, "cfs_plume_gb300", "weights", "unet_warmstart.bin")
+    learned = os.path.exists(weights) and a.arms != "plain"
+
+    # both arms on the same plume (same seed and source values); clocks are
+    # sampled from the first timed step to the last
+    clocks = ClockSampler(local)
+    clocks.start()
+    g = Plume(p)
+    plain = measure_arm(g, a, dist, nbox, rank)
+    g.close()
+    lrn = None
+    if learned:
+        from cfs_plume_gb300.net import PlumeNet
+        net = PlumeNet(device=local, path=weights)
+        gl = Plume(_abi.plume_config(res, precision=prec, seed=rank, device=local,
+                                     warm_start=_abi.WARM_LEARNED))
+        net.attach(gl)
+        lrn = measure_arm(gl, a, dist, nbox, rank)
+        gl.close()
+        net.close()
+    clk = clocks.stop()
+    head = lrn if lrn is not None else plain
+    ms_max, value, iters = head["ms"], head["value"], head["iters"]
+    launches, ms_solve = head["launches"], head["ms_solve"]
+    sweep_ms, sweep_launches = head["sweep_ms"], head["sweep_launches"]
+    e2e = head["e2e"]
+    N = res[0] * res[1] * res[2]
 
     peak, peak_kind = measured_peaks()
     mean_iters = statistics.mean(iters)
@@ -276,12 +311,18 @@ def main():
         "data": "synthetic",
         "config": {"workload": "plume %dx%dx%d, closed box, box source +-0.05 seeded noise, "
                                "buoyancy 1, vorticity 2, MIC(0)-PCG rel-residual 1e-6" % res,
-                   "res": list(res), "solver": "plain MIC(0)-PCG (learned start not in this build)",
+                   "res": list(res),
+                   "solver": ("MIC(0)-PCG from the learned U-Net warm start (plain fallback)" if lrn
+                              else "plain MIC(0)-PCG from p = 0"),
                    "precision": "FP32 fields, FP64 CG scalars/MIC diagonal" if S == 4 else "FP64",
                    "l2": "step working set %.0f MB > 129 MB L2 (no flush needed)" %
-                         (37 * S * g.N / 1e6),
+                         (37 * S * N / 1e6),
                    "parallelism": "replicas" if world > 1 else "single"},
         "pcg_iters_per_step": mean_iters,
+        "arms": {name: {"value": r["value"], "unit": "steps/s", "ms_per_step": r["ms"] / a.steps,
+                        "pcg_iters_per_step": statistics.mean(r["iters"]), "fallbacks": r["fallbacks"],
+                        "max_rel_residual": r["max_rel_residual"], "e2e": r["e2e"]}
+                 for name, r in (("plain", plain), ("learned", lrn)) if r is not None},
         "achieved_gbs_step": step_bytes / (ms_max / a.steps / 1000.0) / 1e9,
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "k_mic_wave_cl (MIC(0) forward/backward sweep)",
@@ -296,7 +337,7 @@ def main():
                            "unit": "GB/s", "frac": (achieved_solve / peak) if achieved_solve else None,
                            "bytes_model": "N_int*(5S+2P+2 + iters*(16S+2P+3)) per solve"},
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": nbox * 8,
-                "d2h_bytes_per_step": 3 * g.N * 8},
+                "d2h_bytes_per_step": 3 * N * 8},
         "clocks": clk,
     }
     if rank == 0 and a.cpu_steps > 0:

@@ -364,6 +364,7 @@ class EngineT : public Engine {
       if (!net_) return fail(PLUME_ERR_STATE, "learned warm start without an attached network");
       const int prc = net_->predict(net_ws_, div_, pres_, std::is_same<T, double>::value ? 1 : 0, s_, err_);
       if (prc != PLUME_OK) return prc;
+      launches_ += net_->launches_per_predict();
       // Galerkin scaling: the guess is never worse than p = 0 in the A-norm
       k_guess_scale_dots<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, pres_, div_, st_, part_);
       PL_CHECK_LAUNCH();

@@ -536,6 +536,10 @@ class Net : public NetRuntime {
     return PLUME_OK;
   }
 
+  // scale (2) + input (1) + forward (10 convolutions, 2 pools, 2 upsamplings,
+  // output layer) + guess (1)
+  int launches_per_predict() const override { return 19; }
+
   int device_ = 0;
   cudaStream_t s_ = nullptr;
   char* params_ = nullptr;

@@ -13,6 +13,8 @@ class NetRuntime {
   // Interior cells of x (device grid, FP32 or FP64) = the network's initial
   // guess for A x = b; everything is queued on `stream`.  Returns plume_status.
   virtual int predict(void* ws, const void* b, void* x, int is_double, void* stream, std::string& err) = 0;
+  // Kernel launches one predict() makes.
+  virtual int launches_per_predict() const = 0;
 };
 
 }  // namespace plume
