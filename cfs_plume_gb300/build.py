@@ -82,6 +82,7 @@ def build(verbose=False, ptxas_info=False):
         ("unet.cu", [nvcc] + common_nv),
         ("plume_api.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-I" + os.path.join(cuda, "include")]),
         ("snapshot.cpp", ["g++", "-O2", "-std=c++17", "-fPIC"] + zc),
+        ("batch.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread"]),
     ]
     jobs = []
     with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:

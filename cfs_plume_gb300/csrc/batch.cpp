@@ -1,0 +1,144 @@
+// batch.cpp -- many independent plumes on one GPU (include/plume_batch.h).
+//
+// Host C++ over the C ABI: each instance is a plume_handle with its own CUDA
+// stream; a pool of host threads steps them concurrently.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/plume.h"
+#include "../../include/plume_batch.h"
+#include "../../include/plume_solver.h"
+#include "engine.h"
+
+struct plume_batch {
+  std::vector<plume_handle*> h;
+};
+
+namespace {
+
+uint64_t mix(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+double uniform(uint64_t seed, uint64_t k) { return (mix(mix(seed) + k) >> 11) * (1.0 / 9007199254740992.0); }
+
+int fail(int code, const std::string& msg) {
+  plume::global_error() = msg;
+  return code;
+}
+
+}  // namespace
+
+extern "C" {
+
+int plume_batch_params(uint64_t seed, int32_t index, plume_params* p) {
+  if (!p || index < 0) return fail(PLUME_ERR_INVALID, "bad argument");
+  static const int kGrids[4][3] = {{32, 32, 32}, {48, 64, 48}, {64, 96, 64}, {96, 128, 96}};
+  const uint64_t s = seed + (uint64_t)index;
+  plume_default_params(p);
+  const int* g = kGrids[(int)(uniform(s, 0) * 4.0) & 3];
+  const int X = g[0], Y = g[1], Z = g[2];
+  p->res[0] = X;
+  p->res[1] = Y;
+  p->res[2] = Z;
+  for (int k = 0; k < 6; k++) p->bc[k] = 1;
+  p->precision = PLUME_PREC_FP32;
+  p->criterion = PLUME_CRIT_REL2;
+  p->tol = 1e-6;
+  p->max_iters = 1000;
+  p->source = PLUME_SRC_BOX;
+  p->source_noise = 0.05;
+  p->seed = s;
+  p->buoyancy = 0.5 + 1.5 * uniform(s, 1);
+  p->vorticity_eps = 4.0 * uniform(s, 2);
+  const int wx = (28 * X) / 48 - (20 * X) / 48, wz = (28 * Z) / 48 - (20 * Z) / 48;
+  const double cx = X / 3.0 + (X / 3.0) * uniform(s, 3), cz = Z / 3.0 + (Z / 3.0) * uniform(s, 4);
+  p->box_lo[0] = std::max(1, std::min(X - 1 - wx, (int)std::lround(cx - wx / 2.0)));
+  p->box_lo[2] = std::max(1, std::min(Z - 1 - wz, (int)std::lround(cz - wz / 2.0)));
+  p->box_hi[0] = p->box_lo[0] + wx;
+  p->box_hi[2] = p->box_lo[2] + wz;
+  p->box_lo[1] = (2 * Y) / 64;
+  p->box_hi[1] = (6 * Y) / 64;
+  return PLUME_OK;
+}
+
+int plume_batch_create(const plume_params* params, int32_t n, plume_batch** out) {
+  if (!params || !out || n < 1) return fail(PLUME_ERR_INVALID, "bad argument");
+  plume_batch* b = new (std::nothrow) plume_batch();
+  if (!b) return fail(PLUME_ERR_OOM, "out of host memory");
+  for (int i = 0; i < n; i++) {
+    plume_handle* h = nullptr;
+    const int rc = plume_create(&params[i], &h);
+    if (rc != PLUME_OK) {
+      const std::string why = "instance " + std::to_string(i) + ": " + plume_last_error(nullptr);
+      plume_batch_destroy(b);
+      return fail(rc, why);
+    }
+    b->h.push_back(h);
+  }
+  *out = b;
+  return PLUME_OK;
+}
+
+void plume_batch_destroy(plume_batch* b) {
+  if (!b) return;
+  for (plume_handle* h : b->h) plume_destroy(h);
+  delete b;
+}
+
+int plume_batch_size(plume_batch* b, int32_t* n) {
+  if (!b || !n) return fail(PLUME_ERR_INVALID, "bad argument");
+  *n = (int32_t)b->h.size();
+  return PLUME_OK;
+}
+
+int plume_batch_handle(plume_batch* b, int32_t i, plume_handle** h) {
+  if (!b || !h || i < 0 || i >= (int32_t)b->h.size()) return fail(PLUME_ERR_INVALID, "bad instance");
+  *h = b->h[i];
+  return PLUME_OK;
+}
+
+int plume_batch_run(plume_batch* b, int32_t first_step, int32_t steps, int32_t threads, double* seconds,
+                    plume_step_stats* stats) {
+  if (!b || steps < 0 || threads < 0) return fail(PLUME_ERR_INVALID, "bad argument");
+  const int n = (int)b->h.size();
+  const int T = threads == 0 ? n : std::min(threads, n);
+  std::vector<int> rcs(n, PLUME_OK);
+  std::vector<std::string> errs(n);
+  const auto t0 = std::chrono::steady_clock::now();
+  // thread t owns instances t, t+T, ...; it advances them round-robin one step
+  // at a time, so every instance makes progress while another one's solve waits
+  auto worker = [&](int t) {
+    for (int s = 0; s < steps; s++)
+      for (int i = t; i < n; i += T) {
+        if (rcs[i] != PLUME_OK) continue;
+        int rc = plume_add_source(b->h[i], first_step + s);
+        if (rc == PLUME_OK) rc = plume_step(b->h[i], stats ? &stats[(size_t)i * steps + s] : nullptr);
+        if (rc != PLUME_OK) {
+          rcs[i] = rc;
+          errs[i] = plume_last_error(b->h[i]);
+        }
+      }
+    for (int i = t; i < n; i += T)
+      if (rcs[i] == PLUME_OK && plume_sync(b->h[i]) != PLUME_OK) {
+        rcs[i] = PLUME_ERR_CUDA;
+        errs[i] = plume_last_error(b->h[i]);
+      }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 0; t < T; t++) pool.emplace_back(worker, t);
+  for (auto& th : pool) th.join();
+  if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  for (int i = 0; i < n; i++)
+    if (rcs[i] != PLUME_OK) return fail(rcs[i], "instance " + std::to_string(i) + ": " + errs[i]);
+  return PLUME_OK;
+}
+
+}  // extern "C"
