@@ -371,7 +371,11 @@ class EngineT : public Engine {
       k_guess_scale_apply<T><<<gI, 256, 0, s_>>>(g_, pres_, st_);
       PL_CHECK_LAUNCH();
     }
-    int rc = solve_device(div_, pres_);
+    // a learned-start solve gets at most twice the previous step's
+    // iterations: a guess that does not pay off falls back early
+    int cap = p_.max_iters;
+    if (learned && last_iters_ > 0) cap = std::min(p_.max_iters, std::max(20, 2 * last_iters_));
+    int rc = solve_device(div_, pres_, cap);
     if (rc != PLUME_OK) return rc;
     if (learned && !st_host_->converged) {
       // the guess did not lead to convergence: plain MIC-PCG from p = 0
@@ -380,6 +384,7 @@ class EngineT : public Engine {
       rc = solve_device(div_, pres_);
       if (rc != PLUME_OK) return rc;
     }
+    last_iters_ = st_host_->iter;
     PL_TRY(cudaEventRecord(ev_[2], s_));
     k_gradient<T><<<gI, 256, 0, s_>>>(g_, c_, vel_, pres_);
     PL_CHECK_LAUNCH();
@@ -760,14 +765,15 @@ class EngineT : public Engine {
 
   // MIC-PCG (FLUID_3D_MIC.cpp:918-1015); x (natural layout) holds the initial
   // guess on entry and the solution on return, b is the natural right side.
-  int solve_device(const T* b, T* x) {
+  int solve_device(const T* b, T* x, int max_iters = -1) {
+    if (max_iters < 0) max_iters = p_.max_iters;
     const int gK = grid_for(k_.total);
     k_to_skew<T, T><<<gK, 256, 0, s_>>>(g_, k_, b, sb_);
     PL_CHECK_LAUNCH();
     k_to_skew<T, T><<<gK, 256, 0, s_>>>(g_, k_, x, sx_);
     PL_CHECK_LAUNCH();
     k_cgs_init<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, k_, sb_, sx_, sr_, st_, part_, p_.tol,
-                                                      p_.max_iters, p_.criterion);
+                                                      max_iters, p_.criterion);
     PL_CHECK_LAUNCH();
     prof_it_ = -1;
     int rc = mic_sweeps(sr_, sqf_, sz_);
@@ -780,7 +786,7 @@ class EngineT : public Engine {
     int chunk = 4;
     T* dcur = sd_;  // direction of the previous iteration (beta = 0 on the first)
     T* dnext = sd2_;
-    for (int it = 0; it < p_.max_iters + chunk;) {
+    for (int it = 0; it < max_iters + chunk;) {
       for (int kk = 0; kk < chunk; kk++) {
         rc = launch_spmv_dir(sz_, dcur, dnext, sq_);
         if (rc != PLUME_OK) return rc;
@@ -968,6 +974,7 @@ class EngineT : public Engine {
   NetRuntime* net_ = nullptr;
   void* net_ws_ = nullptr;
   int last_fallback_ = 0;
+  int last_iters_ = 0;  // iterations of the last accepted step solve
   static constexpr int kProfEvents = 64;
   bool prof_on_ = false;
   cudaEvent_t prof_ev_[2][kProfEvents] = {};

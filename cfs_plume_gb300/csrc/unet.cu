@@ -519,7 +519,7 @@ class Net : public NetRuntime {
     else
       k_sumsq_interior<float><<<nb, kThreads, 0, s>>>(d, (const float*)b, ws.dpart);
     NT_LAUNCH();
-    k_rms_scale<<<1, 32, 0, s>>>(ws.dpart, nb, count, ws.scale);
+    k_rms_scale<<<1, 256, 0, s>>>(ws.dpart, nb, count, ws.scale);
     NT_LAUNCH();
     if (is_double)
       k_input_from_rhs<double><<<nb, kThreads, 0, s>>>(d, (const double*)b, ws.scale, view(ws.xin, 16, d));
@@ -833,7 +833,7 @@ int plume_dataset_generate(const plume_dataset_spec* spec, plume_dataset** out) 
         if (st < sp.skip) continue;
         const size_t slot = (size_t)i * per + (st - sp.skip);
         k_sumsq_interior<float><<<nb, kThreads, 0, s>>>(ds.d, b, dpart);
-        k_rms_scale<<<1, 32, 0, s>>>(dpart, nb, count, scale);
+        k_rms_scale<<<1, 256, 0, s>>>(dpart, nb, count, scale);
         k_store_pair<float><<<nb, kThreads, 0, s>>>(ds.d, b, x, scale, ds.in + slot * cells,
                                                     ds.tgt + slot * cells);
         if (cudaGetLastError() != cudaSuccess) {

@@ -715,12 +715,18 @@ __global__ void __launch_bounds__(256) k_sumsq_interior(Dims d, const T* b, doub
 }
 
 // scale[0] = rms over `count` interior cells (0 when the field is all zero)
-__global__ void k_rms_scale(const double* part, int nparts, double count, float* scale) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0.0;
-    for (int k = 0; k < nparts; k++) s += part[k];
-    scale[0] = (float)sqrt(s / count);
+// (one block of 256 threads: strided partial sums, then a fixed-order tree)
+__global__ void __launch_bounds__(256) k_rms_scale(const double* part, int nparts, double count, float* scale) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int k = threadIdx.x; k < nparts; k += 256) s += part[k];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) scale[0] = (float)sqrt(sh[0] / count);
 }
 
 // network input from a right-hand side: interior b / scale, 0 elsewhere
