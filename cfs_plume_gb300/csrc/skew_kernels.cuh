@@ -4,6 +4,7 @@
 // threads run over the stored elements row by row, so loads and stores are
 // contiguous; padding elements are kept at zero.
 #pragma once
+#include <type_traits>
 #include "solver_kernels.cuh"
 #include "wave.cuh"
 
@@ -44,6 +45,23 @@ __device__ inline T mult_a_skew(const Grid& g, const Skew& k, const T* v, int e,
          vzm * coef<T>(wall_zm(g, z)) + vzp * coef<T>(wall_zp(g, z));
 }
 
+// mult_a_skew with every product and sum in FP64
+template <typename T>
+__device__ inline double mult_a_skew_d(const Grid& g, const Skew& k, const T* v, int e, int ix, int iy,
+                                       int iz) {
+  const int x = ix + 1, y = iy + 1, z = iz + 1;
+  const double vxm = ix > 0 ? (double)v[skew_at(k, ix - 1, iy, iz)] : 0.0;
+  const double vxp = ix + 1 < k.nx ? (double)v[skew_at(k, ix + 1, iy, iz)] : 0.0;
+  const double vym = iy > 0 ? (double)v[e - k.W] : 0.0;
+  const double vyp = iy + 1 < k.ny ? (double)v[e + k.W] : 0.0;
+  const double vzm = iz > 0 ? (double)v[e - (int)k.plane] : 0.0;
+  const double vzp = iz + 1 < k.nz ? (double)v[e + (int)k.plane] : 0.0;
+  return adiag<double>(g, x, y, z) * (double)v[e] + vxm * coef<double>(wall_xm(g, x)) +
+         vxp * coef<double>(wall_xp(g, x)) + vym * coef<double>(wall_ym(g, y)) +
+         vyp * coef<double>(wall_yp(g, y)) + vzm * coef<double>(wall_zm(g, z)) +
+         vzp * coef<double>(wall_zp(g, z));
+}
+
 // natural full grid -> skewed interior (padding zero)
 template <typename S, typename T>
 __global__ void k_to_skew(Grid g, Skew k, const S* nat, T* sk) {
@@ -75,7 +93,14 @@ __global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState
     T v = T(0);
     if (skew_cell(k, e, ix, iy, iz)) {
       const T bi = b[e];
-      v = bi - mult_a_skew(g, k, x, e, ix, iy, iz);
+      if (std::is_same<T, float>::value) {
+        // FP32 fields: b - A x accumulated in FP64, so a large initial guess
+        // (|x| ~ N^2 |b| for the smoothest modes) does not leave rounding
+        // noise above the stop test in r; x = 0 gives r = b as before
+        v = (T)((double)bi - mult_a_skew_d(g, k, x, e, ix, iy, iz));
+      } else {
+        v = bi - mult_a_skew(g, k, x, e, ix, iy, iz);
+      }
       bb += bi * bi;
     }
     r[e] = v;
