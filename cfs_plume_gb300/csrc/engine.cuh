@@ -63,6 +63,22 @@ inline std::vector<int> column_cells(int X, int Y, int Z) {
   return cells;
 }
 
+// Field download into host memory the GPU can address (pageable memory on a
+// system with coherent host access): dst[o], o = cell * ncomp + component, in
+// FP64 (the reference's AoS layout); consecutive threads write consecutive
+// doubles.
+template <typename T>
+__global__ void k_planes_to_host(const T* a, const T* b, const T* c, int ncomp, long long N, double* dst) {
+  const long long n = N * ncomp;
+  for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < n;
+       o += (long long)gridDim.x * blockDim.x) {
+    const long long cell = ncomp == 1 ? o : o / 3;
+    const int comp = ncomp == 1 ? 0 : (int)(o - cell * 3);
+    const T* src = comp == 0 ? a : (comp == 1 ? b : c);
+    dst[o] = (double)src[cell];
+  }
+}
+
 template <typename T, int C, bool EXACT>
 cudaError_t launch_wave_c(const WaveArgs<T>& a, int grid, size_t smem, cudaStream_t s) {
   void (*kf)(WaveArgs<T>) = a.backward ? k_mic_wave<T, C, EXACT, true> : k_mic_wave<T, C, EXACT, false>;
@@ -192,6 +208,15 @@ class EngineT : public Engine {
     set_consts();
 
     PL_TRY(cudaSetDevice(p.device));
+    {  // the GPU writes downloads straight into the caller's (pageable) buffer
+       // when it can access host memory coherently (Grace + Blackwell over C2C)
+      int pageable = 0;
+      if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, p.device) != cudaSuccess)
+        pageable = 0;
+      const char* off = getenv("PLUME_NO_HOST_DIRECT");
+      host_direct_ = pageable == 1 && !(off && atoi(off) != 0);
+      (void)cudaGetLastError();
+    }
     PL_TRY(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
     for (auto* e : {&ev_[0], &ev_[1], &ev_[2], &ev_[3]}) PL_TRY(cudaEventCreate(e));
 
@@ -375,13 +400,13 @@ class EngineT : public Engine {
     // iterations: a guess that does not pay off falls back early
     int cap = p_.max_iters;
     if (learned && last_iters_ > 0) cap = std::min(p_.max_iters, std::max(20, 2 * last_iters_));
-    int rc = solve_device(div_, pres_, cap);
+    int rc = solve_device(div_, pres_, cap, !learned && keep_p == 0);
     if (rc != PLUME_OK) return rc;
     if (learned && !st_host_->converged) {
       // the guess did not lead to convergence: plain MIC-PCG from p = 0
       last_fallback_ = 1;
       PL_TRY(cudaMemsetAsync(pres_, 0, (size_t)g_.N * sizeof(T), s_));
-      rc = solve_device(div_, pres_);
+      rc = solve_device(div_, pres_, -1, true);
       if (rc != PLUME_OK) return rc;
     }
     last_iters_ = st_host_->iter;
@@ -765,7 +790,8 @@ class EngineT : public Engine {
 
   // MIC-PCG (FLUID_3D_MIC.cpp:918-1015); x (natural layout) holds the initial
   // guess on entry and the solution on return, b is the natural right side.
-  int solve_device(const T* b, T* x, int max_iters = -1) {
+  // x_zero: the caller knows x = 0 on the interior (r = b without A x)
+  int solve_device(const T* b, T* x, int max_iters = -1, bool x_zero = false) {
     if (max_iters < 0) max_iters = p_.max_iters;
     const int gK = grid_for(k_.total);
     k_to_skew<T, T><<<gK, 256, 0, s_>>>(g_, k_, b, sb_);
@@ -773,7 +799,7 @@ class EngineT : public Engine {
     k_to_skew<T, T><<<gK, 256, 0, s_>>>(g_, k_, x, sx_);
     PL_CHECK_LAUNCH();
     k_cgs_init<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, k_, sb_, sx_, sr_, st_, part_, p_.tol,
-                                                      max_iters, p_.criterion);
+                                                      max_iters, p_.criterion, x_zero ? 1 : 0);
     PL_CHECK_LAUNCH();
     prof_it_ = -1;
     int rc = mic_sweeps(sr_, sqf_, sz_);
@@ -881,6 +907,12 @@ class EngineT : public Engine {
   // device plane -> host doubles at dst[k*stride + off]
   int fetch_plane(const T* src, double* dst, int stride, int off) {
     const size_t N = (size_t)g_.N;
+    if (host_direct_ && stride == 1) {
+      k_planes_to_host<T><<<grid_for((long long)N), 256, 0, s_>>>(src, src, src, 1, (long long)N, dst);
+      PL_CHECK_LAUNCH();
+      PL_TRY(cudaStreamSynchronize(s_));
+      return PLUME_OK;
+    }
     PL_TRY(cudaMemcpyAsync(stage_, src, N * sizeof(T), cudaMemcpyDeviceToHost, s_));
     PL_TRY(cudaStreamSynchronize(s_));
     const T* h = (const T*)stage_;
@@ -888,6 +920,13 @@ class EngineT : public Engine {
     return PLUME_OK;
   }
   int fetch_vec(const V3<T>& v, double* dst) {
+    if (host_direct_) {
+      const long long N = g_.N;
+      k_planes_to_host<T><<<grid_for(3 * N), 256, 0, s_>>>(v.x, v.y, v.z, 3, N, dst);
+      PL_CHECK_LAUNCH();
+      PL_TRY(cudaStreamSynchronize(s_));
+      return PLUME_OK;
+    }
     int rc = fetch_plane(v.x, dst, 3, 0);
     if (rc == PLUME_OK) rc = fetch_plane(v.y, dst, 3, 1);
     if (rc == PLUME_OK) rc = fetch_plane(v.z, dst, 3, 2);
@@ -975,6 +1014,7 @@ class EngineT : public Engine {
   void* net_ws_ = nullptr;
   int last_fallback_ = 0;
   int last_iters_ = 0;  // iterations of the last accepted step solve
+  bool host_direct_ = false;  // downloads written by a kernel into host memory
   static constexpr int kProfEvents = 64;
   bool prof_on_ = false;
   cudaEvent_t prof_ev_[2][kProfEvents] = {};

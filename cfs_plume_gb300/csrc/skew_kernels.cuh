@@ -85,7 +85,7 @@ __global__ void k_from_skew(Grid g, Skew k, const T* sk, T* nat) {
 // set-up part 1: r = b - A x, b.b
 template <typename T>
 __global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState* st, double* part,
-                           double tol, int max_iters, int criterion) {
+                           double tol, int max_iters, int criterion, int x_zero) {
   __shared__ double sh[32];
   T bb = T(0);
   PL_GRID_STRIDE(e, (int)k.total) {
@@ -93,7 +93,9 @@ __global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState
     T v = T(0);
     if (skew_cell(k, e, ix, iy, iz)) {
       const T bi = b[e];
-      if (std::is_same<T, float>::value) {
+      if (x_zero) {
+        v = bi;  // the guess is zero: r = b exactly
+      } else if (std::is_same<T, float>::value) {
         // FP32 fields: b - A x accumulated in FP64, so a large initial guess
         // (|x| ~ N^2 |b| for the smoothest modes) does not leave rounding
         // noise above the stop test in r; x = 0 gives r = b as before

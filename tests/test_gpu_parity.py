@@ -283,3 +283,19 @@ def test_sweep_profiling_counts_every_sweep_launch():
     assert n == sum(2 * s.iterations for s in stats)
     assert 0 < ms < sum(s.ms_solve for s in stats)
     h.close()
+
+
+@pytest.mark.gpu
+def test_direct_download_matches_staged(monkeypatch):
+    """Downloads written by a kernel straight into host memory (devices with
+    coherent pageable-memory access) equal the staged copy bit for bit."""
+    res = (24, 32, 24)
+    out = {}
+    for flag in ("0", "1"):
+        monkeypatch.setenv("PLUME_NO_HOST_DIRECT", flag)
+        h = Plume(_abi.plume_config(res))
+        h.run(0, 2)
+        out[flag] = (h.field("velocity"), h.field("pressure"), h.field("cachedQuadratic"))
+        h.close()
+    for a, b in zip(out["0"], out["1"]):
+        np.testing.assert_array_equal(a, b)
