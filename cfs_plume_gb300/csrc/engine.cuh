@@ -225,7 +225,7 @@ class EngineT : public Engine {
     const size_t n = (size_t)g_.N;
     const size_t aT = align(n * sizeof(T));
     const size_t bytes = 37 * aT + align(n * sizeof(double)) + align(n) +
-                         align(sizeof(CgState)) + align(3 * kRedBlocks * sizeof(double));
+                         align(sizeof(CgState)) + align(8 * kRedBlocks * sizeof(double));
     cudaError_t e = cudaMalloc(&pool_, bytes);
     if (e != cudaSuccess) {
       (void)cudaGetLastError();
@@ -246,7 +246,7 @@ class EngineT : public Engine {
     P64_ = (double*)take(n * sizeof(double));
     obst_ = (uint8_t*)take(n);
     st_ = (CgState*)take(sizeof(CgState));
-    part_ = (double*)take(3 * kRedBlocks * sizeof(double));
+    part_ = (double*)take(8 * kRedBlocks * sizeof(double));
 
     // obstacle slabs (FLUID_3D_MIC.cpp:105-159), kept for download and the
     // state file; kernels derive walls from the flags.
@@ -375,25 +375,40 @@ class EngineT : public Engine {
     // project (lines 314-399)
     k_face_bc<T><<<gF, 256, 0, s_>>>(g_, vel_, ox ? 2 : 0, oy ? 2 : 0, oz ? 2 : 0);
     PL_CHECK_LAUNCH();
-    const int keep_p = (p_.warm_start == PLUME_WARM_PREVIOUS) ? 1 : 0;
+    const bool learned = p_.warm_start == PLUME_WARM_LEARNED;
+    // the learned start also uses the previous step's pressure
+    const int keep_p = (p_.warm_start == PLUME_WARM_PREVIOUS || learned) ? 1 : 0;
     k_divergence<T><<<gI, 256, 0, s_>>>(g_, c_, vel_, div_, pres_, keep_p);
     PL_CHECK_LAUNCH();
-    k_copy_border_all<T><<<gF, 256, 0, s_>>>(g_, pres_);
-    PL_CHECK_LAUNCH();
+    if (!learned) {
+      k_copy_border_all<T><<<gF, 256, 0, s_>>>(g_, pres_);
+      PL_CHECK_LAUNCH();
+    }
     PL_TRY(cudaEventRecord(ev_[1], s_));
-    const bool learned = p_.warm_start == PLUME_WARM_LEARNED;
     last_fallback_ = 0;
     if (learned) {
-      // the network's guess on the interior; the border keeps the reference's
-      // copied zeros
+      // x0 = p_prev + g c with c = net(r0), r0 = b - A p_prev: the network
+      // (an approximate inverse of A) applied to the previous pressure's
+      // residual, scaled by the 1-D A-norm Galerkin factor g = c.r0 / c.A c;
+      // border 0, as the reference's p = 0 leaves it
+      // (a network trained on solve pairs maps b itself: x0 = g c, c = net(b))
       if (!net_) return fail(PLUME_ERR_STATE, "learned warm start without an attached network");
-      const int prc = net_->predict(net_ws_, div_, pres_, std::is_same<T, double>::value ? 1 : 0, s_, err_);
+      const bool corr = net_->kind() == 1;
+      k_zero_border<T><<<gN, 256, 0, s_>>>(g_, pres_);
+      PL_CHECK_LAUNCH();
+      if (corr) {
+        k_residual<T><<<gN, 256, 0, s_>>>(g_, div_, pres_, r_);
+        PL_CHECK_LAUNCH();
+      }
+      const T* rhs = corr ? r_ : div_;
+      const int prc = net_->predict(net_ws_, rhs, z_, std::is_same<T, double>::value ? 1 : 0, s_, err_);
       if (prc != PLUME_OK) return prc;
       launches_ += net_->launches_per_predict();
-      // Galerkin scaling: the guess is never worse than p = 0 in the A-norm
-      k_guess_scale_dots<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, pres_, div_, st_, part_);
+      k_zero_border<T><<<gN, 256, 0, s_>>>(g_, z_);
       PL_CHECK_LAUNCH();
-      k_guess_scale_apply<T><<<gI, 256, 0, s_>>>(g_, pres_, st_);
+      k_guess_dots<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, z_, z_, rhs, st_, part_);
+      PL_CHECK_LAUNCH();
+      k_guess_apply<T><<<gI, 256, 0, s_>>>(g_, corr ? pres_ : nullptr, z_, z_, st_, pres_);
       PL_CHECK_LAUNCH();
     }
     // a learned-start solve gets at most twice the previous step's

@@ -22,8 +22,8 @@ struct CgState {
   double rr, bb;         // r.r and b.b
   double dq;             // d.(A d)
   double tol;            // absolute (reference) or relative (rel2) tolerance
-  double guess_scale;    // Galerkin factor of the last learned initial guess
-  double guess_mean;     // interior mean removed from it (closed boxes)
+  double guess_scale, guess_scale2;  // Galerkin factors of the last learned guess
+  double guess_mean, guess_mean2;    // interior means removed (closed boxes)
   int iter, max_iters, criterion, done;
   int converged, broke, wave_err, pad1;
   unsigned int ticket[4];
@@ -89,61 +89,115 @@ __device__ inline double max_partials(const double* part, double* sh) {
   return block_max(s, sh, -1.0e308);
 }
 
-// ------------------------------------------------- scaled initial guess
-// alpha = (x.b) / (x.A x) over the interior minimises the A-norm error of
-// alpha * x among multiples of a guess x, so alpha * x is never further from
-// the solution than x = 0 in that norm (the norm CG's error bound starts
-// from).  With all six walls closed the constant vector is in A's null space:
-// the A-norm does not see it, but a large constant offset in an FP32 guess
-// sets a rounding floor under the residual, so the guess's interior mean is
-// removed (x.A x is unchanged by it and x.b only through sum(b), which the
-// closed-box divergence keeps at round-off).  Writes st->guess_scale = alpha
-// (0 when x.A x is not positive or a sum is not finite) and st->guess_mean;
-// st->ticket[3] is left at 0.  Grid: kRedBlocks blocks; part holds
-// 3 * gridDim.x doubles.
+// ------------------------------------------------- initial guess from two
+// candidate vectors u (the previous step's pressure) and v (the network's
+// guess): x0 = a (u - mu) + b (v - mv) with (a, b) the A-norm Galerkin
+// projection of the solution onto their span, i.e. the 2x2 system
+//   [u.Au u.Av; u.Av v.Av] [a; b] = [u.b; v.b]
+// (a single-vector projection when the pair is degenerate, 0 when neither
+// helps).  The result is never further from the solution than x = 0, u or v
+// alone in the A-norm, the norm CG's error bound starts from.  With all six
+// walls closed the constant vector is A's null space: the A-norm does not see
+// it, but a large constant offset in an FP32 guess sets a rounding floor under
+// the residual, so each candidate's interior mean (mu, mv) is removed first.
+// u and v must be 0 on the border.  Grid: kRedBlocks blocks; part holds
+// 8 * gridDim.x doubles; st->ticket[3] is left at 0.
 template <typename T>
-__global__ void k_guess_scale_dots(Grid g, const T* x, const T* b, CgState* st, double* part) {
+__global__ void k_guess_dots(Grid g, const T* u, const T* v, const T* b, CgState* st, double* part) {
   __shared__ double sh[32];
-  double xb = 0.0, xax = 0.0, xs = 0.0;
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // ub vb uAu vAv uAv su sv sb
   PL_GRID_STRIDE(k, g.nint) {
     int cx, cy, cz;
     const int i = interior_cell(g, k, cx, cy, cz);
-    const double xi = (double)x[i];
-    xb += xi * (double)b[i];
-    xax += xi * (double)mult_a_cell(g, x, i, cx, cy, cz);
-    xs += xi;
+    const double ui = (double)u[i], vi = (double)v[i], bi = (double)b[i];
+    const double au = (double)mult_a_cell(g, u, i, cx, cy, cz);
+    const double av = (double)mult_a_cell(g, v, i, cx, cy, cz);
+    acc[0] += ui * bi;
+    acc[1] += vi * bi;
+    acc[2] += ui * au;
+    acc[3] += vi * av;
+    acc[4] += ui * av;
+    acc[5] += ui;
+    acc[6] += vi;
+    acc[7] += bi;
   }
-  const double s1 = block_sum(xb, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s1;
-  const double s2 = block_sum(xax, sh);
-  if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = s2;
-  const double s3 = block_sum(xs, sh);
-  if (threadIdx.x == 0) part[2 * gridDim.x + blockIdx.x] = s3;
+  for (int q = 0; q < 8; q++) {
+    const double t = block_sum(acc[q], sh);
+    if (threadIdx.x == 0) part[q * gridDim.x + blockIdx.x] = t;
+  }
   if (arrive_last(&st->ticket[3])) {
-    const double t1 = sum_partials(part, sh);
-    const double t2 = sum_partials(part + gridDim.x, sh);
-    const double t3 = sum_partials(part + 2 * gridDim.x, sh);
+    double tot[8];
+    for (int q = 0; q < 8; q++) tot[q] = sum_partials(part + q * gridDim.x, sh);
     if (threadIdx.x == 0) {
       const bool closed = g.wall[0] && g.wall[1] && g.wall[2] && g.wall[3] && g.wall[4] && g.wall[5];
-      const double mean = closed ? t3 / (double)g.nint : 0.0;
-      const double a = t2 > 0.0 ? t1 / t2 : 0.0;
-      const bool ok = isfinite(a) && isfinite(mean);
+      const double n = (double)g.nint;
+      const double mu = closed ? tot[5] / n : 0.0, mv = closed ? tot[6] / n : 0.0;
+      // with the means removed: (u - mu).b = u.b - mu sum(b); A 1 = 0 leaves the A-products
+      const double ub = tot[0] - mu * tot[7], vb = tot[1] - mv * tot[7];
+      const double uu = tot[2], vv = tot[3], uv = tot[4];
+      double a = 0.0, c = 0.0;
+      const double det = uu * vv - uv * uv;
+      if (uu > 0.0 && vv > 0.0 && det > 1e-10 * uu * vv) {
+        a = (ub * vv - vb * uv) / det;
+        c = (uu * vb - uv * ub) / det;
+      } else {  // degenerate pair: the better single candidate (gain g^2 / a)
+        const double gu = uu > 0.0 ? ub * ub / uu : 0.0, gv = vv > 0.0 ? vb * vb / vv : 0.0;
+        if (gu >= gv && gu > 0.0) a = ub / uu;
+        else if (gv > 0.0) c = vb / vv;
+      }
+      const bool ok = isfinite(a) && isfinite(c) && isfinite(mu) && isfinite(mv);
       st->guess_scale = ok ? a : 0.0;
-      st->guess_mean = ok ? mean : 0.0;
+      st->guess_scale2 = ok ? c : 0.0;
+      st->guess_mean = ok ? mu : 0.0;
+      st->guess_mean2 = ok ? mv : 0.0;
       st->ticket[3] = 0;
     }
   }
 }
 
-// x = alpha * (x - mean) on the interior; exactly 0 when alpha is 0 (so a
-// non-finite guess never survives)
+// x = base + a (u - mu) + b (v - mv) on the interior (base may be null; x may
+// alias base or u); terms with a zero coefficient are dropped, so a
+// non-finite candidate never survives
 template <typename T>
-__global__ void k_guess_scale_apply(Grid g, T* x, const CgState* st) {
-  const double a = st->guess_scale, m = st->guess_mean;
+__global__ void k_guess_apply(Grid g, const T* base, const T* u, const T* v, const CgState* st, T* x) {
+  const double a = st->guess_scale, c = st->guess_scale2, mu = st->guess_mean, mv = st->guess_mean2;
   PL_GRID_STRIDE(k, g.nint) {
     int cx, cy, cz;
     const int i = interior_cell(g, k, cx, cy, cz);
-    x[i] = a == 0.0 ? T(0) : (T)(a * ((double)x[i] - m));
+    double r = base ? (double)base[i] : 0.0;
+    if (a != 0.0) r += a * ((double)u[i] - mu);
+    if (c != 0.0) r += c * ((double)v[i] - mv);
+    x[i] = (T)r;
+  }
+}
+
+// r = b - A x on interior cells (FP64 accumulation), 0 on the border
+template <typename T>
+__global__ void k_residual(Grid g, const T* b, const T* x, T* r) {
+  PL_GRID_STRIDE(i, g.N) {
+    const int cx = i % g.X, cy = (i / g.X) % g.Y, cz = i / g.slab;
+    const bool in = cx > 0 && cy > 0 && cz > 0 && cx < g.X - 1 && cy < g.Y - 1 && cz < g.Z - 1;
+    double v = 0.0;
+    if (in) {
+      const double ax = (double)adiag<T>(g, cx, cy, cz) * (double)x[i] +
+                        (double)x[i - 1] * (double)coef<T>(wall_xm(g, cx)) +
+                        (double)x[i + 1] * (double)coef<T>(wall_xp(g, cx)) +
+                        (double)x[i - g.X] * (double)coef<T>(wall_ym(g, cy)) +
+                        (double)x[i + g.X] * (double)coef<T>(wall_yp(g, cy)) +
+                        (double)x[i - g.slab] * (double)coef<T>(wall_zm(g, cz)) +
+                        (double)x[i + g.slab] * (double)coef<T>(wall_zp(g, cz));
+      v = (double)b[i] - ax;
+    }
+    r[i] = (T)v;
+  }
+}
+
+// zero the six border faces of a full-grid field
+template <typename T>
+__global__ void k_zero_border(Grid g, T* f) {
+  PL_GRID_STRIDE(i, g.N) {
+    const int x = i % g.X, y = (i / g.X) % g.Y, z = i / g.slab;
+    if (x == 0 || y == 0 || z == 0 || x == g.X - 1 || y == g.Y - 1 || z == g.Z - 1) f[i] = T(0);
   }
 }
 

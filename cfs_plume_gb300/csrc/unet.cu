@@ -6,11 +6,14 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "../../include/plume.h"
@@ -89,32 +92,51 @@ View none() {
 }
 
 // ---------------------------------------------------------- launch helpers
-template <int CI, int CO>
+template <int CI, int CO, int MF>
 cudaError_t conv_t(const Dims& d, int batch, View in, const uint2* wf, const float* bias, View out, View mask,
                    int relu, cudaStream_t s) {
-  using C = ConvCfg<CI, CO>;
-  cudaError_t e = cudaFuncSetAttribute(k_conv3<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+  using C = ConvCfg<CI, CO, MF>;
+  cudaError_t e =
+      cudaFuncSetAttribute(k_conv3<CI, CO, MF>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
   if (e != cudaSuccess) return e;
-  dim3 grid(conv_bricks<CI, CO>(d), batch);
-  k_conv3<CI, CO><<<grid, 256, C::SMEM, s>>>(d, in, wf, bias, out, mask, relu);
+  dim3 grid(conv_bricks<CI, CO, MF>(d), batch);
+  k_conv3<CI, CO, MF><<<grid, 256, C::SMEM, s>>>(d, in, wf, bias, out, mask, relu);
   return cudaGetLastError();
 }
 
-cudaError_t conv(int ci, int co, const Dims& d, int batch, View in, const uint2* wf, const float* bias, View out,
-                 View mask, int relu, cudaStream_t s) {
-#define PL_CONV(A, B) \
-  if (ci == A && co == B) return conv_t<A, B>(d, batch, in, wf, bias, out, mask, relu, s);
-  PL_CONV(16, 16)
-  PL_CONV(16, 32)
-  PL_CONV(32, 16)
-  PL_CONV(32, 32)
-  PL_CONV(32, 64)
-  PL_CONV(64, 32)
-  PL_CONV(64, 64)
-  PL_CONV(96, 32)
-  PL_CONV(32, 96)
-  PL_CONV(48, 16)
-  PL_CONV(16, 48)
+// Tile shapes (rows per warp) a layer shape may use: accumulators MF*NF*4 <= 64
+// registers and the halo brick within 227 KB of shared memory.
+inline int conv_shapes(int ci, int co, int* mfs) {
+  int n = 0;
+  for (int mf = 1; mf <= 8; mf *= 2) {
+    const int by = mf >= 4 ? 8 : 4, bz = 8 * mf / by;
+    const long long smem = 18LL * (by + 2) * (bz + 2) * (ci + 8) * 2;
+    if (mf * (co / 8) <= 16 && smem <= 227 * 1024) mfs[n++] = mf;
+  }
+  return n;
+}
+
+cudaError_t conv(int ci, int co, int mf, const Dims& d, int batch, View in, const uint2* wf, const float* bias,
+                 View out, View mask, int relu, cudaStream_t s) {
+#define PL_CONV(A, B, M) \
+  if (ci == A && co == B && mf == M) return conv_t<A, B, M>(d, batch, in, wf, bias, out, mask, relu, s);
+#define PL_CONV4(A, B) PL_CONV(A, B, 1) PL_CONV(A, B, 2) PL_CONV(A, B, 4) PL_CONV(A, B, 8)
+#define PL_CONV3(A, B) PL_CONV(A, B, 1) PL_CONV(A, B, 2) PL_CONV(A, B, 4)
+#define PL_CONV2(A, B) PL_CONV(A, B, 1) PL_CONV(A, B, 2)
+  PL_CONV4(16, 16)
+  PL_CONV3(16, 32)
+  PL_CONV4(32, 16)
+  PL_CONV3(32, 32)
+  PL_CONV2(32, 64)
+  PL_CONV3(64, 32)
+  PL_CONV2(64, 64)
+  PL_CONV3(96, 32)
+  PL_CONV(32, 96, 1)
+  PL_CONV4(48, 16)
+  PL_CONV2(16, 48)
+#undef PL_CONV4
+#undef PL_CONV3
+#undef PL_CONV2
 #undef PL_CONV
   return cudaErrorInvalidValue;
 }
@@ -360,8 +382,8 @@ class Net : public NetRuntime {
     const Dims* d = ws.d;
     const View no = none();
     auto cv = [&](int l, View in, View out) {
-      return conv(kLayers[l].cin, kLayers[l].cout, d[kLayers[l].level], nb, in, wf_[l], w_ + boff_[l], out, no,
-                  1, s);
+      return conv_tuned(kLayers[l].cin, kLayers[l].cout, d[kLayers[l].level], nb, in, wf_[l], w_ + boff_[l], out,
+                        no, 1, s);
     };
     NT(cv(E1A, view(ws.xin, 16, d[0]), view(ws.e1a, 16, d[0])));
     NT(cv(E1B, view(ws.e1a, 16, d[0]), view(ws.cat1, 48, d[0], 32)));
@@ -440,7 +462,8 @@ class Net : public NetRuntime {
     };
     // input gradient of layer l: conv with the mirrored weights
     auto dx = [&](int l, View g, View out, View mask) {
-      return conv(kLayers[l].cout, kLayers[l].cin, d[kLayers[l].level], nb, g, wb_[l], nullptr, out, mask, 0, s);
+      return conv_tuned(kLayers[l].cout, kLayers[l].cin, d[kLayers[l].level], nb, g, wb_[l], nullptr, out, mask, 0,
+                        s);
     };
     int rc;
     // level 1, decoder
@@ -482,6 +505,45 @@ class Net : public NetRuntime {
     NT(dx(E1B, view(ws.g_e1b, 16, d[0]), view(ws.g_e1a, 16, d[0]), view(ws.e1a, 16, d[0])));
     if ((rc = wg(E1A, view(ws.xin, 16, d[0]), view(ws.g_e1a, 16, d[0]))) != PLUME_OK) return rc;
     return PLUME_OK;
+  }
+
+  // Convolution with the tile shape the autotuner chose for this layer shape,
+  // grid and batch.  On first use every valid shape runs three times between
+  // CUDA events on `s` (after one untimed run) and the fastest is kept; all
+  // shapes give the same bits, so the timing runs leave a valid output.
+  cudaError_t conv_tuned(int ci, int co, const Dims& d, int nb, View in, const uint2* wf, const float* bias,
+                         View out, View mask, int relu, cudaStream_t s) {
+    const std::tuple<int, int, int, int, int, int> key(ci, co, d.X, d.Y, d.Z, nb);
+    std::lock_guard<std::mutex> lock(tune_mu_);  // handles sharing this network may step concurrently
+    auto it = tuned_.find(key);
+    if (it != tuned_.end()) return conv(ci, co, it->second, d, nb, in, wf, bias, out, mask, relu, s);
+    int mfs[4];
+    const int n = conv_shapes(ci, co, mfs);
+    int best = mfs[0];
+    if (n > 1 && !tune_off_) {
+      cudaEvent_t a = nullptr, b = nullptr;
+      cudaError_t e = cudaEventCreate(&a);
+      if (e == cudaSuccess) e = cudaEventCreate(&b);
+      float best_ms = 1e30f;
+      for (int k = 0; k < n && e == cudaSuccess; k++) {
+        e = conv(ci, co, mfs[k], d, nb, in, wf, bias, out, mask, relu, s);
+        if (e == cudaSuccess) e = cudaEventRecord(a, s);
+        for (int r = 0; r < 3 && e == cudaSuccess; r++) e = conv(ci, co, mfs[k], d, nb, in, wf, bias, out, mask, relu, s);
+        if (e == cudaSuccess) e = cudaEventRecord(b, s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+        if (e == cudaSuccess && ms < best_ms) {
+          best_ms = ms;
+          best = mfs[k];
+        }
+      }
+      if (a) cudaEventDestroy(a);
+      if (b) cudaEventDestroy(b);
+      if (e != cudaSuccess) return e;
+    }
+    tuned_[key] = best;
+    return conv(ci, co, best, d, nb, in, wf, bias, out, mask, relu, s);
   }
 
   int adam_step(int t, float lr, cudaStream_t s, std::string& err) {
@@ -539,6 +601,7 @@ class Net : public NetRuntime {
   // scale (2) + input (1) + forward (10 convolutions, 2 pools, 2 upsamplings,
   // output layer) + guess (1)
   int launches_per_predict() const override { return 19; }
+  int kind() const override { return kind_; }
 
   int device_ = 0;
   cudaStream_t s_ = nullptr;
@@ -549,6 +612,10 @@ class Net : public NetRuntime {
   long long woff_[NCONV + 1] = {}, boff_[NCONV + 1] = {};
   long long nparams_ = 0;
   float scale_c_ = 1.f;
+  int kind_ = 0;  // what the network was trained to map (PLUME_PAIRS_*)
+  std::map<std::tuple<int, int, int, int, int, int>, int> tuned_;  // tile shape per (cin, cout, grid, batch)
+  std::mutex tune_mu_;
+  bool tune_off_ = getenv("PLUME_CONV_TUNE_OFF") != nullptr;  // fixed first shape
   std::string err_;
 };
 
@@ -561,6 +628,7 @@ struct Dataset {
   double target_rms = 0;
   double seconds = 0;
   int device = 0;
+  int kind = 0;  // PLUME_PAIRS_SOLVE or PLUME_PAIRS_CORRECTION
   ~Dataset() {
     if (in) cudaFree(in);
     if (tgt) cudaFree(tgt);
@@ -676,7 +744,7 @@ int plume_net_save(plume_net* net, const char* path) {
   if (rc != PLUME_OK) return rc;
   FILE* f = fopen(path, "wb");
   if (!f) return fail(PLUME_ERR_IO, std::string("cannot write ") + path);
-  const int32_t hdr[2] = {1, 0};
+  const int32_t hdr[2] = {1, net->net.kind_};
   const float sc[2] = {net->net.scale_c_, 0.f};
   bool ok = fwrite("PLUMENET", 1, 8, f) == 8 && fwrite(hdr, 4, 2, f) == 2 && fwrite(&n, 8, 1, f) == 1 &&
             fwrite(sc, 4, 2, f) == 2 && fwrite(w.data(), 4, (size_t)n, f) == (size_t)n;
@@ -700,6 +768,7 @@ int plume_net_load(plume_net* net, const char* path) {
   if (!ok) return fail(PLUME_ERR_IO, std::string("not a network file of this layout: ") + path);
   int rc = plume_net_set_params(net, w.data(), n);
   if (rc != PLUME_OK) return rc;
+  net->net.kind_ = (hdr[1] == 1) ? 1 : 0;
   return plume_net_set_scale(net, sc[0]);
 }
 
@@ -743,8 +812,9 @@ int plume_net_loss_grad(plume_net* net, const int32_t res[3], int32_t batch, int
 int plume_dataset_generate(const plume_dataset_spec* spec, plume_dataset** out) {
   if (!spec || !out) return fail(PLUME_ERR_INVALID, "null argument");
   const plume_dataset_spec& sp = *spec;
-  if (sp.plumes < 1 || sp.steps < 1 || sp.skip < 0 || sp.skip >= sp.steps || sp.threads < 1)
-    return fail(PLUME_ERR_INVALID, "plumes, steps, skip or threads out of range");
+  if (sp.plumes < 1 || sp.steps < 1 || sp.skip < 0 || sp.skip >= sp.steps || sp.threads < 1 ||
+      sp.kind < 0 || sp.kind > 1)
+    return fail(PLUME_ERR_INVALID, "plumes, steps, skip, threads or kind out of range");
   for (int k = 0; k < 3; k++)
     if (sp.res[k] < 8 || sp.res[k] % 4 != 0) return fail(PLUME_ERR_INVALID, "grid dimensions must be multiples of 4");
   std::string err;
@@ -754,6 +824,7 @@ int plume_dataset_generate(const plume_dataset_spec* spec, plume_dataset** out) 
   Dataset& ds = h->ds;
   ds.d = make_dims(sp.res[0], sp.res[1], sp.res[2]);
   ds.device = sp.device;
+  ds.kind = sp.kind;
   const int per = sp.steps - sp.skip;
   ds.pairs = sp.plumes * per;
   const size_t cells = (size_t)ds.d.cells;
@@ -776,12 +847,16 @@ int plume_dataset_generate(const plume_dataset_spec* spec, plume_dataset** out) 
     }
     double* dpart = nullptr;
     float* scale = nullptr;
-    if (cudaMalloc((void**)&dpart, kMaxBlocks * 8 + 256) != cudaSuccess) {
+    const size_t cells_al = al(cells * 4);
+    if (cudaMalloc((void**)&dpart, kMaxBlocks * 8 + 256 + (sp.kind == 1 ? 2 * cells_al : 0)) != cudaSuccess) {
       rcs[t] = PLUME_ERR_OOM;
       e = "workspace";
       return;
     }
     scale = (float*)((char*)dpart + kMaxBlocks * 8);
+    // correction pairs: the previous pressure and the residual it leaves
+    float* p_prev = sp.kind == 1 ? (float*)((char*)dpart + kMaxBlocks * 8 + 256) : nullptr;
+    float* r0 = sp.kind == 1 ? (float*)((char*)p_prev + cells_al) : nullptr;
     for (int i = t; i < sp.plumes && rcs[t] == PLUME_OK; i += T) {
       const uint64_t seed = sp.seed + (uint64_t)i;
       plume_params p;
@@ -823,7 +898,14 @@ int plume_dataset_generate(const plume_dataset_spec* spec, plume_dataset** out) 
       const float* x = (const float*)eng->device_field(PLUME_F_PRESSURE);
       const int nb = blocks_for(ds.d.cells);
       const double count = (double)(X - 2) * (Y - 2) * (Z - 2);
+      if (sp.kind == 1 && cudaMemsetAsync(p_prev, 0, cells * 4, s) != cudaSuccess) rc = PLUME_ERR_CUDA;
       for (int st = 0; st < sp.steps && rc == PLUME_OK; st++) {
+        if (sp.kind == 1 && st > 0 &&
+            cudaMemcpyAsync(p_prev, x, cells * 4, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+          rc = PLUME_ERR_CUDA;
+          e = "copy of the previous pressure";
+          break;
+        }
         rc = plume_add_source(ph, st);
         if (rc == PLUME_OK) rc = plume_step(ph, nullptr);
         if (rc != PLUME_OK) {
@@ -832,10 +914,18 @@ int plume_dataset_generate(const plume_dataset_spec* spec, plume_dataset** out) 
         }
         if (st < sp.skip) continue;
         const size_t slot = (size_t)i * per + (st - sp.skip);
-        k_sumsq_interior<float><<<nb, kThreads, 0, s>>>(ds.d, b, dpart);
-        k_rms_scale<<<1, 256, 0, s>>>(dpart, nb, count, scale);
-        k_store_pair<float><<<nb, kThreads, 0, s>>>(ds.d, b, x, scale, ds.in + slot * cells,
-                                                    ds.tgt + slot * cells);
+        if (sp.kind == 1) {  // (r0, p - p_prev) with r0 = b - A p_prev
+          k_closed_box_residual<float><<<nb, kThreads, 0, s>>>(ds.d, b, p_prev, r0);
+          k_sumsq_interior<float><<<nb, kThreads, 0, s>>>(ds.d, r0, dpart);
+          k_rms_scale<<<1, 256, 0, s>>>(dpart, nb, count, scale);
+          k_store_correction<float><<<nb, kThreads, 0, s>>>(ds.d, r0, x, p_prev, scale, ds.in + slot * cells,
+                                                            ds.tgt + slot * cells);
+        } else {
+          k_sumsq_interior<float><<<nb, kThreads, 0, s>>>(ds.d, b, dpart);
+          k_rms_scale<<<1, 256, 0, s>>>(dpart, nb, count, scale);
+          k_store_pair<float><<<nb, kThreads, 0, s>>>(ds.d, b, x, scale, ds.in + slot * cells,
+                                                      ds.tgt + slot * cells);
+        }
         if (cudaGetLastError() != cudaSuccess) {
           rc = PLUME_ERR_CUDA;
           e = "pair store launch";
@@ -927,6 +1017,7 @@ int plume_net_train(plume_net* net, plume_dataset* dsh, const plume_train_spec* 
   int rc = ws.alloc(r, sp.batch, true, err);
   if (rc != PLUME_OK) return fail(rc, err);
   m.scale_c_ = (float)ds.target_rms;
+  m.kind_ = ds.kind;
   const float inv_scale = ds.target_rms > 0 ? (float)(1.0 / ds.target_rms) : 1.f;
   const double interior = (double)(r[0] - 2) * (r[1] - 2) * (r[2] - 2);
   int* hidx = nullptr;

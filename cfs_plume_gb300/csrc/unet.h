@@ -15,6 +15,9 @@ class NetRuntime {
   virtual int predict(void* ws, const void* b, void* x, int is_double, void* stream, std::string& err) = 0;
   // Kernel launches one predict() makes.
   virtual int launches_per_predict() const = 0;
+  // 0: maps a right-hand side b to the solution; 1: maps the residual of the
+  // previous step's pressure to the pressure change
+  virtual int kind() const = 0;
 };
 
 }  // namespace plume

@@ -81,15 +81,18 @@ __device__ __forceinline__ uint32_t pack_bf2(float lo, float hi) {
 }
 
 // ------------------------------------------------------------- convolution
-// Brick shape: 16 cells along x, BY x BZ rows; 8 warps, MF row fragments each.
-template <int CIN, int COUT>
+// Brick shape: 16 cells along x, BY x BZ rows; 8 warps, MF row fragments
+// (16-cell rows) each.  MF in {1, 2, 4, 8} is the tile-shape knob the
+// autotuner picks per layer and grid (unet.cu); every shape accumulates each
+// output in the same order, so the choice never changes a result.
+template <int CIN, int COUT, int MF_>
 struct ConvCfg {
   static constexpr int NF = COUT / 8;
   static constexpr int KC = CIN / 16;
-  static constexpr int MF = (NF > 8) ? 1 : ((NF <= 4 && CIN <= 32) ? 4 : 2);
+  static constexpr int MF = MF_;
   static constexpr int WARPS = 8;
   static constexpr int ROWS = WARPS * MF;
-  static constexpr int BY = (MF == 4) ? 8 : 4;
+  static constexpr int BY = (MF >= 4) ? 8 : 4;
   static constexpr int BZ = ROWS / BY;
   static constexpr int HX = 18, HY = BY + 2, HZ = BZ + 2;
   static constexpr int HCELLS = HX * HY * HZ;
@@ -99,9 +102,9 @@ struct ConvCfg {
   static_assert(ROWS % BY == 0, "brick rows");
 };
 
-template <int CIN, int COUT>
+template <int CIN, int COUT, int MF>
 inline int conv_bricks(const Dims& d) {
-  using C = ConvCfg<CIN, COUT>;
+  using C = ConvCfg<CIN, COUT, MF>;
   return ((d.X + 15) / 16) * ((d.Y + C::BY - 1) / C::BY) * ((d.Z + C::BZ - 1) / C::BZ);
 }
 
@@ -129,11 +132,11 @@ __device__ __forceinline__ void load_halo(const Dims& d, const bf16* src, int cs
 //   relu : clamp at 0
 //   mask : if mask.p, zero every output whose mask element is not > 0
 // grid: (bricks, batch); block 256; dynamic smem ConvCfg::SMEM
-template <int CIN, int COUT>
+template <int CIN, int COUT, int MF>
 __global__ void __launch_bounds__(256) k_conv3(Dims d, View in, const uint2* __restrict__ wf,
                                                const float* __restrict__ bias, View out, View mask,
                                                int relu) {
-  using C = ConvCfg<CIN, COUT>;
+  using C = ConvCfg<CIN, COUT, MF>;
   extern __shared__ __align__(128) unsigned char conv_smem[];
   bf16* hb = reinterpret_cast<bf16*>(conv_smem);
   const int nbx = (d.X + 15) / 16, nby = (d.Y + C::BY - 1) / C::BY;
@@ -158,13 +161,24 @@ __global__ void __launch_bounds__(256) k_conv3(Dims d, View in, const uint2* __r
       for (int k = 0; k < 4; k++) acc[i][j][k] = 0.f;
 
   const uint32_t hbase = smem_u32addr(hb);
+  // B fragments are loaded one k-chunk ahead of their use (register double
+  // buffer), so the weight loads overlap the previous chunk's MMAs
+  constexpr int NSTEP = 27 * C::KC;
+  uint2 bnext[C::NF];
+#pragma unroll
+  for (int nf = 0; nf < C::NF; nf++) bnext[nf] = __ldg(&wf[nf * 32 + lane]);
   for (int off = 0; off < 27; off++) {
     const int dz = off / 9 - 1, dy = (off / 3) % 3 - 1, dx = off % 3 - 1;
 #pragma unroll
     for (int kc = 0; kc < C::KC; kc++) {
       uint2 bw[C::NF];
 #pragma unroll
-      for (int nf = 0; nf < C::NF; nf++) bw[nf] = __ldg(&wf[((off * C::KC + kc) * C::NF + nf) * 32 + lane]);
+      for (int nf = 0; nf < C::NF; nf++) bw[nf] = bnext[nf];
+      const int step = off * C::KC + kc + 1;
+      if (step < NSTEP) {
+#pragma unroll
+        for (int nf = 0; nf < C::NF; nf++) bnext[nf] = __ldg(&wf[(step * C::NF + nf) * 32 + lane]);
+      }
 #pragma unroll
       for (int mf = 0; mf < C::MF; mf++) {
         const int row = warp * C::MF + mf;
@@ -763,6 +777,45 @@ __global__ void k_store_pair(Dims d, const T* b, const T* p, const float* scale,
     const bool in = interior(d, i);
     in_slot[i] = __float2bfloat16_rn(in ? (float)b[i] * inv : 0.f);
     tgt_slot[i] = in ? (float)p[i] * inv : 0.f;
+  }
+}
+
+// r = b - A x on interior cells for a closed box (A: number of interior
+// neighbours on the diagonal, -1 per interior neighbour), FP64 accumulation;
+// 0 on the border
+template <typename T>
+__global__ void k_closed_box_residual(Dims d, const T* b, const T* x, float* r) {
+  const long long sy = d.X, sz = (long long)d.X * d.Y;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.cells;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int cx = (int)(i % d.X), cy = (int)((i / d.X) % d.Y), cz = (int)(i / sz);
+    float v = 0.f;
+    if (cx > 0 && cx < d.X - 1 && cy > 0 && cy < d.Y - 1 && cz > 0 && cz < d.Z - 1) {
+      double s = 0.0;
+      int cnt = 0;
+      if (cx > 1) { s += (double)x[i - 1]; cnt++; }
+      if (cx < d.X - 2) { s += (double)x[i + 1]; cnt++; }
+      if (cy > 1) { s += (double)x[i - sy]; cnt++; }
+      if (cy < d.Y - 2) { s += (double)x[i + sy]; cnt++; }
+      if (cz > 1) { s += (double)x[i - sz]; cnt++; }
+      if (cz < d.Z - 2) { s += (double)x[i + sz]; cnt++; }
+      v = (float)((double)b[i] - ((double)cnt * (double)x[i] - s));
+    }
+    r[i] = v;
+  }
+}
+
+// one correction pair into the store: r0 / s (BF16) and (p - p_prev) / s
+template <typename T>
+__global__ void k_store_correction(Dims d, const float* r0, const T* p, const float* p_prev,
+                                   const float* scale, bf16* in_slot, float* tgt_slot) {
+  const float s = scale[0];
+  const float inv = s > 0.f ? 1.f / s : 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.cells;
+       i += (long long)gridDim.x * blockDim.x) {
+    const bool in = interior(d, i);
+    in_slot[i] = __float2bfloat16_rn(in ? r0[i] * inv : 0.f);
+    tgt_slot[i] = in ? ((float)p[i] - p_prev[i]) * inv : 0.f;
   }
 }
 

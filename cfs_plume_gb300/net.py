@@ -12,11 +12,13 @@ from .plume import PlumeError, load_library
 
 _signed = False
 LOSS_MSE, LOSS_ENERGY = 0, 1
+PAIRS_SOLVE, PAIRS_CORRECTION = 0, 1
 
 
 class PlumeDatasetSpec(C.Structure):
     _fields_ = [("res", C.c_int32 * 3), ("plumes", C.c_int32), ("steps", C.c_int32), ("skip", C.c_int32),
-                ("threads", C.c_int32), ("device", C.c_int32), ("seed", C.c_uint64), ("tol", C.c_double)]
+                ("threads", C.c_int32), ("device", C.c_int32), ("seed", C.c_uint64), ("tol", C.c_double),
+                ("kind", C.c_int32)]
 
 
 class PlumeTrainSpec(C.Structure):
@@ -154,11 +156,11 @@ class PlumeNet:
 class PairStore:
     """(b / rms(b), p / rms(b)) pairs from plain solves of randomised plumes, on the GPU."""
 
-    def __init__(self, res, plumes, steps, skip=0, threads=8, seed=0, tol=1e-6, device=0):
+    def __init__(self, res, plumes, steps, skip=0, threads=8, seed=0, tol=1e-6, device=0, kind=PAIRS_SOLVE):
         self.lib = _lib()
         self.res = tuple(res)
         sp = PlumeDatasetSpec(res=(C.c_int32 * 3)(*res), plumes=plumes, steps=steps, skip=skip, threads=threads,
-                              device=device, seed=seed, tol=tol)
+                              device=device, seed=seed, tol=tol, kind=kind)
         self.h = C.c_void_p()
         _check(self.lib.plume_dataset_generate(C.byref(sp), C.byref(self.h)))
         n, rms, secs = C.c_int32(), C.c_double(), C.c_double()

@@ -7,7 +7,9 @@
    source centre uniform in the middle third of the floor, buoyancy U[0.5, 2],
    vorticity U[0, 4], +-0.05 seeded noise) are simulated with plain MIC-PCG
    (FP32 fields, rel-L2 1e-6); every solve after `--skip` steps is kept on the
-   GPU as (b / rms(b), p / rms(b)).
+   GPU as (b / rms(b), p / rms(b)), or with `--pairs correction` (the default)
+   as (r0 / rms(r0), (p - p_prev) / rms(r0)), r0 = b - A p_prev, p_prev the
+   previous step's pressure.
 2. Training: Adam on the network's own BF16 tensor-core forward and backward
    kernels, cosine step size, the last `--val-plumes` plumes held out; the
    loss is the energy norm e^T A e of the error (the norm CG's error bound
@@ -27,7 +29,7 @@ import time
 import numpy as np
 
 from . import _abi
-from .net import LOSS_ENERGY, LOSS_MSE, PairStore, PlumeNet
+from .net import LOSS_ENERGY, LOSS_MSE, PAIRS_CORRECTION, PAIRS_SOLVE, PairStore, PlumeNet
 from .plume import Plume
 
 
@@ -68,6 +70,8 @@ def main(argv=None):
     ap.add_argument("--lr-final", type=float, default=5e-5)
     ap.add_argument("--loss", default="energy", choices=["energy", "mse"],
                     help="energy: e^T A e of the error (CG's error norm); mse: squared error")
+    ap.add_argument("--pairs", default="correction", choices=["correction", "solve"],
+                    help="correction: (b - A p_prev) -> p - p_prev; solve: b -> p")
     ap.add_argument("--seed", type=int, default=1000)
     ap.add_argument("--init", default=None, help="start from these weights")
     ap.add_argument("--out", default=None)
@@ -84,7 +88,8 @@ def main(argv=None):
         net = PlumeNet(path=a.init)
         summary = {"weights": a.init, "eval": {}}
         return finish(a, net, summary, t0)
-    ds = PairStore(res, a.plumes, a.steps, skip=a.skip, threads=a.threads, seed=a.seed)
+    ds = PairStore(res, a.plumes, a.steps, skip=a.skip, threads=a.threads, seed=a.seed,
+                   kind=PAIRS_CORRECTION if a.pairs == "correction" else PAIRS_SOLVE)
     print("pairs %d from %d plumes in %.1f s (solution rms %.4g)" % (ds.pairs, a.plumes, ds.seconds,
                                                                       ds.target_rms), flush=True)
     net = PlumeNet(seed=a.seed, path=a.init)
@@ -100,7 +105,7 @@ def main(argv=None):
     if a.out:
         os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
         net.save(a.out)
-    summary = {"pairs": ds.pairs, "grid": list(res), "generate_s": ds.seconds, "train_s": secs, "loss": a.loss,
+    summary = {"pairs": ds.pairs, "pair_kind": a.pairs, "grid": list(res), "generate_s": ds.seconds, "train_s": secs, "loss": a.loss,
                "epochs": a.epochs, "batch": a.batch, "train_loss": [float(v) for v in tl],
                "val_loss": [float(v) for v in vl], "eval": {}}
     return finish(a, net, summary, t0)

@@ -82,7 +82,17 @@ typedef struct plume_dataset_spec {
   int32_t device;
   uint64_t seed;
   double tol;       /* rel-L2 stop test of the generating solves               */
+  int32_t kind;     /* PLUME_PAIRS_SOLVE or PLUME_PAIRS_CORRECTION             */
 } plume_dataset_spec;
+
+/* What a pair (and a network trained on such pairs) maps:
+   SOLVE:      b / rms(b) -> p / rms(b)   (the solve's right-hand side to its
+               solution; the step uses x0 = scaled network output)
+   CORRECTION: r0 / rms(r0) -> (p - p_prev) / rms(r0), r0 = b - A p_prev with
+               p_prev the previous step's pressure (the step uses
+               x0 = p_prev + scaled network output on r0).
+   The kind is stored in the network file. */
+enum { PLUME_PAIRS_SOLVE = 0, PLUME_PAIRS_CORRECTION = 1 };
 
 /* Simulates `plumes` closed-box plumes with the batched-plume randomisation
    (box source centre uniform in the middle third of the floor, buoyancy

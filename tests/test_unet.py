@@ -155,12 +155,15 @@ def test_gradients_are_deterministic(net):
 
 
 @pytest.mark.gpu
-def test_pairs_are_normalised_solves():
-    """Generated pairs: b / rms(b) has unit rms over interior cells and the
-    target solves the Poisson system A x = b to the stop test."""
+@pytest.mark.parametrize("kind", [0, 1])
+def test_pairs_are_normalised_solves(kind):
+    """Generated pairs: the input has unit rms over interior cells and the
+    target solves A x = input to the stop test -- for solve pairs (b, p) and
+    for correction pairs (r0 = b - A p_prev, p - p_prev), since
+    A (p - p_prev) = b - A p_prev."""
     from cfs_plume_gb300.net import PairStore
     res = (16, 24, 16)
-    ds = PairStore(res, plumes=2, steps=4, skip=1, threads=2, seed=11)
+    ds = PairStore(res, plumes=2, steps=4, skip=1, threads=2, seed=11, kind=kind)
     assert ds.pairs == 6
     X, Y, Z = res
     for i in (0, 5):
@@ -248,8 +251,9 @@ WEIGHTS = __import__("os").path.join(__import__("os").path.dirname(__import__("o
 
 @pytest.mark.gpu
 def test_trained_network_saves_iterations():
-    """The committed network (trained on 20k pairs of 64x96x64 plumes with
-    the energy loss) against the zero start on an unseen 64x96x64 plume: fewer
+    """The committed network (trained on 20k correction pairs of 64x96x64
+    plumes with the energy loss) against the zero start on an unseen 64x96x64
+    plume: fewer
     PCG iterations per step, every solve meeting the same rel-L2 1e-6 test
     without fallback, velocity within 1e-4 relative L2."""
     from cfs_plume_gb300.net import PlumeNet
@@ -260,5 +264,28 @@ def test_trained_network_saves_iterations():
     il = np.mean([s.iterations for s in sl[2:]])
     assert not any(s.fallback for s in sl)
     assert all(s.converged and s.rel_residual <= 1e-6 for s in sl)
-    assert il < 0.93 * ip, (il, ip)
+    assert il < 0.85 * ip, (il, ip)
     assert rel(vl, vp) < 1e-4
+
+
+@pytest.mark.gpu
+def test_tile_shapes_give_identical_outputs(monkeypatch):
+    """The autotuner's tile shape never changes a result: the forward pass
+    with tuning (fastest shape per layer) equals the fixed smallest shape bit
+    for bit."""
+    from cfs_plume_gb300.net import PlumeNet
+    params = random_params(10)
+    rng = np.random.default_rng(11)
+    res = (32, 48, 32)
+    inp = smooth_field(rng, res, 2).astype(np.float32)
+    outs = []
+    for off in (True, False):
+        if off:
+            monkeypatch.setenv("PLUME_CONV_TUNE_OFF", "1")
+        else:
+            monkeypatch.delenv("PLUME_CONV_TUNE_OFF", raising=False)
+        n = PlumeNet(seed=0)
+        n.params = params
+        outs.append(n.forward(inp, res))
+        n.close()
+    np.testing.assert_array_equal(outs[0], outs[1])
