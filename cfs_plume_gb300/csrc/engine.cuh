@@ -394,7 +394,7 @@ class EngineT : public Engine {
       // (a network trained on solve pairs maps b itself: x0 = g c, c = net(b))
       if (!net_) return fail(PLUME_ERR_STATE, "learned warm start without an attached network");
       const bool corr = net_->kind() == 1;
-      k_zero_border<T><<<gN, 256, 0, s_>>>(g_, pres_);
+      k_zero_border<T><<<gF, 256, 0, s_>>>(g_, pres_);
       PL_CHECK_LAUNCH();
       if (corr) {
         k_residual<T><<<gN, 256, 0, s_>>>(g_, div_, pres_, r_);
@@ -404,7 +404,7 @@ class EngineT : public Engine {
       const int prc = net_->predict(net_ws_, rhs, z_, std::is_same<T, double>::value ? 1 : 0, s_, err_);
       if (prc != PLUME_OK) return prc;
       launches_ += net_->launches_per_predict();
-      k_zero_border<T><<<gN, 256, 0, s_>>>(g_, z_);
+      k_zero_border<T><<<gF, 256, 0, s_>>>(g_, z_);
       PL_CHECK_LAUNCH();
       k_guess_dots<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, z_, z_, rhs, st_, part_);
       PL_CHECK_LAUNCH();

@@ -192,12 +192,26 @@ __global__ void k_residual(Grid g, const T* b, const T* x, T* r) {
   }
 }
 
-// zero the six border faces of a full-grid field
+// zero the six border faces of a full-grid field (face cells only: the two
+// z faces, the two y faces, the two x faces; edges are written more than once)
 template <typename T>
 __global__ void k_zero_border(Grid g, T* f) {
-  PL_GRID_STRIDE(i, g.N) {
-    const int x = i % g.X, y = (i / g.X) % g.Y, z = i / g.slab;
-    if (x == 0 || y == 0 || z == 0 || x == g.X - 1 || y == g.Y - 1 || z == g.Z - 1) f[i] = T(0);
+  const int nz = 2 * g.slab, ny = 2 * g.X * g.Z, nx = 2 * g.Y * g.Z;
+  PL_GRID_STRIDE(k, nz + ny + nx) {
+    int i;
+    if (k < nz) {
+      const int side = k / g.slab, j = k - side * g.slab;
+      i = j + (side ? (g.Z - 1) * g.slab : 0);
+    } else if (k < nz + ny) {
+      const int m = k - nz, side = m / (g.X * g.Z), j = m - side * g.X * g.Z;
+      const int x = j % g.X, z = j / g.X;
+      i = x + (side ? g.Y - 1 : 0) * g.X + z * g.slab;
+    } else {
+      const int m = k - nz - ny, side = m / (g.Y * g.Z), j = m - side * g.Y * g.Z;
+      const int y = j % g.Y, z = j / g.Y;
+      i = (side ? g.X - 1 : 0) + y * g.X + z * g.slab;
+    }
+    f[i] = T(0);
   }
 }
 
