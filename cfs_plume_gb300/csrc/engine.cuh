@@ -824,6 +824,12 @@ class EngineT : public Engine {
     // zeroed so that 0 * d_old on the first iteration can never see stale
     // non-finite values
     PL_TRY(cudaMemsetAsync(sd_, 0, (size_t)k_.total * sizeof(T), s_));
+    if (!prof_on_ && cg_graph_ready()) {
+      // the whole iteration loop as one graph launch (conditional while node)
+      PL_TRY(cudaMemsetAsync(&st_->bodies, 0, sizeof(int), s_));
+      PL_TRY(cudaGraphLaunch(cg_exec_, s_));
+      return finish_solve(x, true);
+    }
     int chunk = 4;
     T* dcur = sd_;  // direction of the previous iteration (beta = 0 on the first)
     T* dnext = sd2_;
@@ -853,10 +859,85 @@ class EngineT : public Engine {
       if (st_host_->done) break;
       if (chunk < 16) chunk *= 2;
     }
+    return finish_solve(x, false);
+  }
+
+  // The CG iteration loop as a CUDA graph: a conditional while node whose
+  // body is 16 iterations (SpMV + direction, update, forward and backward MIC
+  // sweeps, r.z) followed by k_cg_continue, which sets the loop condition from
+  // the device-side state.  Built on first use by capturing the body on the
+  // handle's stream; if any step fails, the host-driven loop is used instead.
+  static constexpr int kCgBody = 16;  // even: the direction buffers swap back
+  static constexpr int kCgBodyLaunches = kCgBody * 5 + 1;
+  bool cg_graph_ready() {
+    if (cg_exec_) return true;
+    if (cg_graph_failed_) return false;
+    const int saved = launches_;
+    cudaGraph_t graph = nullptr;
+    cudaGraphConditionalHandle h = 0;
+    bool capturing = false;
+    cudaError_t e = cudaGraphCreate(&graph, 0);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};  // every other byte zero
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp);
+    if (e == cudaSuccess)
+      e = cudaStreamBeginCaptureToGraph(s_, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeRelaxed);
+    capturing = e == cudaSuccess;
+    int rc = PLUME_OK;
+    T* dcur = sd_;
+    T* dnext = sd2_;
+    for (int kk = 0; kk < kCgBody && e == cudaSuccess && rc == PLUME_OK; kk++) {
+      rc = launch_spmv_dir(sz_, dcur, dnext, sq_);
+      if (rc == PLUME_OK) {
+        k_cgs_axpy_v<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, dnext, sq_, sx_, sr_, st_, part_);
+        e = cudaGetLastError();
+      }
+      if (rc == PLUME_OK && e == cudaSuccess) rc = mic_sweeps(sr_, sqf_, sz_);
+      if (rc == PLUME_OK && e == cudaSuccess) {
+        k_cgs_rz_v<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sr_, sz_, st_, part_);
+        e = cudaGetLastError();
+      }
+      std::swap(dcur, dnext);
+    }
+    if (e == cudaSuccess && rc == PLUME_OK) {
+      k_cg_continue<<<1, 32, 0, s_>>>(h, st_);
+      e = cudaGetLastError();
+    }
+    if (capturing) {
+      cudaGraph_t body = nullptr;
+      const cudaError_t e2 = cudaStreamEndCapture(s_, &body);
+      if (e == cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess && rc == PLUME_OK) e = cudaGraphInstantiate(&cg_exec_, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    launches_ = saved;  // captured launches ran nothing
+    err_.clear();
+    (void)cudaGetLastError();
+    if (e != cudaSuccess || rc != PLUME_OK || !cg_exec_) {
+      if (cg_exec_) cudaGraphExecDestroy(cg_exec_);
+      cg_exec_ = nullptr;
+      cg_graph_failed_ = true;
+      return false;
+    }
+    return true;
+  }
+
+  // Solution back to the natural layout and the solver state to the host
+  // (one synchronisation).
+  int finish_solve(T* x, bool graph) {
+    const int gK = grid_for(k_.total);
+    int rc = PLUME_OK;
     k_from_skew<T><<<gK, 256, 0, s_>>>(g_, k_, sx_, x);
     PL_CHECK_LAUNCH();
     PL_TRY(cudaMemcpyAsync(st_host_, st_, sizeof(CgState), cudaMemcpyDeviceToHost, s_));
     PL_TRY(cudaStreamSynchronize(s_));
+    if (graph) launches_ += st_host_->bodies * kCgBodyLaunches;
     if (prof_on_) {
       // iterations whose sweeps ran: all counted ones, less the last when the
       // rel-L2 test stopped the solve before its sweeps (k_cgs_axpy_v)
@@ -971,6 +1052,8 @@ class EngineT : public Engine {
 
   void release() {
     if (s_) cudaStreamSynchronize(s_);
+    if (cg_exec_) cudaGraphExecDestroy(cg_exec_);
+    cg_exec_ = nullptr;
     if (net_ws_) net_->free_workspace(net_ws_);
     net_ws_ = nullptr;
     if (pool_) cudaFree(pool_);
@@ -1029,6 +1112,8 @@ class EngineT : public Engine {
   void* net_ws_ = nullptr;
   int last_fallback_ = 0;
   int last_iters_ = 0;  // iterations of the last accepted step solve
+  cudaGraphExec_t cg_exec_ = nullptr;  // CG loop graph (cg_graph_ready)
+  bool cg_graph_failed_ = getenv("PLUME_NO_CG_GRAPH") != nullptr;
   bool host_direct_ = false;  // downloads written by a kernel into host memory
   static constexpr int kProfEvents = 64;
   bool prof_on_ = false;

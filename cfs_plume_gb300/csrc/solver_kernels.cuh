@@ -25,7 +25,7 @@ struct CgState {
   double guess_scale, guess_scale2;  // Galerkin factors of the last learned guess
   double guess_mean, guess_mean2;    // interior means removed (closed boxes)
   int iter, max_iters, criterion, done;
-  int converged, broke, wave_err, pad1;
+  int converged, broke, wave_err, bodies;  // bodies: CG-graph loop bodies run this solve
   unsigned int ticket[4];
 };
 
@@ -212,6 +212,18 @@ __global__ void k_zero_border(Grid g, T* f) {
       i = (side ? g.X - 1 : 0) + y * g.X + z * g.slab;
     }
     f[i] = T(0);
+  }
+}
+
+// Last node of the CG-graph loop body: keep looping while the solve is not
+// done.  The body count also bounds the loop on the device: a body holds 16
+// iterations and every iteration counts towards max_iters, so a loop that ran
+// (max_iters + 64) / 16 bodies stops even if no kernel ever set `done`.
+static __global__ void k_cg_continue(cudaGraphConditionalHandle h, CgState* st) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    st->bodies += 1;
+    const bool more = !st->done && st->bodies * 16 <= st->max_iters + 64;
+    cudaGraphSetConditional(h, more ? 1u : 0u);
   }
 }
 

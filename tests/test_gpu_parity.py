@@ -299,3 +299,25 @@ def test_direct_download_matches_staged(monkeypatch):
         h.close()
     for a, b in zip(out["0"], out["1"]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [_abi.PREC_FP32, _abi.PREC_FP64])
+def test_cg_graph_matches_host_loop(monkeypatch, precision):
+    """The CG loop captured as a CUDA graph (conditional while node, the loop
+    condition set on the device) runs the same kernels in the same order as
+    the host-driven loop: identical iteration counts and fields."""
+    res = (24, 32, 24)
+    out = {}
+    for flag in ("1", None):
+        if flag:
+            monkeypatch.setenv("PLUME_NO_CG_GRAPH", flag)
+        else:
+            monkeypatch.delenv("PLUME_NO_CG_GRAPH", raising=False)
+        h = Plume(_abi.plume_config(res, precision=precision))
+        _, st = h.run_timed(0, 3)
+        out[flag] = ([s.iterations for s in st], h.field("velocity"), h.field("pressure"))
+        h.close()
+    assert out["1"][0] == out[None][0]
+    np.testing.assert_array_equal(out["1"][1], out[None][1])
+    np.testing.assert_array_equal(out["1"][2], out[None][2])
