@@ -576,6 +576,7 @@ class EngineT : public Engine {
     return PLUME_OK;
   }
 
+  void use_cg_graph(bool on) override { no_cg_graph_ = !on; }
   const void* device_field(int field) override { return scalar_ptr(field); }
   void* stream_handle() override { return (void*)s_; }
   int attach_net(NetRuntime* net) override {
@@ -824,7 +825,7 @@ class EngineT : public Engine {
     // zeroed so that 0 * d_old on the first iteration can never see stale
     // non-finite values
     PL_TRY(cudaMemsetAsync(sd_, 0, (size_t)k_.total * sizeof(T), s_));
-    if (!prof_on_ && cg_graph_ready()) {
+    if (!prof_on_ && !no_cg_graph_ && cg_graph_ready()) {
       // the whole iteration loop as one graph launch (conditional while node)
       PL_TRY(cudaMemsetAsync(&st_->bodies, 0, sizeof(int), s_));
       PL_TRY(cudaGraphLaunch(cg_exec_, s_));
@@ -1113,6 +1114,7 @@ class EngineT : public Engine {
   int last_fallback_ = 0;
   int last_iters_ = 0;  // iterations of the last accepted step solve
   cudaGraphExec_t cg_exec_ = nullptr;  // CG loop graph (cg_graph_ready)
+  bool no_cg_graph_ = false;
   bool cg_graph_failed_ = getenv("PLUME_NO_CG_GRAPH") != nullptr;
   bool host_direct_ = false;  // downloads written by a kernel into host memory
   static constexpr int kProfEvents = 64;

@@ -46,6 +46,9 @@ class Engine {
   virtual const void* device_field(int field) = 0;
   virtual void* stream_handle() = 0;
   virtual int attach_net(NetRuntime* net) = 0;
+  // CG loop as a CUDA graph (default) or driven from the host; many handles
+  // stepping concurrently interleave better with the host-driven loop
+  virtual void use_cg_graph(bool on) = 0;
   virtual int32_t total_steps() const = 0;
   virtual double total_time() const = 0;
   virtual double dx() const = 0;

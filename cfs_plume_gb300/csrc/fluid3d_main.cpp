@@ -15,7 +15,9 @@
 //   source noise (0), seed (0), precision (fp64 | fp32), solver criterion
 //   (reference | rel2), solver tolerance (1e-10), solver max iterations (1000),
 //   mic tau (0.97), mic sigma (0.25), damping (0.9), warm start (zero |
-//   previous), write state (1), write streams (1), device (0).
+//   previous | learned), warm start network (path of a trained network for
+//   "learned"; default cfs_plume_gb300/weights/unet_warmstart.bin next to the
+//   binary's ../weights), write state (1), write streams (1), device (0).
 #include <sys/stat.h>
 
 #include <cctype>
@@ -29,6 +31,7 @@
 #include <vector>
 
 #include "../../include/plume.h"
+#include "../../include/plume_net.h"
 
 namespace {
 
@@ -109,6 +112,14 @@ int check(int rc, plume_handle* h, const char* what) {
 
 }  // namespace
 
+// <dir of the binary>/../weights/unet_warmstart.bin (the package layout)
+static std::string default_network_path(const char* argv0) {
+  std::string d = argv0 ? argv0 : "";
+  const size_t slash = d.find_last_of('/');
+  d = slash == std::string::npos ? std::string(".") : d.substr(0, slash);
+  return d + "/../weights/unet_warmstart.bin";
+}
+
 int main(int argc, char* argv[]) {
   if (argc != 2) {  // fluid3D.cpp:303-307
     std::cout << " Usage: " << argv[0] << " *.cfg" << std::endl;
@@ -151,7 +162,10 @@ int main(int argc, char* argv[]) {
   p.mic_tau = cfg.num("mic tau", 0.97);
   p.mic_sigma = cfg.num("mic sigma", 0.25);
   p.damping_w = cfg.num("damping", 0.9);
-  if (cfg.str("warm start", "zero") == "previous") p.warm_start = PLUME_WARM_PREVIOUS;
+  const std::string warm = cfg.str("warm start", "zero");
+  if (warm == "previous") p.warm_start = PLUME_WARM_PREVIOUS;
+  if (warm == "learned") p.warm_start = PLUME_WARM_LEARNED;
+  const std::string net_path = cfg.str("warm start network", default_network_path(argv[0]));
   p.device = cfg.integer("device", 0);
   const bool write_state = cfg.integer("write state", 1) != 0;
   const bool write_streams = cfg.integer("write streams", 1) != 0;
@@ -167,6 +181,17 @@ int main(int argc, char* argv[]) {
 
   plume_handle* h = nullptr;
   if (check(plume_create(&p, &h), nullptr, "plume_create") != PLUME_OK) return 1;
+  plume_net* net = nullptr;
+  if (p.warm_start == PLUME_WARM_LEARNED) {
+    if (check(plume_net_create(0, p.device, &net), nullptr, "plume_net_create") != PLUME_OK ||
+        check(plume_net_load(net, net_path.c_str()), nullptr, "plume_net_load") != PLUME_OK ||
+        check(plume_attach_net(h, net), nullptr, "plume_attach_net") != PLUME_OK) {
+      plume_destroy(h);
+      plume_net_destroy(net);
+      return 1;
+    }
+    std::cout << " Using learned warm start: " << net_path << std::endl;
+  }
   int rc = PLUME_OK;
   for (int step = 0; step < snapshots && rc == PLUME_OK; step++) {  // fluid3D.cpp:357-398
     std::cout << " Simulation step " << 1 + step << " of " << snapshots << std::endl;
@@ -185,5 +210,6 @@ int main(int argc, char* argv[]) {
     if (rc == PLUME_OK && write_streams) rc = check(plume_append_streams(h, snapshot_path.c_str()), h, "append_streams");
   }
   plume_destroy(h);
+  plume_net_destroy(net);  // after the handle that used it
   return rc == PLUME_OK ? 0 : 1;
 }

@@ -63,3 +63,23 @@ def test_cli_run_matches_oracle(exe, tmp_path):
         assert err < 1e-9, (name, err)
     dims = np.fromfile(snap + "velocity.final.matrix.dims", dtype="<i4")
     assert tuple(dims) == (2, 3 * 10 * 12 * 8)
+
+
+@pytest.mark.gpu
+def test_cli_learned_warm_start(exe, tmp_path):
+    """`warm start = learned` loads the committed network next to the binary
+    and every solve still meets the configured stop test."""
+    snap = str(tmp_path) + "/snaps/"
+    cfg = tmp_path / "learned.cfg"
+    cfg.write_text("xres = 32\nyres = 48\nzres = 32\nvorticity = 2\nbuoyancy = 1\nprecision = fp32\n"
+                   "solver criterion = rel2\nsolver tolerance = 1e-6\nsource = box\nsource noise = 0.05\n"
+                   "source box = 11 1 11 19 4 19\ntop = 1\nbottom = 1\n"
+                   "warm start = learned\nsnapshot path = %s\nsimulation snapshots = 3\n"
+                   "write streams = 0\n" % snap)
+    r = subprocess.run([exe, str(cfg)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "Using learned warm start" in r.stdout
+    rel = [float(line.split("relative two norm:")[1].split()[0])
+           for line in r.stdout.splitlines() if "relative two norm:" in line]
+    assert len(rel) == 3 and all(v <= 1e-6 for v in rel)
+    assert os.path.exists(snap + "fluid.0002.fluid3d.gz")
