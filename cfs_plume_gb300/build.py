@@ -80,8 +80,8 @@ def build(verbose=False, ptxas_info=False):
         ("engine_f32.cu", [nvcc] + common_nv),
         ("noalloc.cu", [nvcc] + common_nv + ["-fmad=false"]),
         ("unet.cu", [nvcc] + common_nv),
-        ("plume_api.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-I" + os.path.join(cuda, "include")]),
-        ("snapshot.cpp", ["g++", "-O2", "-std=c++17", "-fPIC"] + zc),
+        ("plume_api.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-I" + os.path.join(cuda, "include")]),
+        ("snapshot.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread"] + zc),
         ("batch.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread"]),
     ]
     jobs = []

@@ -202,13 +202,12 @@ int main(int argc, char* argv[]) {
     std::cout << "   " << st.iterations << " iterations converged to inf norm: " << st.max_residual
               << " relative two norm: " << st.rel_residual << "  (" << st.ms_total << " ms)"
               << std::endl;
-    if (write_state) {
-      char buffer[1024];
-      snprintf(buffer, sizeof(buffer), "%sfluid.%04i.fluid3d", snapshot_path.c_str(), step);
-      rc = check(plume_write_state(h, buffer), h, "write_state");
-    }
-    if (rc == PLUME_OK && write_streams) rc = check(plume_append_streams(h, snapshot_path.c_str()), h, "append_streams");
+    // writeGz + appendStreams (fluid3D.cpp:376-386) on the handle's writer
+    // thread, overlapping the next steps
+    const int what = (write_state ? 1 : 0) | (write_streams ? 2 : 0);
+    if (what) rc = check(plume_snapshot_async(h, snapshot_path.c_str(), step, what), h, "snapshot");
   }
+  if (rc == PLUME_OK) rc = check(plume_wait_snapshots(h), h, "snapshot");
   plume_destroy(h);
   plume_net_destroy(net);  // after the handle that used it
   return rc == PLUME_OK ? 0 : 1;

@@ -2,8 +2,14 @@
 //
 // Thin layer: argument checks, status codes, and the host-side file output.
 // All field arithmetic happens in the CUDA engines; there is no CPU path.
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <functional>
+#include <memory>
+#include <mutex>
 #include <new>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -12,9 +18,90 @@
 #include "engine.h"
 #include "snapshot.h"
 
+// Background writer of one handle: snapshot jobs run in call order on one
+// thread, at most two in flight (queued or running); the first error is
+// kept until it is reported.  Field buffers are recycled between jobs.
+class SnapshotWriter {
+ public:
+  using FieldSet = std::vector<std::vector<double>>;
+  SnapshotWriter() : th_([this] { run(); }) {}
+  ~SnapshotWriter() {
+    {
+      std::lock_guard<std::mutex> l(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    th_.join();  // pending jobs finish first
+  }
+  std::shared_ptr<FieldSet> field_set() {
+    std::lock_guard<std::mutex> l(mu_);
+    if (!spare_.empty()) {
+      auto f = spare_.back();
+      spare_.pop_back();
+      return f;
+    }
+    return std::make_shared<FieldSet>(PLUME_F_COUNT);
+  }
+  void recycle(std::shared_ptr<FieldSet> f) {
+    std::lock_guard<std::mutex> l(mu_);
+    if (spare_.size() < 2) spare_.push_back(std::move(f));
+  }
+  void push(std::function<int(std::string&)> job) {
+    std::unique_lock<std::mutex> l(mu_);
+    cv_.wait(l, [&] { return inflight_ < 2; });
+    ++inflight_;
+    q_.push_back(std::move(job));
+    cv_.notify_all();
+  }
+  int take_error(std::string& e, bool wait_all) {
+    std::unique_lock<std::mutex> l(mu_);
+    if (wait_all) cv_.wait(l, [&] { return inflight_ == 0; });
+    const int r = rc_;
+    e = err_;
+    rc_ = PLUME_OK;
+    err_.clear();
+    return r;
+  }
+
+ private:
+  void run() {
+    for (;;) {
+      std::function<int(std::string&)> job;
+      {
+        std::unique_lock<std::mutex> l(mu_);
+        cv_.wait(l, [&] { return stop_ || !q_.empty(); });
+        if (q_.empty()) return;
+        job = std::move(q_.front());
+        q_.pop_front();
+      }
+      std::string e;
+      const int r = job(e);
+      {
+        std::lock_guard<std::mutex> l(mu_);
+        if (r != PLUME_OK && rc_ == PLUME_OK) {
+          rc_ = r;
+          err_ = e;
+        }
+        --inflight_;
+      }
+      cv_.notify_all();
+    }
+  }
+  std::mutex mu_;
+  std::condition_variable cv_;
+  std::deque<std::function<int(std::string&)>> q_;
+  std::vector<std::shared_ptr<FieldSet>> spare_;
+  int inflight_ = 0;
+  bool stop_ = false;
+  int rc_ = PLUME_OK;
+  std::string err_;
+  std::thread th_;  // last: started after every other member exists
+};
+
 struct plume_handle {
   plume::Engine* eng = nullptr;
   std::string err;
+  std::unique_ptr<SnapshotWriter> writer;
 };
 
 namespace plume {
@@ -95,6 +182,7 @@ int plume_create(const plume_params* p, plume_handle** out) {
 
 void plume_destroy(plume_handle* h) {
   if (!h) return;
+  h->writer.reset();  // waits for pending snapshots
   delete h->eng;
   delete h;
 }
@@ -235,7 +323,69 @@ int plume_mic_diagonal(plume_handle* h, double* precon) {
 
 int plume_sync(plume_handle* h) {
   if (!h) return PLUME_ERR_INVALID;
-  return from_engine(h, h->eng->sync());
+  const int rc = from_engine(h, h->eng->sync());
+  if (rc != PLUME_OK) return rc;
+  return plume_wait_snapshots(h);
+}
+
+int plume_wait_snapshots(plume_handle* h) {
+  if (!h) return PLUME_ERR_INVALID;
+  if (!h->writer) return PLUME_OK;
+  std::string e;
+  const int rc = h->writer->take_error(e, true);
+  return rc == PLUME_OK ? PLUME_OK : set_err(h, rc, e);
+}
+
+int plume_snapshot_async(plume_handle* h, const char* dir, int32_t step, int32_t what) {
+  if (!h) return PLUME_ERR_INVALID;
+  if (!dir || step < 0 || (what & 3) == 0 || (what & ~3) != 0)
+    return set_err(h, PLUME_ERR_INVALID, "need a directory, step >= 0 and what in 1..3");
+  const plume_params& p = h->eng->params();
+  if (!p.cache_fields) return set_err(h, PLUME_ERR_STATE, "snapshots need cache_fields = 1");
+  if (!h->writer) h->writer.reset(new (std::nothrow) SnapshotWriter());
+  if (!h->writer) return set_err(h, PLUME_ERR_OOM, "writer thread");
+  {
+    std::string e;
+    const int rc = h->writer->take_error(e, false);  // an earlier snapshot's failure
+    if (rc != PLUME_OK) return set_err(h, rc, e);
+  }
+  // copy every field the writers read while the step loop waits; the rest
+  // happens on the writer thread
+  const size_t N = (size_t)p.res[0] * p.res[1] * p.res[2];
+  std::shared_ptr<SnapshotWriter::FieldSet> fs = h->writer->field_set();
+  const plume::FieldFetch live = make_fetch(h);
+  for (int f = 0; f < PLUME_F_COUNT; f++) {
+    const int rc = live(f, (*fs)[f]);
+    if (rc != PLUME_OK) return from_engine(h, rc);
+  }
+  auto ob = std::make_shared<std::vector<uint8_t>>(N);
+  int rc = h->eng->download_obstacles(ob->data(), ob->size());
+  if (rc != PLUME_OK) return from_engine(h, rc);
+  plume::StateHeader hd;
+  for (int k = 0; k < 3; k++) hd.res[k] = p.res[k];
+  hd.total_steps = h->eng->total_steps();
+  hd.dx = h->eng->dx();
+  hd.total_time = h->eng->total_time();
+  hd.dt = p.dt;
+  hd.buoyancy = p.buoyancy;
+  hd.vorticity_eps = p.vorticity_eps;
+  char name[64];
+  snprintf(name, sizeof(name), "fluid.%04i.fluid3d", step);
+  const std::string d = dir, state_path = d + name;
+  int res[3] = {p.res[0], p.res[1], p.res[2]};
+  SnapshotWriter* w = h->writer.get();
+  h->writer->push([=](std::string& e) {
+    const plume::FieldFetch held = [fs](int f, std::vector<double>& buf) {
+      buf = (*fs)[f];
+      return PLUME_OK;
+    };
+    int r = PLUME_OK;
+    if (what & 1) r = plume::write_state_gz(state_path, hd, held, *ob, e);
+    if (r == PLUME_OK && (what & 2)) r = plume::append_streams(d, res, held, e);
+    w->recycle(fs);
+    return r;
+  });
+  return PLUME_OK;
 }
 
 int plume_profile_sweeps(plume_handle* h, int on) {

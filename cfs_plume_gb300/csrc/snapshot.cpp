@@ -1,9 +1,13 @@
 // snapshot.cpp -- reference-format state files and SVD streams (host C++).
 #include "snapshot.h"
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <thread>
 
 #include "../../include/plume.h"
 
@@ -15,33 +19,42 @@ namespace plume {
 
 namespace {
 
-// gzip output.  With zlib: gzopen(path, "wb1") exactly as the reference.
-// Without zlib headers at build time: a gzip member of stored (uncompressed)
-// deflate blocks, which zlib's gzread reads like any other member.
+// gzip output.  With zlib: the byte stream is cut into 16 MB pieces, each
+// deflated at level 1 (the reference's "wb1") into a complete gzip member by a
+// pool of host threads, and the members are written in order; concatenated
+// members are one valid gzip file, which zlib's gzread (the reference's
+// readGz) reads straight through.  Without zlib headers at build time: one
+// gzip member of stored (uncompressed) deflate blocks.
 class GzOut {
  public:
   bool open(const std::string& path) {
-#if defined(PLUME_HAVE_ZLIB)
-    f_ = gzopen(path.c_str(), "wb1");
-    return f_ != nullptr;
-#else
     f_ = fopen(path.c_str(), "wb");
     if (!f_) return false;
+#if defined(PLUME_HAVE_ZLIB)
+    pieces_.clear();
+    pieces_.emplace_back();
+    pieces_.back().reserve(kPiece);
+#else
     static const unsigned char hdr[10] = {0x1f, 0x8b, 8, 0, 0, 0, 0, 0, 0, 3};
     fwrite(hdr, 1, 10, f_);
     crc_ = 0xffffffffu;
     size_ = 0;
-    return true;
 #endif
+    return true;
   }
   bool write(const void* data, size_t n) {
     const unsigned char* p = (const unsigned char*)data;
 #if defined(PLUME_HAVE_ZLIB)
     while (n > 0) {
-      const unsigned chunk = n > (1u << 30) ? (1u << 30) : (unsigned)n;
-      if (gzwrite(f_, p, chunk) != (int)chunk) return false;
-      p += chunk;
-      n -= chunk;
+      std::vector<unsigned char>& cur = pieces_.back();
+      const size_t take = std::min(n, kPiece - cur.size());
+      cur.insert(cur.end(), p, p + take);
+      p += take;
+      n -= take;
+      if (cur.size() == kPiece) {
+        pieces_.emplace_back();
+        pieces_.back().reserve(kPiece);
+      }
     }
     return true;
 #else
@@ -61,7 +74,32 @@ class GzOut {
   }
   bool close() {
 #if defined(PLUME_HAVE_ZLIB)
-    return gzclose(f_) == Z_OK;
+    if (pieces_.back().empty() && pieces_.size() > 1) pieces_.pop_back();
+    const size_t np = pieces_.size();
+    std::vector<std::vector<unsigned char>> out(np);
+    std::atomic<size_t> next(0);
+    std::atomic<bool> ok(true);
+    auto work = [&]() {
+      for (size_t k = next++; k < np; k = next++) {
+        if (!deflate_member(pieces_[k], out[k])) ok = false;
+        std::vector<unsigned char>().swap(pieces_[k]);  // release the raw piece early
+      }
+    };
+    unsigned hw = std::thread::hardware_concurrency();
+    if (const char* env = getenv("PLUME_GZ_THREADS")) {  // deflate threads (default: all cores, <= 32)
+      const int t = atoi(env);
+      if (t >= 1) hw = (unsigned)t;
+    }
+    const size_t nt = std::min<size_t>(np, std::max(1u, std::min(hw, 32u)));
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < nt; t++) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    bool wrote = ok.load();
+    for (size_t k = 0; k < np && wrote; k++)
+      wrote = fwrite(out[k].data(), 1, out[k].size(), f_) == out[k].size();
+    pieces_.clear();
+    return (fclose(f_) == 0) && wrote;
 #else
     const unsigned char last[5] = {1, 0, 0, 0xff, 0xff};  // final empty stored block
     fwrite(last, 1, 5, f_);
@@ -75,8 +113,26 @@ class GzOut {
   }
 
  private:
+  FILE* f_ = nullptr;
 #if defined(PLUME_HAVE_ZLIB)
-  gzFile f_ = nullptr;
+  static constexpr size_t kPiece = (size_t)16 << 20;
+  std::vector<std::vector<unsigned char>> pieces_;
+
+  // one complete gzip member (header, level-1 deflate stream, CRC-32, size)
+  static bool deflate_member(const std::vector<unsigned char>& in, std::vector<unsigned char>& out) {
+    z_stream z;
+    memset(&z, 0, sizeof(z));
+    if (deflateInit2(&z, 1, Z_DEFLATED, 15 + 16, 8, Z_DEFAULT_STRATEGY) != Z_OK) return false;
+    out.resize(deflateBound(&z, (uLong)in.size()) + 64);
+    z.next_in = const_cast<Bytef*>(in.data());
+    z.avail_in = (uInt)in.size();
+    z.next_out = out.data();
+    z.avail_out = (uInt)out.size();
+    const int rc = deflate(&z, Z_FINISH);
+    out.resize(z.total_out);
+    deflateEnd(&z);
+    return rc == Z_STREAM_END;
+  }
 #else
   void update_crc(const unsigned char* p, size_t n) {
     static uint32_t table[256];
@@ -93,7 +149,6 @@ class GzOut {
     for (size_t i = 0; i < n; i++) c = table[(c ^ p[i]) & 0xff] ^ (c >> 8);
     crc_ = c;
   }
-  FILE* f_ = nullptr;
   uint32_t crc_ = 0;
   uint64_t size_ = 0;
 #endif

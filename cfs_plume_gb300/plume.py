@@ -61,6 +61,8 @@ def load_library(path=LIB_PATH):
         "plume_mic_diagonal": (C.c_int, [H, C.c_void_p]),
         "plume_sync": (C.c_int, [H]),
         "plume_profile_sweeps": (C.c_int, [H, C.c_int]),
+        "plume_snapshot_async": (C.c_int, [H, C.c_char_p, C.c_int32, C.c_int32]),
+        "plume_wait_snapshots": (C.c_int, [H]),
         "plume_sweep_times": (C.c_int, [H, P(C.c_double), P(C.c_int64)]),
     }
     for name, (res, args) in sig.items():
@@ -162,6 +164,15 @@ class Plume:
     def append_streams(self, directory):
         d = directory if directory.endswith("/") else directory + "/"
         _check(self.lib.plume_append_streams(self.h, os.fsencode(d)), self.h)
+
+    def snapshot_async(self, directory, step, state=True, streams=True):
+        """State file and/or stream rows written by the handle's writer thread."""
+        d = directory if directory.endswith("/") else directory + "/"
+        what = (1 if state else 0) | (2 if streams else 0)
+        _check(self.lib.plume_snapshot_async(self.h, os.fsencode(d), step, what), self.h)
+
+    def wait_snapshots(self):
+        _check(self.lib.plume_wait_snapshots(self.h), self.h)
 
     def solve_poisson(self, b, x0=None):
         b = np.ascontiguousarray(b, dtype=np.float64)

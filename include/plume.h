@@ -198,6 +198,19 @@ int plume_write_state(plume_handle* h, const char* path);
    and <dir>pressure.matrix.transpose, and rewrite the six .dims files. */
 int plume_append_streams(plume_handle* h, const char* dir);
 
+/* Asynchronous snapshot (no counterpart in the reference, whose writeGz and
+   appendStreams block the step loop): the fields are copied to host memory
+   before the call returns; deflating (in parallel, gzip level 1) and the file
+   writes run on the handle's writer thread, in call order.  what: bit 0 = the
+   state file "<dir>fluid.%04i.fluid3d.gz" of `step` (as plume_write_state),
+   bit 1 = the stream rows under `dir` (as plume_append_streams).  At most two
+   snapshots are in flight; a third call waits for the oldest.  A write error
+   is returned by the next plume_snapshot_async, plume_wait_snapshots or
+   plume_sync; plume_destroy waits for pending writes. */
+int plume_snapshot_async(plume_handle* h, const char* dir, int32_t step, int32_t what);
+/* Wait until every snapshot of the handle is on disk. */
+int plume_wait_snapshots(plume_handle* h);
+
 /* Human-readable text of a status code. */
 const char* plume_strerror(int status);
 
