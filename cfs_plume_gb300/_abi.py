@@ -24,9 +24,11 @@ FIELDS = [
     "cachedPressure", "cachedDivergence", "prevorticity",
 ]
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
+# PLUME_F_POST_IOP: only assigned by a moving-box step (include/plume_box.h)
+FIELD_ID["postIOP"] = len(FIELDS)
 VECTOR_FIELDS = {"velocity", "velocityOld", "force", "vorticity", "preprojection",
                  "prediffusion", "preadvection", "cachedQuadratic", "postadvection",
-                 "prevorticity"}
+                 "prevorticity", "postIOP"}
 
 # (double)0.1f: the reference stores `_buoyancy = 0.1f` in a double (FLUID_3D_MIC.cpp:36)
 BUOYANCY_REF = struct.unpack("f", struct.pack("f", 0.1))[0]
@@ -124,3 +126,18 @@ def plume_config(res, precision=PREC_FP32, criterion=CRIT_REL2, tol=1e-6, seed=0
                 precision=precision, criterion=criterion, tol=tol)
     args.update(kw)
     return default_params(**args)
+
+
+class PlumeBox(C.Structure):
+    """plume_box (include/plume_box.h): the state of the reference's BOX."""
+    _fields_ = [
+        ("center", C.c_double * 3),
+        ("original_center", C.c_double * 3),
+        ("lengths", C.c_double * 3),
+        ("rotation", C.c_double * 9),
+        ("theta", C.c_double),
+        ("phi", C.c_double),
+        ("period", C.c_double),
+        ("translation_period", C.c_double),
+        ("dt", C.c_double),
+    ]

@@ -83,6 +83,8 @@ def build(verbose=False, ptxas_info=False):
         ("plume_api.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-I" + os.path.join(cuda, "include")]),
         ("snapshot.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread"] + zc),
         ("batch.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread"]),
+        # the box state must round after every operation on Arm hosts too
+        ("box.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]),
     ]
     jobs = []
     with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:

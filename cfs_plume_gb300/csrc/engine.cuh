@@ -6,6 +6,7 @@
 // keeps for the reduced solvers are produced as extra kernel outputs or by
 // pointer rotation instead of separate full-array copies.
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -341,7 +342,57 @@ class EngineT : public Engine {
   }
 
   // ------------------------------------------------------------------ step
-  int step(plume_step_stats* stats) override {
+  int step(plume_step_stats* stats) override { return step_impl(nullptr, stats); }
+
+  // FLUID_3D_MIC::stepWithMovingObstacle (FLUID_3D_MIC.cpp:236-310): the
+  // step without buoyancy, with the obstacle stomp between damping and
+  // projection.
+  int step_moving_box(const plume_box& box, plume_step_stats* stats) override {
+    BoxDev b;
+    if (!box_dev(box, b)) return fail(PLUME_ERR_INVALID, "box with non-finite or zero parameters");
+    if (!iop_in_) {
+      const size_t N = (size_t)g_.N;
+      PL_TRY(cudaMalloc(&iop_in_, N));
+      PL_TRY(cudaMemsetAsync(iop_in_, 0, N, s_));  // border cells stay 0
+      PL_TRY(cudaMalloc(&iop_val_, 3 * N * sizeof(double)));
+      if (p_.cache_fields) {
+        PL_TRY(cudaMalloc(&iop_post_pool_, 3 * N * sizeof(T)));
+        PL_TRY(cudaMemsetAsync(iop_post_pool_, 0, 3 * N * sizeof(T), s_));
+        post_iop_ = V3<T>{iop_post_pool_, iop_post_pool_ + N, iop_post_pool_ + 2 * N};
+      }
+    }
+    return step_impl(&b, stats);
+  }
+
+  // FLUID_3D_MIC::setInitialVelocity(BOX*) (FLUID_3D_MIC.cpp:744-764)
+  int set_initial_velocity_box(const plume_box& box) override {
+    BoxDev b;
+    if (!box_dev(box, b)) return fail(PLUME_ERR_INVALID, "box with non-finite or zero parameters");
+    launches_ = 0;
+    k_box_stomp<T><<<grid_for(g_.N), 256, 0, s_>>>(g_, b, vel_, vel_, 0, nullptr, nullptr, 1);
+    PL_CHECK_LAUNCH();
+    PL_TRY(cudaStreamSynchronize(s_));
+    return PLUME_OK;
+  }
+
+  bool has_iop() const override { return has_iop_; }
+
+  int download_iop(uint8_t* inside, double* values, size_t n) override {
+    const size_t N = (size_t)g_.N;
+    if (n != N) return fail(PLUME_ERR_INVALID, "the obstacle matrix needs N cells");
+    if (!has_iop_) return fail(PLUME_ERR_STATE, "no moving-box step has run");
+    std::vector<uint8_t> in(N);
+    PL_TRY(cudaMemcpyAsync(in.data(), iop_in_, N, cudaMemcpyDeviceToHost, s_));
+    if (values) PL_TRY(cudaMemcpyAsync(values, iop_val_, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, s_));
+    PL_TRY(cudaStreamSynchronize(s_));
+    if (values)  // only inside cells are written on the device
+      for (size_t c = 0; c < N; c++)
+        if (!in[c]) values[3 * c] = values[3 * c + 1] = values[3 * c + 2] = 0.0;
+    if (inside) memcpy(inside, in.data(), N);
+    return PLUME_OK;
+  }
+
+  int step_impl(const BoxDev* box, plume_step_stats* stats) {
     const int cache = p_.cache_fields ? 1 : 0;
     const int gN = grid_for(g_.N);
     const int gI = grid_for(g_.nint);
@@ -350,7 +401,9 @@ class EngineT : public Engine {
     launches_ = 0;
     PL_TRY(cudaEventRecord(ev_[0], s_));
     // forces: walls, buoyancy, prevorticity (FLUID_3D_MIC.cpp:188-199)
-    k_forces<T><<<gN, 256, 0, s_>>>(g_, vel_, dens_, heat_, prevort_, c_, cache);
+    StepConsts<T> cf = c_;
+    if (box) cf.has_beta = 0;  // the moving step adds no buoyancy (lines 247-254)
+    k_forces<T><<<gN, 256, 0, s_>>>(g_, vel_, dens_, heat_, prevort_, cf, cache);
     PL_CHECK_LAUNCH();
     if (c_.has_vort) {  // addVorticity returns early when eps <= 0 (line 527)
       k_vort1<T><<<gN, 256, 0, s_>>>(g_, vel_, vort_, mag_, c_);
@@ -372,6 +425,13 @@ class EngineT : public Engine {
     k_damping<T><<<gN, 256, 0, s_>>>(g_, c_, vel_, spare_, preproj_, cache);
     PL_CHECK_LAUNCH();
     std::swap(vel_, spare_);
+    if (box) {
+      // the IOP stomp u <- N [u; 1], cached as postIOP (lines 276-284)
+      k_box_stomp<T><<<gN, 256, 0, s_>>>(g_, *box, vel_, post_iop_, post_iop_.x ? 1 : 0, iop_in_,
+                                         iop_val_, 0);
+      PL_CHECK_LAUNCH();
+      has_iop_ = true;
+    }
     // project (lines 314-399)
     k_face_bc<T><<<gF, 256, 0, s_>>>(g_, vel_, ox ? 2 : 0, oy ? 2 : 0, oz ? 2 : 0);
     PL_CHECK_LAUNCH();
@@ -453,6 +513,10 @@ class EngineT : public Engine {
                          field == PLUME_F_FORCE);
     if (cached && !p_.cache_fields)
       return fail(PLUME_ERR_STATE, "field is not kept when cache_fields = 0");
+    if (field == PLUME_F_POST_IOP && !p_.cache_fields)
+      return fail(PLUME_ERR_STATE, "postIOP is not kept when cache_fields = 0");
+    if (field == PLUME_F_POST_IOP && !has_iop_)
+      return fail(PLUME_ERR_STATE, "postIOP: no moving-box step has run");
     const T* s = scalar_ptr(field);
     if (s) {
       if (n != N) return fail(PLUME_ERR_INVALID, "scalar field needs N doubles");
@@ -973,6 +1037,42 @@ class EngineT : public Engine {
     return PLUME_OK;
   }
 
+  // The per-step constants of the stomp (box.cpp) and a cell range that
+  // certainly contains every inside cell: the circumscribed sphere of the box,
+  // widened by two cells, when R is a rotation; the whole interior otherwise.
+  bool box_dev(const plume_box& box, BoxDev& b) const {
+    if (!box_finite(box)) return false;
+    box_constants(box, b.half, b.omega, b.disp);
+    const int res[3] = {g_.X, g_.Y, g_.Z};
+    for (int k = 0; k < 3; k++) {
+      b.center[k] = box.center[k];
+      b.axis[k] = k == 2 ? 1.0 : 0.0;
+      b.d[k] = 1.0 / res[k];
+      b.lo[k] = 1;
+      b.hi[k] = res[k] - 1;
+    }
+    for (int k = 0; k < 9; k++) b.R[k] = box.rotation[k];
+    double dev = 0;  // max |R^T R - I|
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        double s = 0;
+        for (int k = 0; k < 3; k++) s += b.R[3 * k + i] * b.R[3 * k + j];
+        dev = std::max(dev, std::fabs(s - (i == j ? 1.0 : 0.0)));
+      }
+    if (dev <= 1e-9) {
+      const double rho = std::sqrt(b.half[0] * b.half[0] + b.half[1] * b.half[1] + b.half[2] * b.half[2]) *
+                         (1.0 + 1e-6);
+      for (int k = 0; k < 3; k++) {
+        const double n = res[k];
+        const double lo = std::floor((b.center[k] - rho) * n - 0.5) - 2.0;
+        const double hi = std::ceil((b.center[k] + rho) * n - 0.5) + 3.0;
+        b.lo[k] = (int)std::max(1.0, std::min(n - 1.0, lo));
+        b.hi[k] = (int)std::max(1.0, std::min(n - 1.0, hi));
+      }
+    }
+    return true;
+  }
+
   const T* scalar_ptr(int field) const {
     switch (field) {
       case PLUME_F_DENSITY: return dens_;
@@ -997,6 +1097,7 @@ class EngineT : public Engine {
       case PLUME_F_PREADVECTION: v = vel_old_; return true;  // same data after the swap (line 617)
       case PLUME_F_POSTADVECTION: v = postadv_; return true;
       case PLUME_F_PREVORTICITY: v = prevort_; return true;
+      case PLUME_F_POST_IOP: v = post_iop_; return post_iop_.x != nullptr;
       default: return false;
     }
   }
@@ -1059,6 +1160,12 @@ class EngineT : public Engine {
     net_ws_ = nullptr;
     if (pool_) cudaFree(pool_);
     if (spool_) cudaFree(spool_);
+    if (iop_in_) cudaFree(iop_in_);
+    if (iop_val_) cudaFree(iop_val_);
+    if (iop_post_pool_) cudaFree(iop_post_pool_);
+    iop_in_ = nullptr;
+    iop_val_ = nullptr;
+    iop_post_pool_ = nullptr;
     if (col_cells_) cudaFree(col_cells_);
     if (src_dev_) cudaFree(src_dev_);
     if (src_host_) cudaFreeHost(src_host_);
@@ -1088,6 +1195,13 @@ class EngineT : public Engine {
   T *r_ = nullptr, *d_ = nullptr, *q_ad_ = nullptr, *z_ = nullptr, *qf_ = nullptr, *P_ = nullptr;
   V3<T> vel_{}, vel_old_{}, spare_{}, prevort_{}, postadv_{}, preproj_{}, force_{}, vort_{};
   double* P64_ = nullptr;
+  // moving box: inside mask (N), last-column values (3N doubles) and postIOP,
+  // allocated at the first moving step
+  uint8_t* iop_in_ = nullptr;
+  double* iop_val_ = nullptr;
+  T* iop_post_pool_ = nullptr;
+  V3<T> post_iop_{};
+  bool has_iop_ = false;
   // skewed solver vectors and wavefront configuration
   Skew k_{};
   char* spool_ = nullptr;

@@ -10,6 +10,7 @@
 #include <string>
 
 #include "../../include/plume.h"
+#include "../../include/plume_box.h"
 
 namespace plume {
 
@@ -26,6 +27,13 @@ class Engine {
   // Enqueue one step; if stats != nullptr, wait for it and fill stats.
   virtual int step(plume_step_stats* stats) = 0;
   virtual int run(int32_t first_step, int32_t n, plume_step_stats* stats) = 0;
+  // Moving box obstacle (include/plume_box.h): one stepWithMovingObstacle,
+  // setInitialVelocity(BOX*), and the obstacle matrix of the last moving step
+  // (inside mask and last-column values, full-grid layout).
+  virtual int step_moving_box(const plume_box& box, plume_step_stats* stats) = 0;
+  virtual int set_initial_velocity_box(const plume_box& box) = 0;
+  virtual bool has_iop() const = 0;
+  virtual int download_iop(uint8_t* inside, double* values, size_t n) = 0;
   virtual int download(int field, double* dst, size_t n) = 0;
   virtual int upload(int field, const double* src, size_t n) = 0;
   virtual int download_obstacles(uint8_t* dst, size_t n) = 0;
@@ -55,6 +63,11 @@ class Engine {
   virtual const plume_params& params() const = 0;
   virtual std::string& last_error() = 0;
 };
+
+// box.cpp: half lengths, angular and displacement velocity of a box for the
+// current step; false if a parameter is non-finite or a period is zero.
+void box_constants(const plume_box& b, double half[3], double omega[3], double disp[3]);
+bool box_finite(const plume_box& b);
 
 Engine* make_engine_f64();
 Engine* make_engine_f32();

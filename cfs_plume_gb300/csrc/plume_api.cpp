@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/plume.h"
+#include "../../include/plume_box.h"
 #include "../../include/plume_solver.h"
 #include "engine.h"
 #include "snapshot.h"
@@ -244,6 +245,18 @@ int plume_get_info(plume_handle* h, int32_t res[3], int32_t* total_steps, double
   return PLUME_OK;
 }
 
+// The obstacle matrix of the last moving step, empty before the first one.
+static int fetch_iop(plume_handle* h, plume::IopRecord& iop) {
+  iop.inside.clear();
+  iop.values.clear();
+  if (!h->eng->has_iop()) return PLUME_OK;
+  const plume_params& p = h->eng->params();
+  const size_t N = (size_t)p.res[0] * p.res[1] * p.res[2];
+  iop.inside.resize(N);
+  iop.values.resize(3 * N);
+  return h->eng->download_iop(iop.inside.data(), iop.values.data(), N);
+}
+
 static plume::FieldFetch make_fetch(plume_handle* h) {
   return [h](int field, std::vector<double>& buf) {
     const plume_params& p = h->eng->params();
@@ -252,7 +265,12 @@ static plume::FieldFetch make_fetch(plume_handle* h) {
                      field == PLUME_F_FORCE || field == PLUME_F_VORTICITY ||
                      field == PLUME_F_PREPROJECTION || field == PLUME_F_PREDIFFUSION ||
                      field == PLUME_F_PREADVECTION || field == PLUME_F_CACHED_QUADRATIC ||
-                     field == PLUME_F_POSTADVECTION || field == PLUME_F_PREVORTICITY;
+                     field == PLUME_F_POSTADVECTION || field == PLUME_F_PREVORTICITY ||
+                     field == PLUME_F_POST_IOP;
+    if (field == PLUME_F_POST_IOP && !h->eng->has_iop()) {
+      buf.clear();  // never assigned: written as an empty field
+      return (int)PLUME_OK;
+    }
     buf.resize(vec ? 3 * N : N);
     return h->eng->download(field, buf.data(), buf.size());
   };
@@ -274,7 +292,10 @@ int plume_write_state(plume_handle* h, const char* path) {
   std::vector<uint8_t> ob((size_t)p.res[0] * p.res[1] * p.res[2]);
   int rc = h->eng->download_obstacles(ob.data(), ob.size());
   if (rc != PLUME_OK) return from_engine(h, rc);
-  return plume::write_state_gz(path, hd, make_fetch(h), ob, h->err);
+  plume::IopRecord iop;
+  rc = fetch_iop(h, iop);
+  if (rc != PLUME_OK) return from_engine(h, rc);
+  return plume::write_state_gz(path, hd, make_fetch(h), ob, iop, h->err);
 }
 
 int plume_append_streams(plume_handle* h, const char* dir) {
@@ -282,7 +303,10 @@ int plume_append_streams(plume_handle* h, const char* dir) {
   if (!dir) return set_err(h, PLUME_ERR_INVALID, "null directory");
   const plume_params& p = h->eng->params();
   if (!p.cache_fields) return set_err(h, PLUME_ERR_STATE, "streams need cache_fields = 1");
-  return plume::append_streams(dir, p.res, make_fetch(h), h->err);
+  plume::IopRecord iop;
+  const int rc = fetch_iop(h, iop);
+  if (rc != PLUME_OK) return from_engine(h, rc);
+  return plume::append_streams(dir, p.res, make_fetch(h), iop, h->err);
 }
 
 const char* plume_strerror(int status) {
@@ -361,6 +385,9 @@ int plume_snapshot_async(plume_handle* h, const char* dir, int32_t step, int32_t
   auto ob = std::make_shared<std::vector<uint8_t>>(N);
   int rc = h->eng->download_obstacles(ob->data(), ob->size());
   if (rc != PLUME_OK) return from_engine(h, rc);
+  auto iop = std::make_shared<plume::IopRecord>();
+  rc = fetch_iop(h, *iop);
+  if (rc != PLUME_OK) return from_engine(h, rc);
   plume::StateHeader hd;
   for (int k = 0; k < 3; k++) hd.res[k] = p.res[k];
   hd.total_steps = h->eng->total_steps();
@@ -380,12 +407,30 @@ int plume_snapshot_async(plume_handle* h, const char* dir, int32_t step, int32_t
       return PLUME_OK;
     };
     int r = PLUME_OK;
-    if (what & 1) r = plume::write_state_gz(state_path, hd, held, *ob, e);
-    if (r == PLUME_OK && (what & 2)) r = plume::append_streams(d, res, held, e);
+    if (what & 1) r = plume::write_state_gz(state_path, hd, held, *ob, *iop, e);
+    if (r == PLUME_OK && (what & 2)) r = plume::append_streams(d, res, held, *iop, e);
     w->recycle(fs);
     return r;
   });
   return PLUME_OK;
+}
+
+// ---- moving box obstacle (include/plume_box.h) ----
+int plume_step_moving_box(plume_handle* h, const plume_box* box, plume_step_stats* stats) {
+  if (!h) return PLUME_ERR_INVALID;
+  if (!box) return set_err(h, PLUME_ERR_INVALID, "null box");
+  return from_engine(h, h->eng->step_moving_box(*box, stats));
+}
+
+int plume_set_initial_velocity_box(plume_handle* h, const plume_box* box) {
+  if (!h) return PLUME_ERR_INVALID;
+  if (!box) return set_err(h, PLUME_ERR_INVALID, "null box");
+  return from_engine(h, h->eng->set_initial_velocity_box(*box));
+}
+
+int plume_download_iop(plume_handle* h, uint8_t* inside, double* values, size_t n) {
+  if (!h) return PLUME_ERR_INVALID;
+  return from_engine(h, h->eng->download_iop(inside, values, n));
 }
 
 int plume_profile_sweeps(plume_handle* h, int on) {

@@ -171,8 +171,54 @@ bool put_field(GzOut& g, const int res[3], const double center[3], const double 
 
 }  // namespace
 
+// SPARSE_MATRIX::write / writeGz (SPARSE_MATRIX.cpp:508-561) of the obstacle
+// matrix: rows, cols, entry count, then (row, col, value) in (row, col)
+// order.  Row i of an interior cell holds (i, i) = 1 outside the box, 0
+// inside, and inside also (i, last) = the box velocity component.  Bytes go
+// to `sink` in pieces of about 1 MB.
+static bool put_iop_matrix(const int res[3], const IopRecord& iop,
+                    const std::function<bool(const void*, size_t)>& sink) {
+  const int X = res[0], Y = res[1], Z = res[2];
+  const int rows = 3 * (X - 2) * (Y - 2) * (Z - 2), cols = rows + 1;
+  int inside = 0;
+  for (int z = 1; z < Z - 1; z++)
+    for (int y = 1; y < Y - 1; y++)
+      for (int x = 1; x < X - 1; x++) inside += iop.inside[x + (size_t)y * X + (size_t)z * X * Y] ? 1 : 0;
+  const int total = rows + 3 * inside;
+  const int head[3] = {rows, cols, total};
+  if (!sink(head, sizeof(head))) return false;
+  std::vector<unsigned char> buf;
+  buf.reserve((1 << 20) + 64);
+  auto entry = [&](int r, int c, double v) {
+    unsigned char e[16];
+    memcpy(e, &r, 4);
+    memcpy(e + 4, &c, 4);
+    memcpy(e + 8, &v, 8);
+    buf.insert(buf.end(), e, e + 16);
+  };
+  int row = 0;
+  for (int z = 1; z < Z - 1; z++)
+    for (int y = 1; y < Y - 1; y++)
+      for (int x = 1; x < X - 1; x++) {
+        const size_t c = x + (size_t)y * X + (size_t)z * X * Y;
+        for (int i = 0; i < 3; i++, row++) {
+          if (iop.inside[c]) {
+            entry(row, row, 0.0);
+            entry(row, cols - 1, iop.values[3 * c + i]);
+          } else {
+            entry(row, row, 1.0);
+          }
+        }
+        if (buf.size() >= (1u << 20)) {
+          if (!sink(buf.data(), buf.size())) return false;
+          buf.clear();
+        }
+      }
+  return buf.empty() || sink(buf.data(), buf.size());
+}
+
 int write_state_gz(const std::string& path_in, const StateHeader& h, const FieldFetch& fetch,
-                   const std::vector<uint8_t>& obstacles, std::string& err) {
+                   const std::vector<uint8_t>& obstacles, const IopRecord& iop, std::string& err) {
   std::string path = path_in;
   const size_t n = path.size();
   if (n < 2 || path[n - 1] != 'z' || path[n - 2] != 'g') path += ".gz";  // line 1025-1027
@@ -227,8 +273,20 @@ int write_state_gz(const std::string& path_in, const StateHeader& h, const Field
   const int zres[3] = {0, 0, 0};
   const double zero3[3] = {0, 0, 0};
   const std::vector<double> empty;
-  ok = ok && put_field(g, zres, zero3, zero3, empty);
-  ok = ok && put_field(g, zres, zero3, zero3, empty);
+  ok = ok && put_field(g, zres, zero3, zero3, empty);  // midMaccormack
+  // postIOP (lines 1101-1102): empty until the first moving-box step
+  if (ok) {
+    int rc = fetch(PLUME_F_POST_IOP, buf);
+    if (rc != PLUME_OK) {
+      g.close();
+      err = "field download failed while writing " + path;
+      return rc;
+    }
+    ok = buf.empty() ? put_field(g, zres, zero3, zero3, empty) : put_field(g, h.res, center, lengths, buf);
+  }
+  // the obstacle matrix, only once it has rows (lines 1104-1105)
+  if (ok && !iop.inside.empty())
+    ok = put_iop_matrix(h.res, iop, [&](const void* d, size_t n) { return g.write(d, n); });
   const bool closed = g.close();
   if (!ok || !closed) {
     err = "write failed: " + path;
@@ -263,7 +321,7 @@ double norm2(const std::vector<double>& v) {
 }  // namespace
 
 int append_streams(const std::string& dir, const int res[3], const FieldFetch& fetch,
-                   std::string& err) {
+                   const IopRecord& iop, std::string& err) {
   static const char* dims_names[6] = {"velocity.final.matrix.dims", "velocity.preproject.matrix.dims",
                                       "velocity.prediffuse.matrix.dims",
                                       "velocity.preadvect.matrix.dims", "velocity.iop.matrix.dims",
@@ -290,16 +348,23 @@ int append_streams(const std::string& dir, const int res[3], const FieldFetch& f
     int comps;
     int dims_slot;
   };
-  // lines 1402-1461: four velocity streams, then pressure and divergence rows
-  // into the same pressure stream; the IOP stream is only created.
-  const Row rows_to_write[6] = {
+  // lines 1402-1461: four velocity streams, the postIOP stream once a
+  // moving-box step has run (the IOP stream is created in any case), then
+  // pressure and divergence rows into the same pressure stream.  The
+  // reference never closes its IOP stream's FILE (opened at line 1385, left
+  // out of the fclose list at 1458-1463), so stdio's buffered tail of each
+  // row reaches its file only at process exit, after later rows; here every
+  // row is appended whole, in step order.
+  const bool using_iop = !iop.inside.empty();  // line 1378: _neumannIOP.rows() > 0
+  std::vector<Row> rows_to_write = {
       {"velocity.final.matrix.transpose", PLUME_F_VELOCITY, 3, 0},
       {"velocity.preproject.matrix.transpose", PLUME_F_PREPROJECTION, 3, 1},
       {"velocity.prediffuse.matrix.transpose", PLUME_F_PREDIFFUSION, 3, 2},
       {"velocity.preadvect.matrix.transpose", PLUME_F_PREADVECTION, 3, 3},
-      {"pressure.matrix.transpose", PLUME_F_PRESSURE, 1, 5},
-      {"pressure.matrix.transpose", PLUME_F_DIVERGENCE, 1, 5},
   };
+  if (using_iop) rows_to_write.push_back({"velocity.iop.matrix.transpose", PLUME_F_POST_IOP, 3, 4});
+  rows_to_write.push_back({"pressure.matrix.transpose", PLUME_F_PRESSURE, 1, 5});
+  rows_to_write.push_back({"pressure.matrix.transpose", PLUME_F_DIVERGENCE, 1, 5});
   {
     FILE* iop = fopen((dir + "velocity.iop.matrix.transpose").c_str(), "ab");
     if (!iop) {
@@ -328,6 +393,18 @@ int append_streams(const std::string& dir, const int res[3], const FieldFetch& f
     }
     if (fclose(f) != 0 || !ok) {
       err = std::string("write failed: ") + dir + r.file;
+      return PLUME_ERR_IO;
+    }
+  }
+  if (using_iop) {  // lines 1455-1456: the matrix itself, uncompressed
+    FILE* f = fopen((dir + "neumann.iop.matrices").c_str(), "ab");
+    if (!f) {
+      err = "could not open " + dir + "neumann.iop.matrices";
+      return PLUME_ERR_IO;
+    }
+    const bool ok = put_iop_matrix(res, iop, [&](const void* d, size_t n) { return fwrite(d, 1, n, f) == n; });
+    if (fclose(f) != 0 || !ok) {
+      err = "write failed: " + dir + "neumann.iop.matrices";
       return PLUME_ERR_IO;
     }
   }

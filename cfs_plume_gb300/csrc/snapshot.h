@@ -18,17 +18,27 @@ struct StateHeader {
   double dx, total_time, dt, buoyancy, vorticity_eps;
 };
 
+// The obstacle matrix N of the last moving-box step (FLUID_3D_MIC.h:246,
+// built by setPeeledSparseMovingIOP, FLUID_3D_MIC.cpp:1645-1692), as an
+// inside mask (N cells) and the last-column values (3N); both empty when no
+// moving step has run, in which case the reference writes no matrix.
+struct IopRecord {
+  std::vector<uint8_t> inside;
+  std::vector<double> values;
+};
+
 // fetch(field_id, dst) fills dst (N or 3N doubles, reference layout) and
 // returns 0 on success; field ids are plume_field values.
 using FieldFetch = std::function<int(int, std::vector<double>&)>;
 
-// Writes the state file; `obstacles` has N bytes.  Returns a plume_status.
+// Writes the state file; `obstacles` has N bytes.  PLUME_F_POST_IOP may
+// fetch an empty vector (never assigned).  Returns a plume_status.
 int write_state_gz(const std::string& path, const StateHeader& h, const FieldFetch& fetch,
-                   const std::vector<uint8_t>& obstacles, std::string& err);
+                   const std::vector<uint8_t>& obstacles, const IopRecord& iop, std::string& err);
 
 // Appends one step's rows under `dir` (which must end with a path separator,
 // as the reference's snapshot path does).  Returns a plume_status.
 int append_streams(const std::string& dir, const int res[3], const FieldFetch& fetch,
-                   std::string& err);
+                   const IopRecord& iop, std::string& err);
 
 }  // namespace plume

@@ -489,4 +489,115 @@ __global__ void k_gradient(Grid g, StepConsts<T> c, V3<T> v, const T* p) {
   }
 }
 
+
+// ------------------------------------------------------------ moving box
+// The box of FLUID_3D_MIC::stepWithMovingObstacle as the stomp kernel sees
+// it: every constant is computed once per step on the host (box.cpp).  Cells
+// outside [lo, hi) are certainly outside the box (a bound with a margin of
+// two cells around its circumscribed sphere), so only the cells near the box
+// run the FP64 geometry.
+struct BoxDev {
+  double center[3], half[3], R[9], axis[3], omega[3], disp[3];
+  double d[3];  // cell size per axis, 1 / res (FLUID_3D_MIC::cellCenter)
+  int lo[3], hi[3];
+};
+
+// Inside test and rigid velocity of interior cell (x, y, z), in FP64 with
+// every operation rounded separately in the reference's order (the explicit
+// _rn intrinsics keep the compiler from contracting them into FMAs in the
+// FP32 engine too):
+//   cellCenter          FLUID_3D_MIC.cpp:1717-1730
+//   BOX::inside         BOX.cpp:59-70        |R (p - c)| <= half, per axis
+//   BOX::update_r       BOX.cpp:72-81        r = u - axis (u.axis / |axis|^2)
+//   update_linearVelocity BOX.h:78-83, VEC3.h:154-155   v = w x r + disp
+__device__ inline bool box_cell(const BoxDev& b, int x, int y, int z, double v[3]) {
+  if (x < b.lo[0] || x >= b.hi[0] || y < b.lo[1] || y >= b.hi[1] || z < b.lo[2] ||
+      z >= b.hi[2])
+    return false;
+  const int xyz[3] = {x, y, z};
+  double u[3];
+  for (int k = 0; k < 3; k++) {
+    double p = __dadd_rn(0.0, __dmul_rn((double)xyz[k], b.d[k]));
+    p = __dadd_rn(p, __dmul_rn(b.d[k], 0.5));
+    u[k] = __dsub_rn(p, b.center[k]);
+  }
+  for (int k = 0; k < 3; k++) {
+    const double q = __dadd_rn(__dadd_rn(__dmul_rn(b.R[3 * k], u[0]), __dmul_rn(b.R[3 * k + 1], u[1])),
+                               __dmul_rn(b.R[3 * k + 2], u[2]));
+    if (!(fabs(q) <= b.half[k])) return false;
+  }
+  const double* a = b.axis;
+  const double s = __ddiv_rn(
+      __dadd_rn(__dadd_rn(__dmul_rn(u[0], a[0]), __dmul_rn(u[1], a[1])), __dmul_rn(u[2], a[2])),
+      __dadd_rn(__dadd_rn(__dmul_rn(a[0], a[0]), __dmul_rn(a[1], a[1])), __dmul_rn(a[2], a[2])));
+  double r[3];
+  for (int k = 0; k < 3; k++) r[k] = __dsub_rn(u[k], __dmul_rn(a[k], s));
+  const double* w = b.omega;
+  v[0] = __dadd_rn(__dsub_rn(__dmul_rn(w[1], r[2]), __dmul_rn(r[1], w[2])), b.disp[0]);
+  v[1] = __dadd_rn(__dadd_rn(__dmul_rn(-w[0], r[2]), __dmul_rn(r[0], w[2])), b.disp[1]);
+  v[2] = __dadd_rn(__dsub_rn(__dmul_rn(w[0], r[1]), __dmul_rn(r[0], w[1])), b.disp[2]);
+  return true;
+}
+
+// The obstacle stomp u <- N [u; 1] over the interior (setPeeledSparseMovingIOP,
+// setVelocityNeumann and the sparse product, FLUID_3D_MIC.cpp:1645-1701 and
+// SPARSE_MATRIX.cpp:83-105).  Row i of N holds (i, i) = 1 outside the box,
+// 0 inside, and (i, last) = the box velocity inside; the product accumulates
+// y_i = 0 + u_i N(i,i), then + 1 N(i,last), in that order, which this kernel
+// repeats (so a -0 outside the box becomes +0 as in the reference).
+// mode 0: the stomp, writes inside[] for every interior cell, vals[] for the
+//         inside ones, and when cache != 0 post (postIOP, a copy of the whole
+//         field, border cells included);
+// mode 1: setInitialVelocity(BOX*) (FLUID_3D_MIC.cpp:744-764): u = box
+//         velocity inside, other cells untouched.
+template <typename T>
+__global__ void k_box_stomp(Grid g, BoxDev b, V3<T> vel, V3<T> post, int cache, uint8_t* inside,
+                            double* vals, int mode) {
+  PL_GRID_STRIDE(i, g.N) {
+    const int x = i % g.X;
+    const int t = i / g.X;
+    const int y = t % g.Y;
+    const int z = t / g.Y;
+    if (on_border(g, x, y, z)) {
+      if (mode == 0 && cache) {
+        post.x[i] = vel.x[i];
+        post.y[i] = vel.y[i];
+        post.z[i] = vel.z[i];
+      }
+      continue;
+    }
+    double bv[3];
+    const bool in = box_cell(b, x, y, z, bv);
+    if (mode == 1) {
+      if (in) {
+        vel.x[i] = (T)bv[0];
+        vel.y[i] = (T)bv[1];
+        vel.z[i] = (T)bv[2];
+      }
+      continue;
+    }
+    T* comp[3] = {vel.x, vel.y, vel.z};
+    T out[3];
+    for (int c = 0; c < 3; c++) {
+      const double u = (double)comp[c][i];
+      const double y0 = __dadd_rn(0.0, __dmul_rn(u, in ? 0.0 : 1.0));
+      out[c] = (T)(in ? __dadd_rn(y0, __dmul_rn(bv[c], 1.0)) : y0);
+    }
+    vel.x[i] = out[0];
+    vel.y[i] = out[1];
+    vel.z[i] = out[2];
+    if (cache) {
+      post.x[i] = out[0];
+      post.y[i] = out[1];
+      post.z[i] = out[2];
+    }
+    inside[i] = in ? 1 : 0;
+    if (in) {
+      vals[3 * (size_t)i] = bv[0];
+      vals[3 * (size_t)i + 1] = bv[1];
+      vals[3 * (size_t)i + 2] = bv[2];
+    }
+  }
+}
+
 }  // namespace plume

@@ -16,7 +16,7 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import PlumeParams, PlumeStepStats
+from ._abi import PlumeBox, PlumeParams, PlumeStepStats
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "lib", "libplume.so")
@@ -64,6 +64,14 @@ def load_library(path=LIB_PATH):
         "plume_snapshot_async": (C.c_int, [H, C.c_char_p, C.c_int32, C.c_int32]),
         "plume_wait_snapshots": (C.c_int, [H]),
         "plume_sweep_times": (C.c_int, [H, P(C.c_double), P(C.c_int64)]),
+        "plume_box_init": (C.c_int, [P(PlumeBox), P(C.c_double), P(C.c_double), C.c_double, C.c_double]),
+        "plume_box_spin": (C.c_int, [P(PlumeBox)]),
+        "plume_box_translate": (C.c_int, [P(PlumeBox)]),
+        "plume_box_inside": (C.c_int, [P(PlumeBox), P(C.c_double), P(C.c_int32)]),
+        "plume_box_velocity": (C.c_int, [P(PlumeBox), P(C.c_double), P(C.c_double)]),
+        "plume_step_moving_box": (C.c_int, [H, P(PlumeBox), P(PlumeStepStats)]),
+        "plume_set_initial_velocity_box": (C.c_int, [H, P(PlumeBox)]),
+        "plume_download_iop": (C.c_int, [H, C.c_void_p, C.c_void_p, C.c_size_t]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -203,6 +211,66 @@ class Plume:
         _check(self.lib.plume_mic_diagonal(self.h, p.ctypes.data), self.h)
         return p
 
+    def step_moving_box(self, box, stats=True):
+        """One stepWithMovingObstacle with `box` (a BOX or PlumeBox) as it is."""
+        st = PlumeStepStats()
+        b = box.state if isinstance(box, BOX) else box
+        _check(self.lib.plume_step_moving_box(self.h, C.byref(b), C.byref(st) if stats else None), self.h)
+        return st if stats else None
+
+    def set_initial_velocity_box(self, box):
+        b = box.state if isinstance(box, BOX) else box
+        _check(self.lib.plume_set_initial_velocity_box(self.h, C.byref(b)), self.h)
+
+    def iop(self):
+        """(inside mask [N] uint8, last-column values [N, 3]) of the last moving step."""
+        inside = np.empty(self.N, dtype=np.uint8)
+        vals = np.empty(3 * self.N)
+        _check(self.lib.plume_download_iop(self.h, inside.ctypes.data, vals.ctypes.data, self.N), self.h)
+        return inside, vals.reshape(-1, 3)
+
+
+class BOX:
+    """The reference's moving box (src/geometry/BOX.h) over plume_box."""
+
+    def __init__(self, center, lengths, period, translationPeriod):
+        self.lib = load_library()
+        self.state = PlumeBox()
+        c = (C.c_double * 3)(*center)
+        l = (C.c_double * 3)(*lengths)
+        _check(self.lib.plume_box_init(C.byref(self.state), c, l, period, translationPeriod))
+
+    def set_dt(self, dt):
+        self.state.dt = dt
+
+    def spin(self):
+        _check(self.lib.plume_box_spin(C.byref(self.state)))
+
+    def translate_center(self):
+        _check(self.lib.plume_box_translate(C.byref(self.state)))
+
+    def inside(self, point):
+        out = C.c_int32()
+        _check(self.lib.plume_box_inside(C.byref(self.state), (C.c_double * 3)(*point), C.byref(out)))
+        return bool(out.value)
+
+    def velocity_at(self, point):
+        v = (C.c_double * 3)()
+        _check(self.lib.plume_box_velocity(C.byref(self.state), (C.c_double * 3)(*point), v))
+        return tuple(v)
+
+    @property
+    def theta(self):
+        return self.state.theta
+
+    @property
+    def phi(self):
+        return self.state.phi
+
+    @property
+    def center(self):
+        return tuple(self.state.center)
+
 
 class FLUID_3D_MIC:
     """Facade with the reference class's names (FLUID_3D_MIC.h:37-120).
@@ -269,6 +337,12 @@ class FLUID_3D_MIC:
     def step(self):
         return self.plume.step()
 
+    def stepWithMovingObstacle(self, box):
+        return self.plume.step_moving_box(box)
+
+    def setInitialVelocity(self, box):
+        self.plume.set_initial_velocity_box(box)
+
     def writeGz(self, filename):
         self.plume.write_state(filename)
 
@@ -324,3 +398,6 @@ class FLUID_3D_MIC:
 
     def cachedDivergence(self):
         return self.plume.field("cachedDivergence")
+
+    def postIOP(self):
+        return self._vec("postIOP")

@@ -89,6 +89,9 @@ typedef enum plume_field {
   PLUME_F_CACHED_PRESSURE,
   PLUME_F_CACHED_DIVERGENCE,
   PLUME_F_PREVORTICITY,      /* vector */
+  PLUME_F_POST_IOP,          /* vector: velocity after the obstacle stomp of the
+                                last moving-box step (FLUID_3D_MIC.h:178), before
+                                projection; PLUME_ERR_STATE before the first one */
   PLUME_F_COUNT
 } plume_field;
 

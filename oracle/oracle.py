@@ -11,7 +11,7 @@ import subprocess
 import numpy as np
 
 from cfs_plume_gb300 import _abi
-from cfs_plume_gb300._abi import PlumeParams, PlumeStepStats
+from cfs_plume_gb300._abi import PlumeBox, PlumeParams, PlumeStepStats
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libplume_oracle.so")
@@ -47,6 +47,14 @@ def load():
         "orc_advect_scalar": (None, [P(C.c_int32), C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
         "orc_solve_poisson": (C.c_int32, [P(PlumeParams), C.c_void_p, C.c_void_p, P(PlumeStepStats)]),
         "orc_source_value": (C.c_double, [C.c_uint64, C.c_int32, C.c_int64, C.c_double]),
+        "orc_box_init": (None, [P(PlumeBox), P(C.c_double), P(C.c_double), C.c_double, C.c_double]),
+        "orc_box_spin": (None, [P(PlumeBox)]),
+        "orc_box_translate": (None, [P(PlumeBox)]),
+        "orc_box_inside": (C.c_int, [P(PlumeBox), P(C.c_double)]),
+        "orc_box_velocity": (None, [P(PlumeBox), P(C.c_double), P(C.c_double)]),
+        "orc_step_moving_box": (None, [H, P(PlumeBox), P(PlumeStepStats)]),
+        "orc_set_initial_velocity_box": (None, [H, P(PlumeBox)]),
+        "orc_iop_entries": (C.c_int64, [H, P(C.c_int32), C.c_void_p, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -99,6 +107,25 @@ class Oracle:
         assert self.lib.orc_get_obstacles(self.h, a.ctypes.data, a.size) == 0
         return a
 
+    def step_moving_box(self, box):
+        st = PlumeStepStats()
+        self.lib.orc_step_moving_box(self.h, C.byref(box), C.byref(st))
+        return st
+
+    def set_initial_velocity_box(self, box):
+        self.lib.orc_set_initial_velocity_box(self.h, C.byref(box))
+
+    def iop_entries(self):
+        """((rows, cols), ij [n, 2] int32, values [n]) of the obstacle matrix, or None."""
+        rc = (C.c_int32 * 2)()
+        n = self.lib.orc_iop_entries(self.h, rc, None, None)
+        if n < 0:
+            return None
+        ij = np.empty((n, 2), dtype=np.int32)
+        val = np.empty(n)
+        self.lib.orc_iop_entries(self.h, rc, ij.ctypes.data, val.ctypes.data)
+        return (rc[0], rc[1]), ij, val
+
 
 def _arr3(v):
     return (C.c_int32 * len(v))(*v)
@@ -138,3 +165,29 @@ def solve_poisson(params, b, x0=None):
 
 def source_value(seed, step, cell, noise):
     return load().orc_source_value(seed, step, cell, noise)
+
+
+def box_init(center, lengths, period, translation_period):
+    """BOX(center, lengths, period, translationPeriod) restated (plume_box)."""
+    b = PlumeBox()
+    load().orc_box_init(C.byref(b), (C.c_double * 3)(*center), (C.c_double * 3)(*lengths),
+                        period, translation_period)
+    return b
+
+
+def box_spin(b):
+    load().orc_box_spin(C.byref(b))
+
+
+def box_translate(b):
+    load().orc_box_translate(C.byref(b))
+
+
+def box_inside(b, p):
+    return bool(load().orc_box_inside(C.byref(b), (C.c_double * 3)(*p)))
+
+
+def box_velocity(b, p):
+    v = (C.c_double * 3)()
+    load().orc_box_velocity(C.byref(b), (C.c_double * 3)(*p), v)
+    return tuple(v)

@@ -10,6 +10,8 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <map>
+#include <utility>
 #include <vector>
 
 namespace {
@@ -426,6 +428,11 @@ struct orc_handle {
       cachedDivergence;
   std::vector<Real> velocity, velocityOld, force, vorticity, preprojection, prediffusion,
       preadvection, cachedQuadratic, postadvection, prevorticity;
+  // moving box: postIOP and the obstacle matrix N of the last moving step, as
+  // the map of SPARSE_MATRIX (row, col) -> value; both empty before it
+  std::vector<Real> postIOP;
+  std::map<std::pair<int, int>, Real> neumannIOP;
+  int iopRows = 0, iopCols = 0;
   std::vector<uint8_t> obst;
   Solver solver;
   explicit orc_handle(const plume_params& pp) : p(pp), g(pp.res) {}
@@ -455,6 +462,7 @@ struct orc_handle {
       case PLUME_F_CACHED_QUADRATIC: return &cachedQuadratic;
       case PLUME_F_POSTADVECTION: return &postadvection;
       case PLUME_F_PREVORTICITY: return &prevorticity;
+      case PLUME_F_POST_IOP: return &postIOP;
       default: return nullptr;
     }
   }
@@ -794,6 +802,209 @@ void orc_step(orc_handle* h, plume_step_stats* st) {
   project(*h, st ? st : &local);
   h->totalTime += 0.1;
   h->totalSteps++;
+}
+
+// ------------------------------------------------------------- moving box
+// BOX (src/geometry/BOX.cpp) restated on the plume_box struct.
+namespace {
+const Real kPi = 3.14159265358979323846;
+const Real kAxis[3] = {0.0, 0.0, 1.0};  // BOX.cpp:36
+
+// MATRIX3::rotation (src/linearalgebra/MATRIX3.h:96-117)
+void rotation(const Real axis_in[3], Real theta, Real R[9]) {
+  Real a[3] = {axis_in[0], axis_in[1], axis_in[2]};
+  const Real n = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+  const Real inv = 1.0 / n;
+  for (int k = 0; k < 3; k++) a[k] *= inv;
+  const Real c = cos(theta), s = sin(theta), v = (1.0 - c);
+  R[0] = a[0] * a[0] * v + c;
+  R[1] = a[0] * a[1] * v - a[2] * s;
+  R[2] = a[0] * a[2] * v + a[1] * s;
+  R[3] = a[1] * a[0] * v + a[2] * s;
+  R[4] = a[1] * a[1] * v + c;
+  R[5] = a[1] * a[2] * v - a[0] * s;
+  R[6] = a[2] * a[0] * v - a[1] * s;
+  R[7] = a[2] * a[1] * v + a[0] * s;
+  R[8] = a[2] * a[2] * v + c;
+}
+
+// FLUID_3D_MIC::cellCenter (FLUID_3D_MIC.cpp:1704-1733)
+void cell_center(const Grid& g, int x, int y, int z, Real p[3]) {
+  const Real dx = 1.0 / g.X, dy = 1.0 / g.Y, dz = 1.0 / g.Z;
+  p[0] = 0.0;
+  p[1] = 0.0;
+  p[2] = 0.0;
+  p[0] += x * dx;
+  p[1] += y * dy;
+  p[2] += z * dz;
+  p[0] += dx * 0.5;
+  p[1] += dy * 0.5;
+  p[2] += dz * 0.5;
+}
+
+// BOX::inside (BOX.cpp:59-70)
+bool box_inside(const plume_box& b, const Real p[3]) {
+  Real t[3] = {p[0] - b.center[0], p[1] - b.center[1], p[2] - b.center[2]};
+  Real q[3];
+  for (int r = 0; r < 3; r++)
+    q[r] = b.rotation[3 * r] * t[0] + b.rotation[3 * r + 1] * t[1] + b.rotation[3 * r + 2] * t[2];
+  const Real half[3] = {b.lengths[0] * 0.5, b.lengths[1] * 0.5, b.lengths[2] * 0.5};
+  return fabs(q[0]) <= half[0] && fabs(q[1]) <= half[1] && fabs(q[2]) <= half[2];
+}
+
+// BOX::update_r + update_linearVelocity (BOX.cpp:72-91, BOX.h:65-83, VEC3.h:154-155, 293-296)
+void box_velocity(const plume_box& b, const Real p[3], Real v[3]) {
+  const Real u[3] = {p[0] - b.center[0], p[1] - b.center[1], p[2] - b.center[2]};
+  const Real dot = u[0] * kAxis[0] + u[1] * kAxis[1] + u[2] * kAxis[2];
+  const Real n2 = kAxis[0] * kAxis[0] + kAxis[1] * kAxis[1] + kAxis[2] * kAxis[2];
+  const Real sc = dot / n2;
+  const Real r[3] = {u[0] - kAxis[0] * sc, u[1] - kAxis[1] * sc, u[2] - kAxis[2] * sc};
+  const Real w[3] = {0.0, 0.0, 2 * kPi / b.period};
+  const Real d[3] = {0.25 * 2 * kPi / b.translation_period * cos(b.phi), 0.0, 0.0};
+  const Real c[3] = {w[1] * r[2] - r[1] * w[2], -w[0] * r[2] + r[0] * w[2], w[0] * r[1] - r[0] * w[1]};
+  for (int k = 0; k < 3; k++) v[k] = c[k] + d[k];
+}
+
+// setPeeledSparseMovingIOP + setVelocityNeumann + N * [u; 1] + setWithPeeled
+// (FLUID_3D_MIC.cpp:1645-1701, SPARSE_MATRIX.cpp:83-105, 429-440)
+void moving_iop(orc_handle& h, const plume_box& b) {
+  const Grid& g = h.g;
+  const int peeled = 3 * (g.X - 2) * (g.Y - 2) * (g.Z - 2);
+  h.iopRows = peeled;
+  h.iopCols = peeled + 1;
+  h.neumannIOP.clear();
+  for (int k = 0; k < peeled; k++) h.neumannIOP[std::make_pair(k, k)] = 1.0;
+  const int last = h.iopCols - 1;
+  int index = 0;
+  for (int z = 1; z < g.Z - 1; z++)
+    for (int y = 1; y < g.Y - 1; y++)
+      for (int x = 1; x < g.X - 1; x++)
+        for (int i = 0; i < 3; i++, index++) {
+          Real p[3];
+          cell_center(g, x, y, z, p);
+          if (box_inside(b, p)) {
+            h.neumannIOP[std::make_pair(index, index)] = 0.0;
+            Real v[3];
+            box_velocity(b, p, v);
+            h.neumannIOP[std::make_pair(index, last)] = v[i];
+          }
+        }
+  std::vector<Real> un(peeled + 1);
+  index = 0;
+  for (int z = 1; z < g.Z - 1; z++)
+    for (int y = 1; y < g.Y - 1; y++)
+      for (int x = 1; x < g.X - 1; x++) {
+        const int c = x + y * g.X + z * g.slab;
+        for (int i = 0; i < 3; i++) un[index++] = h.velocity[3 * c + i];
+      }
+  un[peeled] = 1.0;
+  std::vector<Real> y(peeled, 0.0);
+  for (const auto& e : h.neumannIOP) y[e.first.first] += un[e.first.second] * e.second;
+  index = 0;
+  for (int z = 1; z < g.Z - 1; z++)
+    for (int yy = 1; yy < g.Y - 1; yy++)
+      for (int x = 1; x < g.X - 1; x++) {
+        const int c = x + yy * g.X + z * g.slab;
+        for (int i = 0; i < 3; i++) h.velocity[3 * c + i] = y[index++];
+      }
+}
+}  // namespace
+
+void orc_box_init(plume_box* b, const double center[3], const double lengths[3], double period,
+                  double translation_period) {
+  for (int k = 0; k < 3; k++) {
+    b->center[k] = center[k];
+    b->original_center[k] = center[k];
+    b->lengths[k] = lengths[k];
+  }
+  for (int k = 0; k < 9; k++) b->rotation[k] = (k == 0 || k == 4 || k == 8) ? 1.0 : 0.0;
+  b->theta = 0.0;
+  b->phi = 0.0;
+  b->period = period;
+  b->translation_period = translation_period;
+  b->dt = 0.0;
+}
+
+// BOX::spin (BOX.cpp:93-101)
+void orc_box_spin(plume_box* b) {
+  const Real dTheta = 2 * kPi * b->dt / b->period;
+  b->theta += dTheta;
+  if (b->theta >= 2 * kPi) b->theta = 0.0;
+  rotation(kAxis, -1 * b->theta, b->rotation);
+}
+
+// BOX::translate_center (BOX.cpp:104-113)
+void orc_box_translate(plume_box* b) {
+  const Real dPhi = 2 * kPi * b->dt / b->translation_period;
+  b->phi += dPhi;
+  if (b->phi >= 2 * kPi) b->phi = 0.0;
+  const Real disp = 0.25 * sin(b->phi);
+  b->center[0] = b->original_center[0] + disp;
+}
+
+// FLUID_3D_MIC::stepWithMovingObstacle, FLUID_3D_MIC.cpp:236-310
+void orc_step_moving_box(orc_handle* h, const plume_box* box, plume_step_stats* st) {
+  const Grid& g = h->g;
+  h->dt = h->p.dt;
+  std::fill(h->force.begin(), h->force.end(), 0.0);
+  vec_set_zero_border(g, h->velocity.data());
+  sca_set_zero_border(g, h->density.data());
+  vec_axpy(g, h->dt, h->velocity.data(), h->force.data());
+  std::fill(h->force.begin(), h->force.end(), 0.0);
+  h->prevorticity = h->velocity;
+  add_vorticity(*h);
+  vec_axpy(g, h->dt, h->velocity.data(), h->force.data());
+  advect_stam(*h);
+  h->prediffusion = h->velocity;
+  damping(*h);
+  h->preprojection = h->velocity;
+  moving_iop(*h, *box);
+  h->postIOP = h->velocity;
+  plume_step_stats local{};
+  project(*h, st ? st : &local);
+  h->totalTime += 0.1;
+  h->totalSteps++;
+}
+
+// FLUID_3D_MIC::setInitialVelocity(BOX*), FLUID_3D_MIC.cpp:744-764
+void orc_set_initial_velocity_box(orc_handle* h, const plume_box* box) {
+  const Grid& g = h->g;
+  for (int z = 1; z < g.Z - 1; z++)
+    for (int y = 1; y < g.Y - 1; y++)
+      for (int x = 1; x < g.X - 1; x++) {
+        Real p[3];
+        cell_center(g, x, y, z, p);
+        if (box_inside(*box, p)) {
+          Real v[3];
+          box_velocity(*box, p, v);
+          const int c = x + y * g.X + z * g.slab;
+          for (int k = 0; k < 3; k++) h->velocity[3 * c + k] = v[k];
+        }
+      }
+}
+
+int orc_box_inside(const plume_box* b, const double p[3]) { return box_inside(*b, p) ? 1 : 0; }
+void orc_box_velocity(const plume_box* b, const double p[3], double v[3]) { box_velocity(*b, p, v); }
+
+// The obstacle matrix as (row, col, value) triples in map order; returns the
+// entry count (or -1 before the first moving step).  rows_cols may be NULL;
+// the triples are written only when the buffers are given.
+int64_t orc_iop_entries(orc_handle* h, int32_t rows_cols[2], int32_t* ij, double* val) {
+  if (h->iopRows == 0) return -1;
+  if (rows_cols) {
+    rows_cols[0] = h->iopRows;
+    rows_cols[1] = h->iopCols;
+  }
+  int64_t k = 0;
+  for (const auto& e : h->neumannIOP) {
+    if (ij) {
+      ij[2 * k] = e.first.first;
+      ij[2 * k + 1] = e.first.second;
+    }
+    if (val) val[k] = e.second;
+    k++;
+  }
+  return k;
 }
 
 int orc_get(orc_handle* h, int32_t field, double* dst, size_t n) {

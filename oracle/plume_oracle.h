@@ -19,6 +19,7 @@
 #include <stddef.h>
 #include <stdint.h>
 #include "../include/plume.h"
+#include "../include/plume_box.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -54,6 +55,22 @@ void orc_advect_scalar(const int32_t res[3], double dt0, const double* vel_aos,
    FLUID_3D_MIC.cpp:918-1015): x in/out (N), b (N). Returns iterations. */
 int32_t orc_solve_poisson(const plume_params* p, double* x, const double* b,
                           plume_step_stats* stats);
+/* ---- moving box (plume_box, include/plume_box.h) ---- */
+/* BOX constructor, spin, translate_center, inside, rigid velocity (BOX.cpp). */
+void orc_box_init(plume_box* b, const double center[3], const double lengths[3], double period,
+                  double translation_period);
+void orc_box_spin(plume_box* b);
+void orc_box_translate(plume_box* b);
+int orc_box_inside(const plume_box* b, const double p[3]);
+void orc_box_velocity(const plume_box* b, const double p[3], double v[3]);
+/* FLUID_3D_MIC::stepWithMovingObstacle (FLUID_3D_MIC.cpp:236-310). */
+void orc_step_moving_box(orc_handle* h, const plume_box* box, plume_step_stats* stats);
+/* FLUID_3D_MIC::setInitialVelocity(BOX*) (FLUID_3D_MIC.cpp:744-764). */
+void orc_set_initial_velocity_box(orc_handle* h, const plume_box* box);
+/* The last moving step's obstacle matrix as map-ordered triples; returns the
+   entry count, -1 before the first moving step. */
+int64_t orc_iop_entries(orc_handle* h, int32_t rows_cols[2], int32_t* ij, double* val);
+
 /* Seeded source value 1 + noise*(2u-1) for (seed, step, cell). */
 double orc_source_value(uint64_t seed, int32_t step_index, int64_t cell, double noise);
 

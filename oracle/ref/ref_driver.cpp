@@ -12,8 +12,12 @@
 //        steps=N out=DIR/ gz=0|1 streams=0|1 dump=0|1
 //     Per step: source, step(), then (optionally) writeGz("DIR/fluid.%04i.fluid3d")
 //     and appendStreams() into DIR, as runEverytime does.  dump=1 writes the
-//     final state with writeGz to DIR/final.fluid3d.gz.  Prints one line
-//     "STEP i iters=.. " per step parsed from the reference's own output.
+//     final state with writeGz to DIR/final.fluid3d.gz.
+//     Moving box: moving=1 boxc=cx,cy,cz boxl=lx,ly,lz period=P tperiod=T
+//     [initvel=1] builds BOX(boxc, boxl, P, T) with set_dt(0.1); initvel=1
+//     calls setInitialVelocity(&box) once; each step then runs
+//     stepWithMovingObstacle(&box) in place of step() and afterwards
+//     box.spin() and box.translate_center().
 //   fluid3d_ref readgz FILE OUTPREFIX
 //     Reads FILE with the reference's FLUID_3D_MIC::readGz and writes every
 //     field as raw little-endian doubles to OUTPREFIX.<name>.f64 plus
@@ -95,6 +99,21 @@ int main(int argc, char** argv) {
     dump_sca(pre, "cachedDivergence", fluid.cachedDivergence());
     dump_vec(pre, "prevorticity", fluid.prevorticity());
     write_raw(pre + ".obstacles.u8", fluid.obstacles(), (size_t)fluid.size());
+    if (fluid.postIOP().totalCells() > 0) dump_vec(pre, "postIOP", fluid.postIOP());
+    SPARSE_MATRIX& n = fluid.neumannIOPMatrix();
+    if (n.rows() > 0) {  // the obstacle matrix as (row, col) int pairs and values
+      std::vector<int> ij;
+      std::vector<double> val;
+      for (const auto& e : n.matrix()) {
+        ij.push_back(e.first.first);
+        ij.push_back(e.first.second);
+        val.push_back(e.second);
+      }
+      write_raw(pre + ".iop_ij.i32", ij.data(), ij.size() * sizeof(int));
+      write_raw(pre + ".iop_val.f64", val.data(), val.size() * sizeof(double));
+      const int rc[2] = {n.rows(), n.cols()};
+      write_raw(pre + ".iop_dims.i32", rc, sizeof(rc));
+    }
     FILE* f = fopen((pre + ".header.txt").c_str(), "w");
     fprintf(f, "%d %d %d %d %.17g %.17g %.17g %.17g\n", fluid.xRes(), fluid.yRes(), fluid.zRes(),
             fluid.totalSteps(), fluid.dx(), fluid.dt(), fluid.buoyancy(), fluid.vorticityEps());
@@ -132,6 +151,15 @@ int main(int argc, char** argv) {
   if (kv.count("buoyancy")) fluid.buoyancy() = atof(kv["buoyancy"].c_str());
   fluid.snapshotPath() = out;
 
+  const bool moving = kv.count("moving") && kv["moving"] == "1";
+  std::vector<double> bc3 = parse_list(kv.count("boxc") ? kv["boxc"] : "0.5,0.5,0.5");
+  std::vector<double> bl3 = parse_list(kv.count("boxl") ? kv["boxl"] : "0.2,0.2,0.2");
+  BOX obox(VEC3F(bc3[0], bc3[1], bc3[2]), VEC3F(bl3[0], bl3[1], bl3[2]),
+          kv.count("period") ? atof(kv["period"].c_str()) : 4.0,
+          kv.count("tperiod") ? atof(kv["tperiod"].c_str()) : 8.0);
+  obox.set_dt(0.1);
+  if (moving && kv.count("initvel") && kv["initvel"] == "1") fluid.setInitialVelocity(&obox);
+
   const int X = (int)res[0], Y = (int)res[1];
   for (int step = 0; step < steps; step++) {
     if (source == "column") {
@@ -146,7 +174,13 @@ int main(int argc, char** argv) {
             fluid.heatField()[c] = val;
           }
     }
-    fluid.step();
+    if (moving) {
+      fluid.stepWithMovingObstacle(&obox);
+      obox.spin();
+      obox.translate_center();
+    } else {
+      fluid.step();
+    }
     if (gz) {
       char buffer[512];
       snprintf(buffer, sizeof(buffer), "%sfluid.%04i.fluid3d", out.c_str(), step);

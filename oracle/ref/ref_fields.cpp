@@ -4,8 +4,9 @@
 // OpenGL headers, so they are not compiled for the oracle.  This file restates
 // the member functions that the reference's FLUID_3D_MIC.cpp calls, against
 // the reference's own class declarations (FIELD_3D.h, VECTOR3_FIELD_3D.h),
-// each following the cited reference definition.  BOX members used only by
-// the moving-obstacle path abort: the plume path never calls them.
+// each following the cited reference definition.  BOX.cpp includes OpenGL for
+// BOX::draw as well, so the BOX members that FLUID_3D_MIC.cpp and the headless
+// driver call are restated here too (draw is left out).
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
@@ -557,7 +558,57 @@ void VECTOR3_FIELD_3D::readGz(gzFile& file) {
 }
 
 // ----------------------------------------------------------------------- BOX
-// Moving-obstacle members; unreachable from the plume step.
-bool BOX::inside(const VEC3F&) const { abort(); }
-void BOX::update_r(const VEC3F&, VEC3F*) { abort(); }
-void BOX::calculate_displacementVelocity() { abort(); }
+// BOX.cpp:26-41
+BOX::BOX(const VEC3F& center, const VEC3F& lengths, double period, double translationPeriod)
+    : _center(center), _lengths(lengths), _period(period), _translationPeriod(translationPeriod) {
+  set_halfLengths();
+  set_angularVelocity();
+  initialize_rotationMatrix();
+  _theta = 0.0;
+  _phi = 0.0;
+  _currentTime = 0.0;
+  _dt = 0.0;
+  _rotationAxis = VEC3F(0.0, 0.0, 1.0);
+  _displacement = VEC3F(0.0, 0.0, 0.0);
+  _displacementVelocity = VEC3F(0.0, 0.0, 0.0);
+  _original_center = _center;
+}
+BOX::~BOX() {}
+
+// BOX.cpp:50-57
+void BOX::initialize_rotationMatrix() { _rotation = MATRIX3::I(); }
+void BOX::update_rotationMatrix() { _rotation = MATRIX3::rotation(_rotationAxis, -1 * _theta); }
+
+// BOX.cpp:59-70
+bool BOX::inside(const VEC3F& point) const {
+  VEC3F t = point - _center;
+  t = _rotation * t;
+  return fabs(t[0]) <= _halfLengths[0] && fabs(t[1]) <= _halfLengths[1] &&
+         fabs(t[2]) <= _halfLengths[2];
+}
+
+// BOX.cpp:72-81
+void BOX::update_r(const VEC3F& point, VEC3F* r) {
+  VEC3F u = point - _center;
+  *r = u - project_onto(u, _rotationAxis);
+}
+
+// BOX.cpp:84-91
+void BOX::calculate_displacementVelocity() {
+  _displacementVelocity[0] = 0.25 * 2 * M_PI / _translationPeriod * cos(_phi);
+}
+
+// BOX.cpp:93-101
+void BOX::spin() {
+  _theta += 2 * M_PI * _dt / _period;
+  if (_theta >= 2 * M_PI) _theta = 0.0;
+  update_rotationMatrix();
+}
+
+// BOX.cpp:104-113
+void BOX::translate_center() {
+  _phi += 2 * M_PI * _dt / _translationPeriod;
+  if (_phi >= 2 * M_PI) _phi = 0.0;
+  _displacement[0] = 0.25 * sin(_phi);
+  _center[0] = _original_center[0] + _displacement[0];
+}

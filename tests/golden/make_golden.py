@@ -12,10 +12,17 @@ configurations and stores what it produced:
                         per-field sums / L2 norms and every 97th value;
   ref_state_8x10x6/     the reference's own state file (writeGz, gzip level 1)
                         and appendStreams output after 2 steps, as format
-                        fixtures.
+                        fixtures;
+  ref_moving_<case>.npz the moving-box step (stepWithMovingObstacle with the
+                        BOX spun and translated after every step): every
+                        state field, postIOP and the obstacle matrix's
+                        (row, col, value) entries after the last step;
+  ref_moving_state_10x12x8/  the reference's state file and streams of a
+                        moving-box run, as format fixtures.
 
 Needs the reference tree (PLUME_REFERENCE_DIR, default /root/reference) and
-writes nothing outside tests/golden/.  Usage: python tests/golden/make_golden.py
+writes nothing outside tests/golden/.
+Usage: python tests/golden/make_golden.py [plume|moving]   (default: both)
 """
 import os
 import shutil
@@ -68,7 +75,31 @@ def run_ref(p, steps, src, extra=()):
                    capture_output=True)
     fields = {n: np.fromfile(d + "/x.%s.f64" % n) for n in _abi.FIELDS}
     fields["obstacles"] = np.fromfile(d + "/x.obstacles.u8", dtype=np.uint8)
+    if os.path.exists(d + "/x.postIOP.f64"):
+        fields["postIOP"] = np.fromfile(d + "/x.postIOP.f64")
+        fields["iop_dims"] = np.fromfile(d + "/x.iop_dims.i32", dtype=np.int32)
+        fields["iop_ij"] = np.fromfile(d + "/x.iop_ij.i32", dtype=np.int32).reshape(-1, 2)
+        fields["iop_val"] = np.fromfile(d + "/x.iop_val.f64")
     return d, iters, fields
+
+
+# name -> (params kwargs, steps, source, box center, box lengths, period,
+#          translation period, setInitialVelocity first)
+MOVING = {
+    "box_16x20x12": (dict(res=(16, 20, 12), vorticity_eps=1.0), 4, "column",
+                     (0.5, 0.4, 0.5), (0.3, 0.2, 0.4), 4.0, 8.0, True),
+    # fast spin and sway: theta and phi wrap past 2 pi; open faces; the box
+    # reaches out of the domain
+    "box_open_14x12x16": (dict(res=(14, 12, 16), bc=(0, 0, 0, 0, 0, 0), vorticity_eps=0.5,
+                               source=_abi.SRC_BOX, box_lo=(5, 1, 6), box_hi=(9, 3, 10),
+                               source_noise=0.05, seed=3), 8, "box",
+                          (0.85, 0.5, 0.45), (0.5, 0.3, 0.25), 0.45, 0.35, False),
+}
+
+
+def moving_args(c, l, period, tperiod, initvel):
+    return ["moving=1", "boxc=%r,%r,%r" % tuple(c), "boxl=%r,%r,%r" % tuple(l),
+            "period=%r" % period, "tperiod=%r" % tperiod, "initvel=%d" % int(initvel)]
 
 
 def params_record(p):
@@ -80,6 +111,14 @@ def params_record(p):
 def main():
     if not os.path.exists(REF):
         sys.exit("build the reference first: make -C oracle ref")
+    what = sys.argv[1] if len(sys.argv) > 1 else "all"
+    if what in ("all", "plume"):
+        plume_fixtures()
+    if what in ("all", "moving"):
+        moving_fixtures()
+
+
+def plume_fixtures():
     for name, (kw, steps, src) in CASES.items():
         p = _abi.default_params(**kw)
         d, iters, fields = run_ref(p, steps, src)
@@ -119,6 +158,39 @@ def main():
     np.savez_compressed(os.path.join(fx, "fields.npz"), **fields, **params_record(p))
     shutil.rmtree(d)
     print("format fixture:", sorted(os.listdir(fx)))
+
+
+def moving_fixtures():
+    for name, (kw, steps, src, c, l, per, tper, initvel) in MOVING.items():
+        p = _abi.default_params(**kw)
+        d, iters, fields = run_ref(p, steps, src, moving_args(c, l, per, tper, initvel))
+        np.savez_compressed(os.path.join(HERE, "ref_moving_%s.npz" % name), iters=np.array(iters),
+                            steps=steps, box_center=np.array(c), box_lengths=np.array(l),
+                            period=per, translation_period=tper, initvel=int(initvel),
+                            **params_record(p), **fields)
+        shutil.rmtree(d)
+        print("moving", name, "iters", iters)
+
+    # format fixtures of a moving-box run: state file with postIOP and the
+    # obstacle matrix, and the streams with the IOP rows and matrices
+    fx = os.path.join(HERE, "ref_moving_state_10x12x8")
+    shutil.rmtree(fx, ignore_errors=True)
+    os.makedirs(fx)
+    p = _abi.default_params(res=(10, 12, 8), vorticity_eps=1.0)
+    mv = ((0.5, 0.35, 0.5), (0.4, 0.3, 0.35), 2.0, 3.0, True)
+    d = tempfile.mkdtemp(prefix="plume_golden_")
+    subprocess.run(ref_args(p, 2, "column", d) + ["gz=1", "streams=1"] + moving_args(*mv),
+                   check=True, capture_output=True)
+    for f in sorted(os.listdir(d)):
+        if f.startswith("fluid.0001") or f.endswith(".dims") or f.endswith(".transpose") or \
+                f.endswith(".matrices"):
+            shutil.copy(os.path.join(d, f), fx)
+    np.savez_compressed(os.path.join(fx, "box.npz"), box_center=np.array(mv[0]),
+                        box_lengths=np.array(mv[1]), period=mv[2], translation_period=mv[3],
+                        initvel=int(mv[4]), **params_record(p))
+    shutil.rmtree(d)
+    print("moving format fixture:", sorted(os.listdir(fx)))
+
 
 
 if __name__ == "__main__":
