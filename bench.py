@@ -238,6 +238,61 @@ def measure_arm(g, a, dist, nbox, box_values_seed):
             "e2e": dist.sum(n_e2e) / e2e_s, "n_e2e": n_e2e}
 
 
+# the moving box of the stepWithMovingObstacle measurement (cellCenter units)
+MOVING_BOX = dict(center=(0.5, 0.3, 0.5), lengths=(0.35, 0.1, 0.2), period=2.0, translation_period=4.0)
+
+
+def measure_moving(a, dist, res, prec, local, rank):
+    """stepWithMovingObstacle on the same plume with a spinning, swaying box:
+    K device-timed steps (CG loop as a CUDA graph), then K more with CUDA
+    events around every stomp launch for the stomp kernel's roofline."""
+    from cfs_plume_gb300 import _abi
+    from cfs_plume_gb300.plume import BOX, Plume
+    g = Plume(_abi.plume_config(res, precision=prec, seed=rank, device=local))
+    mb = MOVING_BOX
+    box = BOX(mb["center"], mb["lengths"], mb["period"], mb["translation_period"])
+    box.set_dt(0.1)
+    g.run_moving_timed(box, 0, a.warmup, stats=False)
+    dist.barrier()
+    g.lib.plume_sync(g.h)
+    ms, stats = g.run_moving_timed(box, a.warmup, a.steps)
+    dist.barrier()
+    ms_max = dist.max(ms)
+    g.profile_sweeps(True)
+    g.run_moving_timed(box, a.warmup + a.steps, a.steps, stats=False)
+    stomp_ms, stomp_n = g.stomp_times()
+    g.profile_sweeps(False)
+    inside = int(g.iop()[0].sum())
+    g.close()
+    return {"ms": ms_max, "value": dist.sum(a.steps) / (ms_max / 1000.0),
+            "iters": [s.iterations for s in stats], "launches": sum(s.launches for s in stats),
+            "converged": all(s.converged for s in stats), "stomp_ms": stomp_ms,
+            "stomp_launches": stomp_n, "inside": inside}
+
+
+def moving_record(m, res, N, nint, S, peak, steps):
+    # the stomp reads every velocity (border cells for the postIOP copy), writes
+    # postIOP everywhere, the inside mask on the interior, and inside the box
+    # the new velocity and the obstacle matrix's last column (FP64)
+    stomp_bytes = N * 6 * S + nint + m["inside"] * (3 * S + 24)
+    avg = m["stomp_ms"] / m["stomp_launches"] if m["stomp_launches"] else None
+    ach = stomp_bytes / (avg / 1000.0) / 1e9 if avg else None
+    mb = MOVING_BOX
+    return {"value": m["value"], "unit": "steps/s", "ms_per_step": m["ms"] / steps,
+            "pcg_iters_per_step": statistics.mean(m["iters"]), "all_converged": m["converged"],
+            "workload": "stepWithMovingObstacle on the plume %dx%dx%d (no buoyancy), plain MIC(0)-PCG "
+                        "from p = 0, box centre %s lengths %s spin period %g sway period %g, "
+                        "spun and translated after every step" % (res + (mb["center"], mb["lengths"],
+                                                                         mb["period"],
+                                                                         mb["translation_period"])),
+            "inside_cells": m["inside"],
+            "roofline": {"bound": "hbm", "kernel": "k_box_stomp (obstacle stomp, postIOP copy)",
+                         "achieved": ach, "peak": peak, "unit": "GB/s",
+                         "frac": (ach / peak) if ach else None, "bytes_per_launch": stomp_bytes,
+                         "ms_per_launch": avg, "launches_timed": m["stomp_launches"],
+                         "bytes_model": "N*6S + N_int + inside*(3S+24)"}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -251,6 +306,7 @@ def main():
     ap.add_argument("--arms", default="both", choices=["both", "plain"],
                     help="both: plain MIC-PCG and the learned warm start (the headline value)")
     ap.add_argument("--weights", default=None, help="warm-start network (default: the committed one)")
+    ap.add_argument("--no-moving", action="store_true", help="skip the moving-box step measurement")
     a = ap.parse_args()
     rank, world, local = dist_env()
     if a.impl == "reference":
@@ -296,6 +352,7 @@ def main():
         lrn = measure_arm(gl, a, dist, nbox, rank)
         gl.close()
         net.close()
+    mov = None if a.no_moving else measure_moving(a, dist, res, prec, local, rank)
     clk = clocks.stop()
     head = lrn if lrn is not None else plain
     ms_max, value, iters = head["ms"], head["value"], head["iters"]
@@ -351,6 +408,7 @@ def main():
         "solve_roofline": {"kernel": "poisson solve (all MIC-PCG kernels)", "achieved": achieved_solve,
                            "unit": "GB/s", "frac": (achieved_solve / peak) if achieved_solve else None,
                            "bytes_model": "N_int*(5S+2P+2 + iters*(16S+2P+3)) per solve"},
+        "moving_box": moving_record(mov, res, N, nint, S, peak, a.steps) if mov else None,
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": nbox * 8,
                 "d2h_bytes_per_step": 3 * N * 8},
         "clocks": clk,

@@ -324,11 +324,41 @@ class EngineT : public Engine {
   }
 
   int run_timed(int32_t first_step, int32_t n, double* ms, plume_step_stats* stats) override {
+    return timed([&] { return run(first_step, n, stats); }, ms);
+  }
+
+  // n moving-box steps, the box spun and translated on the host after each
+  int run_moving_timed(plume_box& box, int32_t first_step, int32_t n, double* ms,
+                       plume_step_stats* stats) override {
+    return timed(
+        [&] {
+          for (int k = 0; k < n; k++) {
+            int rc = add_source(first_step + k);
+            if (rc == PLUME_OK) rc = step_moving_box(box, stats ? stats + k : nullptr);
+            if (rc != PLUME_OK) return rc;
+            plume_box_spin(&box);
+            plume_box_translate(&box);
+          }
+          return (int)PLUME_OK;
+        },
+        ms);
+  }
+
+  int stomp_times(double* ms, int64_t* launches) override {
+    PL_TRY(cudaStreamSynchronize(s_));
+    *ms = stomp_ms_;
+    *launches = stomp_n_;
+    return PLUME_OK;
+  }
+
+  // CUDA events on the library stream around body()
+  template <typename F>
+  int timed(F&& body, double* ms) {
     cudaEvent_t a, b;
     PL_TRY(cudaEventCreate(&a));
     PL_TRY(cudaEventCreate(&b));
     PL_TRY(cudaEventRecord(a, s_));
-    int rc = run(first_step, n, stats);
+    int rc = body();
     if (rc == PLUME_OK) {
       PL_TRY(cudaEventRecord(b, s_));
       PL_TRY(cudaEventSynchronize(b));
@@ -369,7 +399,7 @@ class EngineT : public Engine {
     BoxDev b;
     if (!box_dev(box, b)) return fail(PLUME_ERR_INVALID, "box with non-finite or zero parameters");
     launches_ = 0;
-    k_box_stomp<T><<<grid_for(g_.N), 256, 0, s_>>>(g_, b, vel_, vel_, 0, nullptr, nullptr, 1);
+    k_box_stomp<T><<<grid_for(box_cells(b)), 256, 0, s_>>>(g_, b, vel_, vel_, 0, nullptr, nullptr, 1);
     PL_CHECK_LAUNCH();
     PL_TRY(cudaStreamSynchronize(s_));
     return PLUME_OK;
@@ -427,9 +457,14 @@ class EngineT : public Engine {
     std::swap(vel_, spare_);
     if (box) {
       // the IOP stomp u <- N [u; 1], cached as postIOP (lines 276-284)
-      k_box_stomp<T><<<gN, 256, 0, s_>>>(g_, *box, vel_, post_iop_, post_iop_.x ? 1 : 0, iop_in_,
-                                         iop_val_, 0);
+      if (prof_on_) PL_TRY(cudaEventRecord(stomp_ev_[0], s_));
+      const int cache_post = post_iop_.x ? 1 : 0;
+      k_box_post<T><<<gN, 256, 0, s_>>>(g_, vel_, post_iop_, cache_post, iop_in_);
       PL_CHECK_LAUNCH();
+      k_box_stomp<T><<<grid_for(box_cells(*box)), 256, 0, s_>>>(g_, *box, vel_, post_iop_, cache_post,
+                                                                 iop_in_, iop_val_, 0);
+      PL_CHECK_LAUNCH();
+      if (prof_on_) PL_TRY(cudaEventRecord(stomp_ev_[1], s_));
       has_iop_ = true;
     }
     // project (lines 314-399)
@@ -491,6 +526,13 @@ class EngineT : public Engine {
     PL_TRY(cudaEventRecord(ev_[3], s_));
     total_time_ += 0.1;  // FLUID_3D_MIC.cpp:221 (goalTime)
     total_steps_ += 1;
+    if (box && prof_on_) {
+      PL_TRY(cudaEventSynchronize(stomp_ev_[1]));
+      float f = 0.f;
+      PL_TRY(cudaEventElapsedTime(&f, stomp_ev_[0], stomp_ev_[1]));
+      stomp_ms_ += f;
+      stomp_n_ += 1;
+    }
     if (stats) return fill_stats(stats);
     return PLUME_OK;
   }
@@ -849,10 +891,14 @@ class EngineT : public Engine {
 
   int profile_sweeps(int on) override {
     PL_TRY(cudaStreamSynchronize(s_));
-    if (on && !prof_ev_[0][0])
+    if (on && !prof_ev_[0][0]) {
       for (auto& buf : prof_ev_)
         for (auto& e : buf) PL_TRY(cudaEventCreate(&e));
+      for (auto& e : stomp_ev_) PL_TRY(cudaEventCreate(&e));
+    }
     prof_on_ = on != 0;
+    stomp_ms_ = 0;
+    stomp_n_ = 0;
     prof_n_[0] = prof_n_[1] = 0;
     prof_ms_ = 0;
     prof_launches_ = 0;
@@ -1060,17 +1106,35 @@ class EngineT : public Engine {
         dev = std::max(dev, std::fabs(s - (i == j ? 1.0 : 0.0)));
       }
     if (dev <= 1e-9) {
-      const double rho = std::sqrt(b.half[0] * b.half[0] + b.half[1] * b.half[1] + b.half[2] * b.half[2]) *
-                         (1.0 + 1e-6);
+      // R is a rotation: inside cells satisfy u = R^T q with |q_k| <= half_k,
+      // so |u_i| <= sum_k |R_ki| |half_k|; widened by 1e-6 and two cells
       for (int k = 0; k < 3; k++) {
+        double ext = 0;
+        for (int j = 0; j < 3; j++) ext += std::fabs(b.R[3 * j + k]) * std::fabs(b.half[j]);
+        ext *= 1.0 + 1e-6;
         const double n = res[k];
-        const double lo = std::floor((b.center[k] - rho) * n - 0.5) - 2.0;
-        const double hi = std::ceil((b.center[k] + rho) * n - 0.5) + 3.0;
+        const double lo = std::floor((b.center[k] - ext) * n - 0.5) - 2.0;
+        const double hi = std::ceil((b.center[k] + ext) * n - 0.5) + 3.0;
         b.lo[k] = (int)std::max(1.0, std::min(n - 1.0, lo));
         b.hi[k] = (int)std::max(1.0, std::min(n - 1.0, hi));
       }
     }
+    double rmax = 0;
+    for (int k = 0; k < 9; k++) {
+      b.fR[k] = (float)b.R[k];
+      rmax = std::max(rmax, std::fabs(b.R[k]));
+    }
+    for (int k = 0; k < 3; k++) {
+      b.fc[k] = (float)b.center[k];
+      b.fh[k] = (float)b.half[k];
+      b.fd[k] = (float)b.d[k];
+    }
+    b.ftol = (float)(1e-5 * (1.0 + rmax));
     return true;
+  }
+
+  static long long box_cells(const BoxDev& b) {
+    return std::max(1LL, (long long)(b.hi[0] - b.lo[0]) * (b.hi[1] - b.lo[1]) * (b.hi[2] - b.lo[2]));
   }
 
   const T* scalar_ptr(int field) const {
@@ -1176,6 +1240,8 @@ class EngineT : public Engine {
     for (auto& buf : prof_ev_)
       for (auto e : buf)
         if (e) cudaEventDestroy(e);
+    for (auto e : stomp_ev_)
+      if (e) cudaEventDestroy(e);
     if (s_) cudaStreamDestroy(s_);
     pool_ = nullptr;
     s_ = nullptr;
@@ -1233,6 +1299,9 @@ class EngineT : public Engine {
   bool host_direct_ = false;  // downloads written by a kernel into host memory
   static constexpr int kProfEvents = 64;
   bool prof_on_ = false;
+  cudaEvent_t stomp_ev_[2] = {nullptr, nullptr};  // around the moving-box stomp
+  double stomp_ms_ = 0;
+  int64_t stomp_n_ = 0;
   cudaEvent_t prof_ev_[2][kProfEvents] = {};
   int prof_n_[2] = {0, 0};
   int prof_idx_[2][kProfEvents / 3] = {};  // PCG iteration of each pair (-1: set-up)

@@ -33,6 +33,10 @@ class Engine {
   virtual int step_moving_box(const plume_box& box, plume_step_stats* stats) = 0;
   virtual int set_initial_velocity_box(const plume_box& box) = 0;
   virtual bool has_iop() const = 0;
+  virtual int run_moving_timed(plume_box& box, int32_t first_step, int32_t n, double* ms,
+                               plume_step_stats* stats) = 0;
+  // with sweep profiling on: summed device ms and launches of the stomp kernel
+  virtual int stomp_times(double* ms, int64_t* launches) = 0;
   virtual int download_iop(uint8_t* inside, double* values, size_t n) = 0;
   virtual int download(int field, double* dst, size_t n) = 0;
   virtual int upload(int field, const double* src, size_t n) = 0;

@@ -428,6 +428,18 @@ int plume_set_initial_velocity_box(plume_handle* h, const plume_box* box) {
   return from_engine(h, h->eng->set_initial_velocity_box(*box));
 }
 
+int plume_run_moving_timed(plume_handle* h, plume_box* box, int32_t first_step_index, int32_t n,
+                           double* ms_device, plume_step_stats* stats) {
+  if (!h) return PLUME_ERR_INVALID;
+  if (!box || !ms_device || n < 0) return set_err(h, PLUME_ERR_INVALID, "bad argument");
+  return from_engine(h, h->eng->run_moving_timed(*box, first_step_index, n, ms_device, stats));
+}
+
+int plume_box_stomp_times(plume_handle* h, double* ms_total, int64_t* launches) {
+  if (!h || !ms_total || !launches) return PLUME_ERR_INVALID;
+  return from_engine(h, h->eng->stomp_times(ms_total, launches));
+}
+
 int plume_download_iop(plume_handle* h, uint8_t* inside, double* values, size_t n) {
   if (!h) return PLUME_ERR_INVALID;
   return from_engine(h, h->eng->download_iop(inside, values, n));

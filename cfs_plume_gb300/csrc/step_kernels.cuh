@@ -500,6 +500,9 @@ struct BoxDev {
   double center[3], half[3], R[9], axis[3], omega[3], disp[3];
   double d[3];  // cell size per axis, 1 / res (FLUID_3D_MIC::cellCenter)
   int lo[3], hi[3];
+  // FP32 copies for the pre-test that sends clearly-outside cells past the
+  // FP64 geometry (FP64 issues at a small fraction of the FP32 rate here)
+  float fc[3], fh[3], fR[9], fd[3], ftol;
 };
 
 // Inside test and rigid velocity of interior cell (x, y, z), in FP64 with
@@ -515,6 +518,20 @@ __device__ inline bool box_cell(const BoxDev& b, int x, int y, int z, double v[3
       z >= b.hi[2])
     return false;
   const int xyz[3] = {x, y, z};
+  {
+    // |q| in FP32 beyond half + tol means outside: tol bounds the FP32
+    // rounding of the centre, offset and R q many times over
+    float uf[3], amax = 0.f;
+    for (int k = 0; k < 3; k++) {
+      uf[k] = ((float)xyz[k] + 0.5f) * b.fd[k] - b.fc[k];
+      amax += fabsf(uf[k]);
+    }
+    const float tol = b.ftol * (1.0f + amax);
+    for (int k = 0; k < 3; k++) {
+      const float q = b.fR[3 * k] * uf[0] + b.fR[3 * k + 1] * uf[1] + b.fR[3 * k + 2] * uf[2];
+      if (fabsf(q) > b.fh[k] * 1.000001f + tol) return false;
+    }
+  }
   double u[3];
   for (int k = 0; k < 3; k++) {
     double p = __dadd_rn(0.0, __dmul_rn((double)xyz[k], b.d[k]));
@@ -539,49 +556,80 @@ __device__ inline bool box_cell(const BoxDev& b, int x, int y, int z, double v[3
   return true;
 }
 
+// -0 by its bit pattern (std::signbit would widen a float to double first,
+// an FP64-pipe conversion per value)
+__device__ inline bool is_neg_zero(float v) { return __float_as_uint(v) == 0x80000000u; }
+__device__ inline bool is_neg_zero(double v) {
+  return (unsigned long long)__double_as_longlong(v) == 0x8000000000000000ull;
+}
+
 // The obstacle stomp u <- N [u; 1] over the interior (setPeeledSparseMovingIOP,
 // setVelocityNeumann and the sparse product, FLUID_3D_MIC.cpp:1645-1701 and
 // SPARSE_MATRIX.cpp:83-105).  Row i of N holds (i, i) = 1 outside the box,
 // 0 inside, and (i, last) = the box velocity inside; the product accumulates
-// y_i = 0 + u_i N(i,i), then + 1 N(i,last), in that order, which this kernel
-// repeats (so a -0 outside the box becomes +0 as in the reference).
-// mode 0: the stomp, writes inside[] for every interior cell, vals[] for the
-//         inside ones, and when cache != 0 post (postIOP, a copy of the whole
-//         field, border cells included);
-// mode 1: setInitialVelocity(BOX*) (FLUID_3D_MIC.cpp:744-764): u = box
-//         velocity inside, other cells untouched.
+// y_i = 0 + u_i N(i,i), then + 1 N(i,last), in that order, which these
+// kernels repeat (so a -0 outside the box becomes +0 as in the reference).
+// Two passes on one stream:
+//   k_box_post   every cell, no FP64: outside-box value 0 + u*1 (u itself but
+//                for -0 -> +0, exact in T, stored only when it changes),
+//                postIOP = that field (border cells copied), inside[] = 0;
+//   k_box_stomp  the box's bounding cells [lo, hi) only: the FP64 inside test
+//                and, inside, u = (0 + u*0) + 1*v_box, postIOP, inside[] = 1
+//                and the last-column values.
+// Keeping the FP64 geometry in its own launch over the bounding cells stops
+// it from running (hoisted by the compiler) for every cell of the grid.
 template <typename T>
-__global__ void k_box_stomp(Grid g, BoxDev b, V3<T> vel, V3<T> post, int cache, uint8_t* inside,
-                            double* vals, int mode) {
+__global__ void k_box_post(Grid g, V3<T> vel, V3<T> post, int cache, uint8_t* inside) {
   PL_GRID_STRIDE(i, g.N) {
     const int x = i % g.X;
     const int t = i / g.X;
     const int y = t % g.Y;
     const int z = t / g.Y;
-    if (on_border(g, x, y, z)) {
-      if (mode == 0 && cache) {
-        post.x[i] = vel.x[i];
-        post.y[i] = vel.y[i];
-        post.z[i] = vel.z[i];
+    T* comp[3] = {vel.x, vel.y, vel.z};
+    T* pc[3] = {post.x, post.y, post.z};
+    const bool border = on_border(g, x, y, z);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const T u = comp[c][i];
+      T o = u;
+      if (!border) {
+        o = T(0) + u * T(1);
+        if (is_neg_zero(u)) comp[c][i] = o;
       }
-      continue;
+      if (cache) pc[c][i] = o;
     }
+    if (!border) inside[i] = 0;
+  }
+}
+
+// mode 0: the stomp of the cells inside the box (after k_box_post);
+// mode 1: setInitialVelocity(BOX*) (FLUID_3D_MIC.cpp:744-764): u = box
+//         velocity inside, other cells untouched.
+template <typename T>
+__global__ void k_box_stomp(Grid g, BoxDev b, V3<T> vel, V3<T> post, int cache, uint8_t* inside,
+                            double* vals, int mode) {
+  const int nx = b.hi[0] - b.lo[0], ny = b.hi[1] - b.lo[1];
+  const int n = nx * ny * (b.hi[2] - b.lo[2]);
+  PL_GRID_STRIDE(k, n) {
+    const int x = b.lo[0] + k % nx;
+    const int t = k / nx;
+    const int y = b.lo[1] + t % ny;
+    const int z = b.lo[2] + t / ny;
     double bv[3];
-    const bool in = box_cell(b, x, y, z, bv);
+    if (!box_cell(b, x, y, z, bv)) continue;
+    const int i = x + y * g.X + z * g.slab;
     if (mode == 1) {
-      if (in) {
-        vel.x[i] = (T)bv[0];
-        vel.y[i] = (T)bv[1];
-        vel.z[i] = (T)bv[2];
-      }
+      vel.x[i] = (T)bv[0];
+      vel.y[i] = (T)bv[1];
+      vel.z[i] = (T)bv[2];
       continue;
     }
     T* comp[3] = {vel.x, vel.y, vel.z};
     T out[3];
+#pragma unroll
     for (int c = 0; c < 3; c++) {
-      const double u = (double)comp[c][i];
-      const double y0 = __dadd_rn(0.0, __dmul_rn(u, in ? 0.0 : 1.0));
-      out[c] = (T)(in ? __dadd_rn(y0, __dmul_rn(bv[c], 1.0)) : y0);
+      const double y0 = __dadd_rn(0.0, __dmul_rn((double)comp[c][i], 0.0));
+      out[c] = (T)__dadd_rn(y0, __dmul_rn(bv[c], 1.0));
     }
     vel.x[i] = out[0];
     vel.y[i] = out[1];
@@ -591,12 +639,10 @@ __global__ void k_box_stomp(Grid g, BoxDev b, V3<T> vel, V3<T> post, int cache, 
       post.y[i] = out[1];
       post.z[i] = out[2];
     }
-    inside[i] = in ? 1 : 0;
-    if (in) {
-      vals[3 * (size_t)i] = bv[0];
-      vals[3 * (size_t)i + 1] = bv[1];
-      vals[3 * (size_t)i + 2] = bv[2];
-    }
+    inside[i] = 1;
+    vals[3 * (size_t)i] = bv[0];
+    vals[3 * (size_t)i + 1] = bv[1];
+    vals[3 * (size_t)i + 2] = bv[2];
   }
 }
 

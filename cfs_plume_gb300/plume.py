@@ -72,6 +72,9 @@ def load_library(path=LIB_PATH):
         "plume_step_moving_box": (C.c_int, [H, P(PlumeBox), P(PlumeStepStats)]),
         "plume_set_initial_velocity_box": (C.c_int, [H, P(PlumeBox)]),
         "plume_download_iop": (C.c_int, [H, C.c_void_p, C.c_void_p, C.c_size_t]),
+        "plume_run_moving_timed": (C.c_int, [H, P(PlumeBox), C.c_int32, C.c_int32, P(C.c_double),
+                                             P(PlumeStepStats)]),
+        "plume_box_stomp_times": (C.c_int, [H, P(C.c_double), P(C.c_int64)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -221,6 +224,22 @@ class Plume:
     def set_initial_velocity_box(self, box):
         b = box.state if isinstance(box, BOX) else box
         _check(self.lib.plume_set_initial_velocity_box(self.h, C.byref(b)), self.h)
+
+    def run_moving_timed(self, box, first_step, n, stats=True):
+        """n moving steps (source, step, box spin + translate), device-timed:
+        (ms, [stats])."""
+        b = box.state if isinstance(box, BOX) else box
+        arr = (PlumeStepStats * n)() if stats else None
+        ms = C.c_double()
+        _check(self.lib.plume_run_moving_timed(self.h, C.byref(b), first_step, n, C.byref(ms), arr),
+               self.h)
+        return ms.value, (list(arr) if stats else None)
+
+    def stomp_times(self):
+        """(summed device ms, launches) of the obstacle stomp while sweep profiling is on."""
+        ms, n = C.c_double(), C.c_int64()
+        _check(self.lib.plume_box_stomp_times(self.h, C.byref(ms), C.byref(n)), self.h)
+        return ms.value, n.value
 
     def iop(self):
         """(inside mask [N] uint8, last-column values [N, 3]) of the last moving step."""

@@ -83,6 +83,18 @@ int plume_step_moving_box(plume_handle* h, const plume_box* box, plume_step_stat
    velocity on every interior cell inside the box; other cells unchanged. */
 int plume_set_initial_velocity_box(plume_handle* h, const plume_box* box);
 
+/* n moving steps timed on the device: for k = 0..n-1, plume_add_source(
+   first_step_index + k), plume_step_moving_box(box), then plume_box_spin and
+   plume_box_translate on *box.  ms_device: CUDA-event time on the library's
+   stream around all n steps.  stats: NULL or n entries. */
+int plume_run_moving_timed(plume_handle* h, plume_box* box, int32_t first_step_index, int32_t n,
+                           double* ms_device, plume_step_stats* stats);
+
+/* While sweep profiling is on (plume_profile_sweeps), every obstacle stomp
+   launch is bracketed by CUDA events too: its summed device time and count
+   since profiling was switched on. */
+int plume_box_stomp_times(plume_handle* h, double* ms_total, int64_t* launches);
+
 /* The obstacle matrix N of the last moving step (neumannIOPMatrix(),
    3 n_int x (3 n_int + 1), n_int = (X-2)(Y-2)(Z-2)), in full-grid layout:
    inside[c] = 1 where the interior cell c was inside the box (its diagonal

@@ -492,3 +492,67 @@ def test_postiop_and_iop_before_a_moving_step_and_without_cache():
     bad = BOX((0.5, 0.5, 0.5), (0.4, 0.4, 0.4), 0.0, 8.0)  # zero period
     with pytest.raises(PlumeError):
         g.step_moving_box(bad)
+
+
+@pytest.mark.gpu
+def test_run_moving_timed_matches_step_loop_and_times_the_stomp():
+    """plume_run_moving_timed (source, moving step, spin, translate per step)
+    gives the same fields and box as the same loop through the single-step
+    calls; with profiling on it times one stomp launch per step."""
+    from cfs_plume_gb300.plume import Plume
+    z = _fixture("box_open_14x12x16")
+    p = _params_from(z)
+    a, b = Plume(p), Plume(p)
+    ba, bb = _gpu_box(z), _gpu_box(z)
+    ms, st = a.run_moving_timed(ba, 0, 5)
+    assert ms > 0 and len(st) == 5
+    for s in range(5):
+        b.add_source(s)
+        b.step_moving_box(bb)
+        bb.spin()
+        bb.translate_center()
+    assert bytes(memoryview(ba.state)) == bytes(memoryview(bb.state))
+    for name in _abi.FIELDS + ["postIOP"]:
+        assert np.array_equal(a.field(name), b.field(name)), name
+    a.profile_sweeps(True)
+    a.run_moving_timed(ba, 5, 3, stats=False)
+    ms, n = a.stomp_times()
+    a.profile_sweeps(False)
+    assert n == 3 and ms > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [_abi.PREC_FP64, _abi.PREC_FP32])
+def test_stomp_mask_on_exact_box_faces(precision):
+    """Cell centres exactly on the box faces (|q| = half, which BOX::inside
+    counts as inside) and a box reaching past the domain, unrotated and then
+    rotated: the GPU mask and last column equal the oracle's bit for bit."""
+    from cfs_plume_gb300.plume import BOX, Plume
+    res = (16, 16, 16)
+    p = _abi.default_params(res=res, precision=precision, source=_abi.SRC_NONE, max_iters=0)
+    # faces through the cell centres x = 4, 11 ((x + 0.5) / 16 = 0.28125, 0.71875)
+    # and z = 1, 9 (0.09375, 0.59375), all exact in binary
+    c, l = (0.5, 0.5, 0.34375), (0.4375, 0.25, 0.5)
+    g = Plume(p)
+    o = oracle.Oracle(p)
+    bg = BOX(c, l, 0.8, 1.3)
+    bg.set_dt(0.1)
+    bo = oracle.box_init(c, l, 0.8, 1.3)
+    bo.dt = 0.1
+    for s in range(4):
+        g.step_moving_box(bg)
+        o.step_moving_box(bo)
+        inside, vals = g.iop()
+        assert np.array_equal(inside, _mask_numpy(res, bo))
+        dims, ij, val = _iop_from_mask(res, inside, vals)
+        odims, oij, oval = o.iop_entries()
+        assert dims == odims and np.array_equal(ij, oij), s
+        assert np.array_equal(val.view(np.uint64), oval.view(np.uint64)), s
+        if s == 0:
+            m = inside.reshape(16, 16, 16)
+            assert m[:, :, 4].any() and m[:, :, 11].any() and m[1, :, :].any() and m[9, :, :].any()
+            assert not m[:, :, 3].any() and not m[:, :, 12].any() and not m[10, :, :].any()
+        bg.spin()
+        bg.translate_center()
+        oracle.box_spin(bo)
+        oracle.box_translate(bo)
