@@ -141,3 +141,17 @@ class PlumeBox(C.Structure):
         ("translation_period", C.c_double),
         ("dt", C.c_double),
     ]
+
+
+class PlumeSvdInfo(C.Structure):
+    """plume_svd_info (include/plume_svd.h)."""
+    _fields_ = [
+        ("rows", C.c_int32),
+        ("cols", C.c_int32),
+        ("kept", C.c_int32),
+        ("sweeps", C.c_int32),
+        ("ms_qr", C.c_double),
+        ("ms_svd", C.c_double),
+        ("ms_u", C.c_double),
+        ("ms_io", C.c_double),
+    ]

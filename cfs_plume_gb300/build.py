@@ -80,6 +80,7 @@ def build(verbose=False, ptxas_info=False):
         ("engine_f32.cu", [nvcc] + common_nv),
         ("noalloc.cu", [nvcc] + common_nv + ["-fmad=false"]),
         ("unet.cu", [nvcc] + common_nv),
+        ("svd.cu", [nvcc] + common_nv),
         ("plume_api.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-I" + os.path.join(cuda, "include")]),
         ("snapshot.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread"] + zc),
         ("batch.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread"]),
@@ -108,6 +109,12 @@ def build(verbose=False, ptxas_info=False):
     exe = os.path.join(BIN, "fluid3D")
     if os.path.exists(main_src) and not _newer(exe, [main_src, lib] + headers):
         _run(["g++", "-O2", "-std=c++17", "-o", exe, main_src, "-L" + LIB, "-lplume",
+              "-Wl,-rpath,$ORIGIN/../lib"])
+    # the svdOutOfCoreMultiple stage binary
+    svd_src = os.path.join(CSRC, "svd_main.cpp")
+    svd_exe = os.path.join(BIN, "svdOutOfCoreMultiple")
+    if os.path.exists(svd_src) and not _newer(svd_exe, [svd_src, lib] + headers):
+        _run(["g++", "-O2", "-std=c++17", "-o", svd_exe, svd_src, "-L" + LIB, "-lplume",
               "-Wl,-rpath,$ORIGIN/../lib"])
     return lib
 

@@ -1,0 +1,81 @@
+// cli_config.h -- what the stage binaries share: the cfg reader and the
+// directory helper of the reference's drivers.
+#pragma once
+#include <sys/stat.h>
+
+#include <cctype>
+#include <cstdlib>
+#include <fstream>
+#include <map>
+#include <string>
+
+namespace plume_cli {
+
+// Config reader with the reference parser's rules (SIMPLE_PARSER.cpp:53-195):
+// `key = value` lines of at most 511 characters, '#' comments only at
+// column 0, keys lower-cased and trimmed, values trimmed, numbers via atof,
+// unknown keys ignored, a non-empty line without '=' is an error.
+class Config {
+ public:
+  bool load(const std::string& path, std::string& err) {
+    std::ifstream f(path.c_str());
+    if (!f.good()) {
+      err = "Failed to open file " + path;
+      return false;
+    }
+    char buffer[512];
+    int line_no = 1;
+    while (!f.eof()) {
+      f.getline(buffer, 512);
+      if (f.fail() && !f.eof()) f.clear();  // over-long line: keep the first 511 chars
+      std::string line(buffer);
+      if (line.empty() || line[0] == '#') continue;
+      const size_t pos = line.find('=');
+      if (pos != std::string::npos) {
+        std::string lhs = trim(line.substr(0, pos));
+        const std::string rhs = trim(line.substr(pos + 1));
+        for (char& c : lhs) c = (char)tolower((unsigned char)c);
+        vals_[lhs] = rhs;
+      } else if (!trim(line).empty()) {
+        err = "Unable to parse, error in line " + std::to_string(line_no) + ": '" + line + "'";
+        return false;
+      }
+      line_no++;
+    }
+    return true;
+  }
+  bool has(const std::string& k) const { return vals_.count(lower(k)) != 0; }
+  double num(const std::string& k, double def) const {
+    auto it = vals_.find(lower(k));
+    return it == vals_.end() ? def : atof(it->second.c_str());
+  }
+  int integer(const std::string& k, int def) const { return (int)num(k, def); }
+  std::string str(const std::string& k, const std::string& def) const {
+    auto it = vals_.find(lower(k));
+    return it == vals_.end() ? def : it->second;
+  }
+
+ private:
+  static std::string trim(const std::string& in) {
+    size_t s = 0, e = in.size();
+    while (s < in.size() && isspace((unsigned char)in[s])) s++;
+    while (e > s && isspace((unsigned char)in[e - 1])) e--;
+    return in.substr(s, e - s);
+  }
+  static std::string lower(std::string k) {
+    for (char& c : k) c = (char)tolower((unsigned char)c);
+    return k;
+  }
+  std::map<std::string, std::string> vals_;
+};
+
+// fluid3D.cpp:40-47: create every prefix of the path
+inline void ensure_directory(const std::string& path) {
+  std::string built;
+  for (size_t i = 0; i < path.size(); i++) {
+    built += path[i];
+    if (path[i] == '/' || i == path.size() - 1) mkdir(built.c_str(), 0755);
+  }
+}
+
+}  // namespace plume_cli

@@ -16,7 +16,7 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import PlumeBox, PlumeParams, PlumeStepStats
+from ._abi import PlumeBox, PlumeParams, PlumeStepStats, PlumeSvdInfo
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "lib", "libplume.so")
@@ -75,6 +75,11 @@ def load_library(path=LIB_PATH):
         "plume_run_moving_timed": (C.c_int, [H, P(PlumeBox), C.c_int32, C.c_int32, P(C.c_double),
                                              P(PlumeStepStats)]),
         "plume_box_stomp_times": (C.c_int, [H, P(C.c_double), P(C.c_int64)]),
+        "plume_svd_stream": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_double, C.c_char_p,
+                                       C.c_char_p, C.c_int32, P(PlumeSvdInfo)]),
+        "plume_svd_columns": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double, C.c_int32,
+                                        C.c_void_p, C.c_void_p, P(C.c_int32), P(PlumeSvdInfo)]),
+        "plume_svd_verify": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -420,3 +425,39 @@ class FLUID_3D_MIC:
 
     def postIOP(self):
         return self._vec("postIOP")
+
+
+def svd_stream(prefix, reduced_path, scratch_path, discard_threshold=1e-9, u_path=None, pca_path=None,
+               device=0):
+    """BIG_MATRIX::outOfCoreSVD + writeFinalU for one snapshot stream on the GPU
+    (include/plume_svd.h).  Returns the plume_svd_info as a dict."""
+    lib = load_library()
+    info = PlumeSvdInfo()
+    enc = lambda v: None if v is None else os.fsencode(v)
+    _check(lib.plume_svd_stream(enc(prefix), enc(reduced_path), enc(scratch_path), discard_threshold,
+                                enc(u_path), enc(pca_path), device, C.byref(info)))
+    return {k: getattr(info, k) for k, _ in PlumeSvdInfo._fields_}
+
+
+def svd_columns(A, discard_threshold=1e-9, with_u=True, device=0):
+    """Snapshot SVD of A (n x m, one snapshot per column) on the GPU:
+    (pca values [m], kept, U [n x kept] or None, info dict)."""
+    lib = load_library()
+    A = np.asfortranarray(A, dtype=np.float64)
+    n, m = A.shape
+    pca = np.empty(m)
+    U = np.empty((n, m), order="F") if with_u else None
+    kept = C.c_int32()
+    info = PlumeSvdInfo()
+    _check(lib.plume_svd_columns(A.ctypes.data, n, m, discard_threshold, device, pca.ctypes.data,
+                                 U.ctypes.data if with_u else None, C.byref(kept), C.byref(info)))
+    k = kept.value
+    return pca, k, (U[:, :k].copy() if with_u else None), {f: getattr(info, f) for f, _ in PlumeSvdInfo._fields_}
+
+
+def svd_verify(prefix, u_path, count=10, device=0):
+    """|c - U U^T c| for the first `count` snapshots of the stream (verifyResults)."""
+    lib = load_library()
+    d = np.empty(count)
+    _check(lib.plume_svd_verify(os.fsencode(prefix), os.fsencode(u_path), count, device, d.ctypes.data))
+    return d

@@ -18,11 +18,15 @@ configurations and stores what it produced:
                         state field, postIOP and the obstacle matrix's
                         (row, col, value) entries after the last step;
   ref_moving_state_10x12x8/  the reference's state file and streams of a
-                        moving-box run, as format fixtures.
+                        moving-box run, as format fixtures;
+  ref_svd_10x12x8.npz   the reference's svdOutOfCoreMultiple (oracle/_ref/svd_ref,
+                        its own main) on the six streams of a 12-step moving-box
+                        run: the input streams, every U.*.matrix and every
+                        singular-value vector.
 
 Needs the reference tree (PLUME_REFERENCE_DIR, default /root/reference) and
 writes nothing outside tests/golden/.
-Usage: python tests/golden/make_golden.py [plume|moving]   (default: both)
+Usage: python tests/golden/make_golden.py [plume|moving|svd]   (default: all)
 """
 import os
 import shutil
@@ -38,6 +42,10 @@ sys.path.insert(0, ROOT)
 from cfs_plume_gb300 import _abi  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref", "fluid3d_ref")
+SVD_REF = os.path.join(ROOT, "oracle", "_ref", "svd_ref")
+SVD_STREAMS = ["velocity.final", "velocity.preproject", "velocity.prediffuse", "velocity.preadvect",
+               "pressure", "velocity.iop"]
+SVD_TAGS = ["final", "preproject", "prediffuse", "preadvect", "pressure", "iop"]
 
 # name -> (params kwargs, steps, reference source mode)
 CASES = {
@@ -116,6 +124,43 @@ def main():
         plume_fixtures()
     if what in ("all", "moving"):
         moving_fixtures()
+    if what in ("all", "svd"):
+        svd_fixtures()
+
+
+def svd_fixtures():
+    base = tempfile.mkdtemp(prefix="plume_golden_")
+    # snapshot path one character longer than the reduced path, so that the
+    # reference's singular-value file name rule yields "<stream>.matrix"
+    snap, red, scr = base + "/snap/", base + "/red/", base + "/scratch/"
+    os.makedirs(snap)
+    p = _abi.default_params(res=(10, 12, 8), vorticity_eps=1.0)
+    subprocess.run(ref_args(p, 12, "column", snap) + ["streams=1"] +
+                   moving_args((0.5, 0.35, 0.5), (0.4, 0.3, 0.35), 2.0, 3.0, True),
+                   check=True, capture_output=True)
+    cfg = base + "/svd.cfg"
+    with open(cfg, "w") as f:
+        f.write("snapshot path = %s\nreduced path = %s\nscratch path = %s\n"
+                "simulation snapshots = 12\nreduced snapshots = 12\ndiscard threshold = 1e-9\n"
+                "iop = 1\n" % (snap, red, scr))
+    r = subprocess.run([SVD_REF, cfg], check=True, capture_output=True, text=True)
+    out = {"threshold": 1e-9}
+    for name, tag in zip(SVD_STREAMS, SVD_TAGS):
+        pre = snap + name + ".matrix"
+        out["dims_" + tag] = np.fromfile(pre + ".dims", dtype="<i4")
+        out["stream_" + tag] = np.fromfile(pre + ".transpose")
+        u = red + "U." + tag + ".matrix"
+        hdr = np.fromfile(u, dtype="<i4", count=2)
+        out["U_" + tag] = np.fromfile(u, dtype="<f8", offset=8).reshape(int(hdr[0]), int(hdr[1]))
+        sv = scr + name + ".matrix.singularValues.vector"
+        nsv = int(np.fromfile(sv, dtype="<i4", count=1)[0])
+        out["pca_" + tag] = np.fromfile(sv, dtype="<f8", offset=4, count=nsv)
+        out["pca_file_bytes_" + tag] = os.path.getsize(red + "pca." + tag + ".vector")
+    diffs = [float(l.split(":")[1]) for l in r.stdout.splitlines() if l.strip().startswith("Diff")]
+    out["verify_diffs"] = np.array(diffs)
+    np.savez_compressed(os.path.join(HERE, "ref_svd_10x12x8.npz"), **out)
+    shutil.rmtree(base)
+    print("svd fixture:", {t: out["U_" + t].shape for t in SVD_TAGS})
 
 
 def plume_fixtures():
