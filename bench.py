@@ -270,6 +270,46 @@ def measure_moving(a, dist, res, prec, local, rank):
             "stomp_launches": stomp_n, "inside": inside}
 
 
+def measure_snapshot_svd(res, prec, local, rank, snaps):
+    """svdOutOfCoreMultiple on the device: `snaps` steps of the same plume with
+    the velocity.final row kept in HBM after each (plume_snapshots), then the
+    in-place QR, SVD of R and U = Q U_R (timed by CUDA events inside)."""
+    from cfs_plume_gb300 import _abi
+    from cfs_plume_gb300.plume import Plume, Snapshots
+    g = Plume(_abi.plume_config(res, precision=prec, seed=rank, device=local))
+    sn = Snapshots(g, "final", snaps)
+    for s in range(snaps):
+        g.add_source(s)
+        g.step(stats=False)
+        sn.append()
+    rows, cols = sn.dims()
+    t0 = time.perf_counter()
+    pca, kept, info = sn.svd(1e-9, u_path=None)
+    wall = time.perf_counter() - t0
+    sn.close()
+    g.close()
+    return {"rows": rows, "cols": cols, "kept": kept, "info": info, "wall_s": wall}
+
+
+def svd_record(r, fp64_peak_tflops):
+    n, m = r["cols"], r["rows"]
+    info = r["info"]
+    qr_flops = 2.0 * n * m * m          # MGS: a dot and an axpy per column pair
+    qr_bytes = 8.0 * n * m * m          # each pass reads and writes the later columns
+    qr_s = info["ms_qr"] / 1000.0
+    ach = qr_flops / qr_s / 1e12 if qr_s > 0 else None
+    return {"workload": "velocity.final snapshots of the same plume kept in HBM (n = 3 N_int = %d, m = %d), "
+                        "Gram-Schmidt QR + one-sided Jacobi SVD of R in FP64, U not formed" % (n, m),
+            "kept": r["kept"], "ms_qr": info["ms_qr"], "ms_svd_of_r": info["ms_svd"],
+            "jacobi_sweeps": info["sweeps"], "wall_s": r["wall_s"],
+            "roofline": {"bound": "fp64", "kernel": "k_mgs_pass (Gram-Schmidt pass)",
+                         "achieved": ach, "peak": fp64_peak_tflops, "unit": "TFLOP/s",
+                         "frac": (ach / fp64_peak_tflops) if ach else None,
+                         "peak_kind": "derived: 2 FP64 FMA/clock/SM (ncu dfma peak_sustained) x 152 SMs x 2070 MHz",
+                         "flops_model": "2 n m^2", "bytes_model": "8 n m^2",
+                         "achieved_gbs": qr_bytes / qr_s / 1e9 if qr_s > 0 else None}}
+
+
 def moving_record(m, res, N, nint, S, peak, steps):
     # the stomp reads every velocity (border cells for the postIOP copy), writes
     # postIOP everywhere, the inside mask on the interior, and inside the box
@@ -307,6 +347,8 @@ def main():
                     help="both: plain MIC-PCG and the learned warm start (the headline value)")
     ap.add_argument("--weights", default=None, help="warm-start network (default: the committed one)")
     ap.add_argument("--no-moving", action="store_true", help="skip the moving-box step measurement")
+    ap.add_argument("--svd-snapshots", type=int, default=48,
+                    help="snapshots for the device snapshot-SVD measurement (0: skip)")
     a = ap.parse_args()
     rank, world, local = dist_env()
     if a.impl == "reference":
@@ -353,6 +395,7 @@ def main():
         gl.close()
         net.close()
     mov = None if a.no_moving else measure_moving(a, dist, res, prec, local, rank)
+    svd = measure_snapshot_svd(res, prec, local, rank, a.svd_snapshots) if a.svd_snapshots > 0 else None
     clk = clocks.stop()
     head = lrn if lrn is not None else plain
     ms_max, value, iters = head["ms"], head["value"], head["iters"]
@@ -409,6 +452,7 @@ def main():
                            "unit": "GB/s", "frac": (achieved_solve / peak) if achieved_solve else None,
                            "bytes_model": "N_int*(5S+2P+2 + iters*(16S+2P+3)) per solve"},
         "moving_box": moving_record(mov, res, N, nint, S, peak, a.steps) if mov else None,
+        "snapshot_svd": svd_record(svd, 2 * 2 * 152 * 2.070e9 / 1e12) if svd else None,
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": nbox * 8,
                 "d2h_bytes_per_step": 3 * N * 8},
         "clocks": clk,

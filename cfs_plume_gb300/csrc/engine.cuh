@@ -684,6 +684,19 @@ class EngineT : public Engine {
 
   void use_cg_graph(bool on) override { no_cg_graph_ = !on; }
   const void* device_field(int field) override { return scalar_ptr(field); }
+  bool device_vector(int field, const void* planes[3]) override {
+    const bool cached = field == PLUME_F_PREVORTICITY || field == PLUME_F_POSTADVECTION ||
+                        field == PLUME_F_PREPROJECTION || field == PLUME_F_FORCE ||
+                        field == PLUME_F_POST_IOP;
+    if (cached && !p_.cache_fields) return false;
+    if (field == PLUME_F_POST_IOP && !has_iop_) return false;
+    V3<T> v;
+    if (!vector_ref(field, v) || !v.x) return false;
+    planes[0] = v.x;
+    planes[1] = v.y;
+    planes[2] = v.z;
+    return true;
+  }
   void* stream_handle() override { return (void*)s_; }
   int attach_net(NetRuntime* net) override {
     PL_TRY(cudaStreamSynchronize(s_));

@@ -56,6 +56,10 @@ class Engine {
   // engine's precision), the engine's cudaStream_t, and the network used by
   // PLUME_WARM_LEARNED solves (nullptr detaches).
   virtual const void* device_field(int field) = 0;
+  // The three device planes (x, y, z) of a vector field, nullptr-free only
+  // when the field is kept (cached fields need cache_fields; postIOP a moving
+  // step); false otherwise.
+  virtual bool device_vector(int field, const void* planes[3]) = 0;
   virtual void* stream_handle() = 0;
   virtual int attach_net(NetRuntime* net) = 0;
   // CG loop as a CUDA graph (default) or driven from the host; many handles

@@ -373,10 +373,12 @@ struct Runner {
   JacobiCtl* ctl = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int sweeps = 0;
+  bool owns_a = true;  // false: A belongs to a plume_snapshots object
   std::string err;
 
   ~Runner() {
     if (s) cudaStreamSynchronize(s);
+    if (!owns_a) A = nullptr;
     double* bufs[] = {A, R, partial, dot, inv, W, sigma, sigma_sorted, UR, U};
     for (double* b : bufs)
       if (b) cudaFree(b);
@@ -386,7 +388,7 @@ struct Runner {
     if (s) cudaStreamDestroy(s);
   }
 
-  int init(int device, size_t n_, int m_) {
+  int init(int device, size_t n_, int m_, double* external_a = nullptr) {
     n = n_;
     m = m_;
     if (n < 1 || m < 1) {
@@ -401,7 +403,12 @@ struct Runner {
     SVD_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     for (auto& e : ev) SVD_TRY(cudaEventCreate(&e));
     const size_t mm = (size_t)m * m;
-    SVD_TRY(cudaMalloc(&A, n * m * sizeof(double)));
+    if (external_a) {
+      A = external_a;
+      owns_a = false;
+    } else {
+      SVD_TRY(cudaMalloc(&A, n * m * sizeof(double)));
+    }
     SVD_TRY(cudaMalloc(&R, mm * sizeof(double)));
     SVD_TRY(cudaMalloc(&W, mm * sizeof(double)));
     SVD_TRY(cudaMalloc(&UR, mm * sizeof(double)));
@@ -614,10 +621,219 @@ int write_u(const std::string& path, const double* U, size_t n, int kept, cudaSt
   return PLUME_OK;
 }
 
+// ---- peeled copies of a handle's field into a snapshot column ---------------
+// appendStreams' peelBoundary().flattened() (VECTOR3_FIELD_3D.cpp:3139-3151,
+// 3222-3232; FIELD_3D.cpp:6679-6689, 6722-6733): interior cells, x fastest,
+// vector components interleaved; FP32 fields widen exactly to FP64.
+template <typename T>
+__global__ void k_peel(int X, int Y, int Z, const T* a, const T* b, const T* c, int comps, double* out) {
+  const long long nx = X - 2, ny = Y - 2, nint = nx * ny * (Z - 2);
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nint;
+       k += (long long)gridDim.x * blockDim.x) {
+    const long long x = k % nx, t = k / nx, y = t % ny, z = t / ny;
+    const size_t cell = (size_t)(x + 1) + (size_t)(y + 1) * X + (size_t)(z + 1) * X * Y;
+    if (comps == 1) {
+      out[k] = (double)a[cell];
+    } else {
+      out[3 * k] = (double)a[cell];
+      out[3 * k + 1] = (double)b[cell];
+      out[3 * k + 2] = (double)c[cell];
+    }
+  }
+}
+
+__global__ void k_sumsq(const double* v, size_t n, double* partial) {
+  __shared__ double sh[kWarps];
+  double s = 0.0;
+  for (size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x; r < n; r += (size_t)gridDim.x * blockDim.x)
+    s = fma(v[r], v[r], s);
+  s = warp_sum(s);
+  if (threadIdx.x % 32 == 0) sh[threadIdx.x / 32] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kWarps; w++) t += sh[w];
+    partial[blockIdx.x] = t;
+  }
+}
+
+constexpr int kNormBlocks = 1024;
+
 }  // namespace svd
 }  // namespace plume
 
 using namespace plume::svd;
+
+struct plume_snapshots {
+  plume_handle* h = nullptr;
+  int stream = 0;
+  int capacity = 0;
+  int count = 0;
+  int device = 0;
+  size_t n = 0;
+  double* A = nullptr;
+  double* partial = nullptr;
+  double* total = nullptr;
+};
+
+namespace {
+
+// The fields of one appendStreams call for a stream (FLUID_3D_MIC.cpp:1402-1461)
+int stream_fields(int stream, int fields[2]) {
+  switch (stream) {
+    case PLUME_STREAM_FINAL: fields[0] = PLUME_F_VELOCITY; return 1;
+    case PLUME_STREAM_PREPROJECT: fields[0] = PLUME_F_PREPROJECTION; return 1;
+    case PLUME_STREAM_PREDIFFUSE: fields[0] = PLUME_F_PREDIFFUSION; return 1;
+    case PLUME_STREAM_PREADVECT: fields[0] = PLUME_F_PREADVECTION; return 1;
+    case PLUME_STREAM_IOP: fields[0] = PLUME_F_POST_IOP; return 1;
+    case PLUME_STREAM_PRESSURE:
+      fields[0] = PLUME_F_PRESSURE;
+      fields[1] = PLUME_F_DIVERGENCE;
+      return 2;
+    default: return 0;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int plume_snapshots_create(plume_handle* h, int32_t stream, int32_t capacity, plume_snapshots** out) {
+  if (!h || !out || capacity < 1 || capacity > 2048) return fail(PLUME_ERR_INVALID, "bad argument");
+  int f[2];
+  if (!stream_fields(stream, f)) return fail(PLUME_ERR_INVALID, "unknown stream");
+  *out = nullptr;
+  plume::Engine* e = plume::engine_of(h);
+  const plume_params& p = e->params();
+  const size_t nint = (size_t)(p.res[0] - 2) * (p.res[1] - 2) * (p.res[2] - 2);
+  std::unique_ptr<plume_snapshots> s(new plume_snapshots());
+  s->h = h;
+  s->stream = stream;
+  s->capacity = capacity;
+  s->device = p.device;
+  s->n = stream == PLUME_STREAM_PRESSURE ? nint : 3 * nint;
+  if (cudaSetDevice(p.device) != cudaSuccess ||
+      cudaMalloc(&s->A, s->n * (size_t)capacity * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&s->partial, kNormBlocks * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&s->total, sizeof(double)) != cudaSuccess) {
+    plume_snapshots_destroy(s.release());
+    (void)cudaGetLastError();
+    return fail(PLUME_ERR_OOM, "snapshot matrix does not fit on the device");
+  }
+  *out = s.release();
+  return PLUME_OK;
+}
+
+void plume_snapshots_destroy(plume_snapshots* s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  for (double* b : {s->A, s->partial, s->total})
+    if (b) cudaFree(b);
+  delete s;
+}
+
+int plume_snapshots_append(plume_snapshots* s, int32_t* appended) {
+  if (!s) return fail(PLUME_ERR_INVALID, "null snapshots");
+  if (appended) *appended = 0;
+  plume::Engine* e = plume::engine_of(s->h);
+  const plume_params& p = e->params();
+  cudaStream_t st = (cudaStream_t)e->stream_handle();
+  int f[2];
+  const int nf = stream_fields(s->stream, f);
+  const bool fp32 = p.precision == PLUME_PREC_FP32;
+  for (int k = 0; k < nf; k++) {
+    if (s->count >= s->capacity) return fail(PLUME_ERR_STATE, "snapshot capacity reached");
+    const void* planes[3] = {nullptr, nullptr, nullptr};
+    int comps = 3;
+    if (s->stream == PLUME_STREAM_PRESSURE) {
+      planes[0] = e->device_field(f[k]);
+      comps = 1;
+    } else if (!e->device_vector(f[k], planes)) {
+      return fail(PLUME_ERR_STATE, "the stream's field is not kept (cache_fields = 0, or no moving step for postIOP)");
+    }
+    if (!planes[0]) return fail(PLUME_ERR_STATE, "the stream's field is not kept");
+    double* colp = s->A + (size_t)s->count * s->n;
+    const int grid = (int)std::min<size_t>((s->n / comps + kThreads - 1) / kThreads, 152 * 16);
+    if (fp32)
+      k_peel<float><<<grid, kThreads, 0, st>>>(p.res[0], p.res[1], p.res[2], (const float*)planes[0],
+                                               (const float*)planes[1], (const float*)planes[2], comps, colp);
+    else
+      k_peel<double><<<grid, kThreads, 0, st>>>(p.res[0], p.res[1], p.res[2], (const double*)planes[0],
+                                                (const double*)planes[1], (const double*)planes[2], comps, colp);
+    k_sumsq<<<kNormBlocks, kThreads, 0, st>>>(colp, s->n, s->partial);
+    k_reduce<<<1, kThreads, 0, st>>>(s->partial, kNormBlocks, 1, s->total, 0);
+    double t = 0.0;
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(&t, s->total, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return fail(PLUME_ERR_CUDA, "snapshot copy on the device failed");
+    if (std::sqrt(t) > 1e-7) {  // `if (velocity.norm2() > 1e-7)` (FLUID_3D_MIC.cpp:1404)
+      s->count++;
+      if (appended) ++*appended;
+    }
+  }
+  return PLUME_OK;
+}
+
+int plume_snapshots_dims(plume_snapshots* s, int32_t* rows, int32_t* cols) {
+  if (!s) return fail(PLUME_ERR_INVALID, "null snapshots");
+  if (rows) *rows = s->count;
+  if (cols) *cols = (int32_t)s->n;
+  return PLUME_OK;
+}
+
+int plume_snapshots_download(plume_snapshots* s, double* dst, size_t n) {
+  if (!s || !dst || n != s->n * (size_t)s->count) return fail(PLUME_ERR_INVALID, "bad argument");
+  if (n && cudaMemcpy(dst, s->A, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(PLUME_ERR_CUDA, "download failed");
+  return PLUME_OK;
+}
+
+int plume_snapshots_svd(plume_snapshots* s, double discard_threshold, const char* u_path, const char* pca_path,
+                        double* pca_out, int32_t* kept_out, plume_svd_info* info) {
+  if (!s) return fail(PLUME_ERR_INVALID, "null snapshots");
+  if (s->count < 1) return fail(PLUME_ERR_STATE, "no snapshots held");
+  cudaStreamSynchronize((cudaStream_t)plume::engine_of(s->h)->stream_handle());
+  Runner r;
+  int rc = r.init(s->device, s->n, s->count, s->A);
+  if (rc == PLUME_OK) rc = r.qr();
+  if (rc == PLUME_OK) rc = r.svd_r();
+  std::vector<double> pca;
+  if (rc == PLUME_OK) rc = r.pca(pca);
+  int kept = 0;
+  if (rc == PLUME_OK) {
+    kept = kept_columns(pca, discard_threshold);
+    rc = r.form_u(u_path ? kept : 0, true);
+  }
+  if (rc == PLUME_OK && cudaStreamSynchronize(r.s) != cudaSuccess) {
+    r.err = "U = Q U_R failed";
+    rc = PLUME_ERR_CUDA;
+  }
+  const int m = s->count;
+  s->count = 0;  // the columns now hold Q
+  if (rc != PLUME_OK) return fail(rc, r.err);
+  const auto t0 = std::chrono::steady_clock::now();
+  if (pca_path && !write_vector(pca_path, pca)) return fail(PLUME_ERR_IO, std::string("could not write ") + pca_path);
+  if (u_path) {
+    rc = write_u(u_path, r.U, s->n, kept, r.s, r.err);
+    if (rc != PLUME_OK) return fail(rc, r.err);
+  }
+  if (pca_out) memcpy(pca_out, pca.data(), m * sizeof(double));
+  if (kept_out) *kept_out = kept;
+  if (info) {
+    info->rows = (int32_t)s->n;
+    info->cols = m;
+    info->kept = kept;
+    info->sweeps = r.sweeps;
+    info->ms_qr = r.ms(0, 1);
+    info->ms_svd = r.ms(1, 2);
+    info->ms_u = r.ms(2, 3);
+    info->ms_io = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return PLUME_OK;
+}
+
+}  // extern "C"
 
 extern "C" {
 

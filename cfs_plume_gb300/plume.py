@@ -80,6 +80,13 @@ def load_library(path=LIB_PATH):
         "plume_svd_columns": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                         C.c_void_p, C.c_void_p, P(C.c_int32), P(PlumeSvdInfo)]),
         "plume_svd_verify": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, C.c_void_p]),
+        "plume_snapshots_create": (C.c_int, [H, C.c_int32, C.c_int32, P(H)]),
+        "plume_snapshots_destroy": (None, [H]),
+        "plume_snapshots_append": (C.c_int, [H, P(C.c_int32)]),
+        "plume_snapshots_dims": (C.c_int, [H, P(C.c_int32), P(C.c_int32)]),
+        "plume_snapshots_download": (C.c_int, [H, C.c_void_p, C.c_size_t]),
+        "plume_snapshots_svd": (C.c_int, [H, C.c_double, C.c_char_p, C.c_char_p, C.c_void_p,
+                                          P(C.c_int32), P(PlumeSvdInfo)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -461,3 +468,53 @@ def svd_verify(prefix, u_path, count=10, device=0):
     d = np.empty(count)
     _check(lib.plume_svd_verify(os.fsencode(prefix), os.fsencode(u_path), count, device, d.ctypes.data))
     return d
+
+
+STREAMS = {"final": 0, "preproject": 1, "prediffuse": 2, "preadvect": 3, "iop": 4, "pressure": 5}
+
+
+class Snapshots:
+    """Rows of one appendStreams stream kept in device memory
+    (plume_snapshots, include/plume_svd.h)."""
+
+    def __init__(self, plume, stream, capacity):
+        self.lib = load_library()
+        self.plume = plume
+        h = C.c_void_p()
+        _check(self.lib.plume_snapshots_create(plume.h, STREAMS[stream], capacity, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.plume_snapshots_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def append(self):
+        n = C.c_int32()
+        _check(self.lib.plume_snapshots_append(self.h, C.byref(n)))
+        return n.value
+
+    def dims(self):
+        r, c = C.c_int32(), C.c_int32()
+        _check(self.lib.plume_snapshots_dims(self.h, C.byref(r), C.byref(c)))
+        return r.value, c.value
+
+    def rows(self):
+        r, c = self.dims()
+        a = np.empty((r, c))
+        _check(self.lib.plume_snapshots_download(self.h, a.ctypes.data, a.size))
+        return a
+
+    def svd(self, discard_threshold=1e-9, u_path=None, pca_path=None):
+        """Factor the held rows (consumed): (pca values, kept, info dict)."""
+        r, _ = self.dims()
+        pca = np.empty(max(r, 1))
+        kept = C.c_int32()
+        info = PlumeSvdInfo()
+        enc = lambda v: None if v is None else os.fsencode(v)
+        _check(self.lib.plume_snapshots_svd(self.h, discard_threshold, enc(u_path), enc(pca_path),
+                                            pca.ctypes.data, C.byref(kept), C.byref(info)))
+        return pca[:r], kept.value, {f: getattr(info, f) for f, _ in PlumeSvdInfo._fields_}

@@ -36,6 +36,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "plume.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -74,6 +76,42 @@ int plume_svd_columns(const double* columns, int32_t n, int32_t m, double discar
    (EIGEN::read layout), computed on the GPU.  diffs: count doubles. */
 int plume_svd_verify(const char* prefix, const char* u_path, int32_t count, int32_t device,
                      double* diffs);
+
+/* ---- snapshots kept in HBM: the streams without the disk round trip ----
+ * A plume_snapshots object collects, from one plume handle, the rows that
+ * FLUID_3D_MIC::appendStreams (FLUID_3D_MIC.cpp:1329-1477) would append to
+ * one stream file -- the peeled field (interior cells, x fastest, vector
+ * components interleaved), kept only when its 2-norm exceeds 1e-7 -- as
+ * FP64 columns of a device matrix, and factors them in place with the same
+ * SVD as plume_svd_stream. */
+typedef enum plume_stream {
+  PLUME_STREAM_FINAL = 0,   /* velocity            (velocity.final.matrix)      */
+  PLUME_STREAM_PREPROJECT,  /* preprojection       (velocity.preproject.matrix) */
+  PLUME_STREAM_PREDIFFUSE,  /* prediffusion        (velocity.prediffuse.matrix) */
+  PLUME_STREAM_PREADVECT,   /* preadvection        (velocity.preadvect.matrix)  */
+  PLUME_STREAM_IOP,         /* postIOP             (velocity.iop.matrix)        */
+  PLUME_STREAM_PRESSURE     /* pressure, then divergence (pressure.matrix)      */
+} plume_stream;
+
+typedef struct plume_snapshots plume_snapshots;
+
+/* Room for `capacity` rows of the handle's `stream` on the handle's device.
+   The handle must outlive the object. */
+int plume_snapshots_create(plume_handle* h, int32_t stream, int32_t capacity, plume_snapshots** out);
+void plume_snapshots_destroy(plume_snapshots* s);
+/* Appends this step's rows (waits for the handle's stream); *appended = rows
+   kept (0..2).  PLUME_ERR_STATE when the field is not kept or the capacity is
+   reached. */
+int plume_snapshots_append(plume_snapshots* s, int32_t* appended);
+/* rows = snapshots held, cols = values per snapshot (the stream's dims). */
+int plume_snapshots_dims(plume_snapshots* s, int32_t* rows, int32_t* cols);
+/* The held rows in the stream file's layout (rows * cols doubles). */
+int plume_snapshots_download(plume_snapshots* s, double* dst, size_t n);
+/* BIG_MATRIX::outOfCoreSVD + writeFinalU on the held rows, which it consumes
+   (the matrix becomes Q; the object is empty afterwards).  u_path / pca_path
+   may be NULL (not written); pca (rows doubles) and kept may be NULL. */
+int plume_snapshots_svd(plume_snapshots* s, double discard_threshold, const char* u_path,
+                        const char* pca_path, double* pca, int32_t* kept, plume_svd_info* info);
 
 #ifdef __cplusplus
 }

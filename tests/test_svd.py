@@ -168,3 +168,43 @@ def test_svd_columns_deterministic():
     a = plume.svd_columns(A, 1e-9)
     b = plume.svd_columns(A, 1e-9)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_device_snapshots_equal_stream_files_and_their_svd(tmp_path, precision):
+    """Rows kept in device memory (plume_snapshots) equal the stream files that
+    plume_append_streams writes, for all six streams of a moving-box run, and
+    their in-place SVD equals plume_svd_stream on those files."""
+    from cfs_plume_gb300 import _abi, plume
+    prec = _abi.PREC_FP64 if precision == "fp64" else _abi.PREC_FP32
+    g = plume.Plume(_abi.default_params(res=(14, 16, 12), vorticity_eps=1.0, precision=prec))
+    box = plume.BOX((0.5, 0.35, 0.5), (0.4, 0.3, 0.35), 2.0, 3.0)
+    box.set_dt(0.1)
+    snaps = {t: plume.Snapshots(g, t, 64) for t in TAGS}
+    d = str(tmp_path / "snap_") + "/"
+    os.makedirs(d)
+    for s in range(10):
+        g.add_source(s)
+        g.step_moving_box(box)
+        box.spin()
+        box.translate_center()
+        g.append_streams(d)
+        for sn in snaps.values():
+            sn.append()
+    red, scr = str(tmp_path / "red") + "/", str(tmp_path / "scr") + "/"
+    os.makedirs(red)
+    os.makedirs(scr)
+    for name, tag in zip(NAMES, TAGS):
+        pre = d + name + ".matrix"
+        A, rows, cols = S.read_stream(pre)
+        held = snaps[tag].rows()
+        assert held.shape == (rows, cols), tag
+        assert np.array_equal(held, A.T), tag
+        info = plume.svd_stream(pre, red, scr, 1e-9, red + "U." + tag + ".matrix")
+        pca, kept, info2 = snaps[tag].svd(1e-9, u_path=red + "Ud." + tag + ".matrix")
+        assert kept == info["kept"], tag
+        assert np.array_equal(S.read_u(red + "U." + tag + ".matrix"), S.read_u(red + "Ud." + tag + ".matrix")), tag
+        assert snaps[tag].dims()[0] == 0
+    for sn in snaps.values():
+        sn.close()
