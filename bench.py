@@ -26,6 +26,7 @@ import json
 import math
 import os
 import statistics
+import struct
 import subprocess
 import sys
 import tempfile
@@ -291,6 +292,71 @@ def measure_snapshot_svd(res, prec, local, rank, snaps):
     return {"rows": rows, "cols": cols, "kept": kept, "info": info, "wall_s": wall}
 
 
+def _write_eigen(path, M):
+    """EIGEN::write layout: int32 rows, cols, then the row-major doubles."""
+    with open(path, "wb") as f:
+        f.write(struct.pack("<ii", M.shape[0], M.shape[1]))
+        M.astype("<f8").tofile(f)
+
+
+def measure_reduced(steps, local, rank, res=(64, 96, 64), rank_r=32, points=2000):
+    """stepReorderedCubatureStam on the GPU with a synthetic reduced model of
+    the reference's file layout (seeded random bases of rank 32, damping 0.99 I,
+    ptof I, inverseProduct 0, 2000 seeded cubature cells), FP32 plume fields."""
+    import numpy as np
+    import shutil
+    from cfs_plume_gb300 import _abi
+    from cfs_plume_gb300.plume import Plume, ReducedModel
+    nint = (res[0] - 2) * (res[1] - 2) * (res[2] - 2)
+    n = 3 * nint
+    rng = np.random.default_rng(7 + rank)
+    d = tempfile.mkdtemp(prefix="plume_reduced_bench_")
+    try:
+        for fn in ("U.preadvect.matrix", "U.final.matrix", "U.prediffuse.matrix"):
+            _write_eigen(os.path.join(d, fn), rng.standard_normal((n, rank_r)) / math.sqrt(n))
+        _write_eigen(os.path.join(d, "damping.peeled.matrix"), 0.99 * np.eye(rank_r))
+        _write_eigen(os.path.join(d, "projected.ptof.matrix"), np.eye(rank_r))
+        _write_eigen(os.path.join(d, "inverseProduct.matrix"), np.zeros((rank_r, rank_r)))
+        cells = np.sort(rng.choice(nint, points, replace=False)).astype("<i4")
+        with open(os.path.join(d, "cubature"), "wb") as f:
+            f.write(struct.pack("<i", points))
+            cells.tofile(f)
+            np.full(points, nint / points, dtype="<f8").tofile(f)
+        g = Plume(_abi.plume_config(res, precision=_abi.PREC_FP32, seed=rank, device=local))
+        m = ReducedModel(g, d)
+        for s in range(3):
+            g.add_source(s)
+            m.step()
+        tot = red = 0.0
+        launches = 0
+        for s in range(steps):
+            g.add_source(3 + s)
+            st = m.step()
+            tot += st.ms_total
+            red += st.ms_solve
+            launches += st.launches
+        m.close()
+        g.close()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return {"res": res, "n": n, "r": rank_r, "points": points, "ms_total": tot / steps, "ms_reduced": red / steps,
+            "launches": launches / steps}
+
+
+def reduced_record(r, peak):
+    # the reduced part reads U_pa and U_f once each (n x r doubles), the
+    # peeled velocity (3 N_int floats) and writes it back
+    bytes_red = 2 * r["n"] * r["r"] * 8 + 2 * r["n"] * 4
+    ach = bytes_red / (r["ms_reduced"] / 1000.0) / 1e9 if r["ms_reduced"] > 0 else None
+    return {"workload": "stepReorderedCubatureStam, plume %dx%dx%d FP32 fields, synthetic reduced model: rank %d "
+                        "bases (FP64), %d cubature points" % (tuple(r["res"]) + (r["r"], r["points"])),
+            "value": 1000.0 / r["ms_total"], "unit": "steps/s", "ms_per_step": r["ms_total"],
+            "ms_reduced_part": r["ms_reduced"], "launches_per_step": r["launches"],
+            "roofline": {"bound": "hbm", "kernel": "reduced part (projection, cubature, unprojection)",
+                         "achieved": ach, "peak": peak, "unit": "GB/s", "frac": (ach / peak) if ach else None,
+                         "bytes_model": "2 n r 8 + 2 n 4 per step (n = 3 N_int)"}}
+
+
 def svd_record(r, fp64_peak_tflops):
     n, m = r["cols"], r["rows"]
     info = r["info"]
@@ -349,6 +415,7 @@ def main():
     ap.add_argument("--no-moving", action="store_true", help="skip the moving-box step measurement")
     ap.add_argument("--svd-snapshots", type=int, default=48,
                     help="snapshots for the device snapshot-SVD measurement (0: skip)")
+    ap.add_argument("--no-reduced", action="store_true", help="skip the reduced-step measurement")
     a = ap.parse_args()
     rank, world, local = dist_env()
     if a.impl == "reference":
@@ -396,6 +463,7 @@ def main():
         net.close()
     mov = None if a.no_moving else measure_moving(a, dist, res, prec, local, rank)
     svd = measure_snapshot_svd(res, prec, local, rank, a.svd_snapshots) if a.svd_snapshots > 0 else None
+    red = None if a.no_reduced else measure_reduced(a.steps, local, rank)
     clk = clocks.stop()
     head = lrn if lrn is not None else plain
     ms_max, value, iters = head["ms"], head["value"], head["iters"]
@@ -453,6 +521,7 @@ def main():
                            "bytes_model": "N_int*(5S+2P+2 + iters*(16S+2P+3)) per solve"},
         "moving_box": moving_record(mov, res, N, nint, S, peak, a.steps) if mov else None,
         "snapshot_svd": svd_record(svd, 2 * 2 * 152 * 2.070e9 / 1e12) if svd else None,
+        "reduced_step": reduced_record(red, peak) if red else None,
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": nbox * 8,
                 "d2h_bytes_per_step": 3 * N * 8},
         "clocks": clk,

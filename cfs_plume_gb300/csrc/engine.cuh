@@ -407,6 +407,40 @@ class EngineT : public Engine {
 
   bool has_iop() const override { return has_iop_; }
 
+  // The full-space stages of SUBSPACE_FLUID_3D_EIGEN::stepReorderedCubatureStam
+  // (SUBSPACE_FLUID_3D_EIGEN.cpp:247-266): velocity walls (density is left
+  // as it is), buoyancy, vorticity confinement, then advectHeatAndDensityStam
+  // (lines 573-601): the velocity's face conditions, density and heat advected
+  // with it, their borders zeroed.  The velocity itself is advected in reduced
+  // coordinates by the caller.
+  int reduced_prestep() override {
+    const int gN = grid_for(g_.N);
+    const int nfaces = 2 * (g_.Y * g_.Z + g_.X * g_.Z + g_.X * g_.Y);
+    const int gF = grid_for(nfaces);
+    launches_ = 0;
+    PL_TRY(cudaEventRecord(ev_[0], s_));
+    k_forces<T><<<gN, 256, 0, s_>>>(g_, vel_, nullptr, heat_, prevort_, c_, 0);
+    PL_CHECK_LAUNCH();
+    if (c_.has_vort) {
+      k_vort1<T><<<gN, 256, 0, s_>>>(g_, vel_, vort_, mag_, c_);
+      PL_CHECK_LAUNCH();
+      k_vort2<T><<<gN, 256, 0, s_>>>(g_, vel_, vort_, mag_, force_, c_, 0);
+      PL_CHECK_LAUNCH();
+    }
+    const int ox = p_.bc[2] == 0, oy = p_.bc[4] == 0, oz = p_.bc[0] == 0;
+    k_face_bc<T><<<gF, 256, 0, s_>>>(g_, vel_, ox ? 1 : 0, oy ? 1 : 0, oz ? 1 : 0);
+    PL_CHECK_LAUNCH();
+    std::swap(dens_, dens_old_);
+    std::swap(heat_, heat_old_);
+    k_advect<T><<<gN, 256, 0, s_>>>(g_, c_, vel_, dens_old_, heat_old_, vel_, dens_, heat_, postadv_, 0, ox,
+                                    oy, oz, 0);
+    PL_CHECK_LAUNCH();
+    total_time_ += 0.1;  // SUBSPACE_FLUID_3D_EIGEN.cpp:298
+    total_steps_ += 1;
+    return PLUME_OK;
+  }
+  int reduced_launches() const override { return launches_; }
+
   int download_iop(uint8_t* inside, double* values, size_t n) override {
     const size_t N = (size_t)g_.N;
     if (n != N) return fail(PLUME_ERR_INVALID, "the obstacle matrix needs N cells");

@@ -33,6 +33,10 @@ class Engine {
   virtual int step_moving_box(const plume_box& box, plume_step_stats* stats) = 0;
   virtual int set_initial_velocity_box(const plume_box& box) = 0;
   virtual bool has_iop() const = 0;
+  // Full-space part of the reduced step (include/plume_reduced.h) on the
+  // engine's stream; kernels launched since its start.
+  virtual int reduced_prestep() = 0;
+  virtual int reduced_launches() const = 0;
   virtual int run_moving_timed(plume_box& box, int32_t first_step, int32_t n, double* ms,
                                plume_step_stats* stats) = 0;
   // with sweep profiling on: summed device ms and launches of the stomp kernel

@@ -99,7 +99,7 @@ __global__ void k_forces(Grid g, V3<T> vel, T* dens, const T* heat, V3<T> prevor
     T vx = vel.x[i], vy = vel.y[i], vz = vel.z[i];
     if (on_border(g, x, y, z)) {
       vx = vy = vz = T(0);
-      dens[i] = T(0);
+      if (dens) dens[i] = T(0);  // null: the reduced step leaves density alone
     }
     if (c.has_beta) {
       const T fy = c.beta * heat[i];
@@ -307,13 +307,19 @@ __device__ inline Trilinear<T> backtrace(const Grid& g, const StepConsts<T>& c, 
 template <typename T>
 __global__ void k_advect(Grid g, StepConsts<T> c, V3<T> vo, const T* dens_o, const T* heat_o,
                          V3<T> vn, T* dens_n, T* heat_n, V3<T> postadv, int cache,
-                         int open_x, int open_y, int open_z) {
+                         int open_x, int open_y, int open_z, int vel_out = 1) {
   PL_GRID_STRIDE(i, g.N) {
     const int x = i % g.X;
     const int t = i / g.X;
     const int y = t % g.Y;
     const int z = t / g.Y;
     const Trilinear<T> w = backtrace(g, c, vo, i, x, y, z);
+    if (!vel_out) {  // advectHeatAndDensityStam: the scalars alone
+      const bool b = on_border(g, x, y, z);
+      dens_n[i] = b ? T(0) : w.apply(dens_o);
+      heat_n[i] = b ? T(0) : w.apply(heat_o);
+      continue;
+    }
     const T ux = w.apply(vo.x), uy = w.apply(vo.y), uz = w.apply(vo.z);
     if (cache) {
       postadv.x[i] = ux;

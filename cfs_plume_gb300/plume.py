@@ -80,6 +80,11 @@ def load_library(path=LIB_PATH):
         "plume_svd_columns": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                         C.c_void_p, C.c_void_p, P(C.c_int32), P(PlumeSvdInfo)]),
         "plume_svd_verify": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, C.c_void_p]),
+        "plume_reduced_create": (C.c_int, [H, C.c_char_p, P(H)]),
+        "plume_reduced_destroy": (None, [H]),
+        "plume_reduced_step": (C.c_int, [H, P(PlumeStepStats)]),
+        "plume_reduced_qdot": (C.c_int, [H, C.c_void_p, C.c_int32, P(C.c_int32)]),
+        "plume_reduced_dims": (C.c_int, [H, P(C.c_int32)]),
         "plume_snapshots_create": (C.c_int, [H, C.c_int32, C.c_int32, P(H)]),
         "plume_snapshots_destroy": (None, [H]),
         "plume_snapshots_append": (C.c_int, [H, P(C.c_int32)]),
@@ -478,6 +483,7 @@ class Snapshots:
     (plume_snapshots, include/plume_svd.h)."""
 
     def __init__(self, plume, stream, capacity):
+        self.h = None
         self.lib = load_library()
         self.plume = plume
         h = C.c_void_p()
@@ -518,3 +524,43 @@ class Snapshots:
         _check(self.lib.plume_snapshots_svd(self.h, discard_threshold, enc(u_path), enc(pca_path),
                                             pca.ctypes.data, C.byref(kept), C.byref(info)))
         return pca[:r], kept.value, {f: getattr(info, f) for f, _ in PlumeSvdInfo._fields_}
+
+
+class ReducedModel:
+    """A reduced (subspace) model attached to a plume handle
+    (plume_reduced, include/plume_reduced.h): step() is the reference's
+    stepReorderedCubatureStam on the handle's state."""
+
+    def __init__(self, plume, reduced_path):
+        self.h = None
+        self.lib = load_library()
+        self.plume = plume
+        d = reduced_path if reduced_path.endswith("/") else reduced_path + "/"
+        h = C.c_void_p()
+        _check(self.lib.plume_reduced_create(plume.h, os.fsencode(d), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.plume_reduced_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def step(self, stats=True):
+        st = PlumeStepStats()
+        _check(self.lib.plume_reduced_step(self.h, C.byref(st) if stats else None))
+        return st if stats else None
+
+    def qdot(self):
+        n = C.c_int32()
+        _check(self.lib.plume_reduced_qdot(self.h, None, 0, C.byref(n)))
+        q = np.empty(n.value)
+        _check(self.lib.plume_reduced_qdot(self.h, q.ctypes.data, n.value, C.byref(n)))
+        return q
+
+    def dims(self):
+        d = (C.c_int32 * 5)()
+        _check(self.lib.plume_reduced_dims(self.h, d))
+        return dict(preadvect=d[0], prediffuse=d[1], preproject=d[2], final=d[3], cubature_points=d[4])

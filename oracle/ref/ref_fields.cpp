@@ -612,3 +612,73 @@ void BOX::translate_center() {
   _displacement[0] = 0.25 * sin(_phi);
   _center[0] = _original_center[0] + _displacement[0];
 }
+
+// BOX.cpp:43-45
+BOX::BOX() {}
+
+// --------------------------------------------- members the reduced step calls
+// FIELD_3D.cpp:6753-6764
+VectorXd FIELD_3D::flattenedEigen() const {
+  VectorXd final(_totalCells);
+  int index = 0;
+  for (int z = 0; z < _zRes; z++)
+    for (int y = 0; y < _yRes; y++)
+      for (int x = 0; x < _xRes; x++, index++) final[index] = (*this)(x, y, z);
+  return final;
+}
+
+// VECTOR3_FIELD_3D.cpp:3434-3553: U^T times the peeled field (x fastest,
+// components interleaved), accumulated in the reference's grouping: per row
+// (y, z) four partial sums over x = 0, 4, ... (and x + 1, + 2, + 3), added to
+// the total in that order, then the leftover x one at a time.
+VectorXd VECTOR3_FIELD_3D::peeledProject(const MatrixXd& U) {
+  const int xPeeled = _xRes - 2;
+  const int slabPeeled = (_xRes - 2) * (_yRes - 2);
+  const int totalColumns = U.cols();
+  VectorXd final = VectorXd::Zero(totalColumns);
+  VectorXd unroll[4];
+  for (int k = 0; k < 4; k++) unroll[k].resize(totalColumns);
+  const int stride = 4;
+  for (int z = 0; z < _zRes - 2; z++) {
+    const int zCached = 3 * z * slabPeeled;
+    for (int y = 0; y < _yRes - 2; y++) {
+      const int yzCached = 3 * y * xPeeled + zCached;
+      const int xEnd = (_xRes - 2) / stride * stride;
+      for (int k = 0; k < 4; k++) unroll[k].setZero();
+      for (int x = 0; x < xEnd; x += stride)
+        for (int k = 0; k < 4; k++) {
+          const int index = 3 * (x + k) + yzCached;
+          const VEC3F v3 = (*this)(x + k + 1, y + 1, z + 1);
+          const Vector3d v(v3[0], v3[1], v3[2]);
+          unroll[k].noalias() += U.block(index, 0, 3, totalColumns).transpose() * v;
+        }
+      for (int k = 0; k < 4; k++) final.noalias() += unroll[k];
+      for (int x = xEnd; x < _xRes - 2; x++) {
+        const int index = 3 * x + yzCached;
+        const VEC3F v3 = (*this)(x + 1, y + 1, z + 1);
+        const Vector3d v(v3[0], v3[1], v3[2]);
+        final.noalias() += U.block(index, 0, 3, totalColumns).transpose() * v;
+      }
+    }
+  }
+  return final;
+}
+
+// VECTOR3_FIELD_3D.cpp:3558-3605: each peeled cell = (U row 3i, 3i+1, 3i+2) . q
+void VECTOR3_FIELD_3D::peeledUnproject(const MatrixXd& U, const VectorXd& q) {
+  const int xPeeled = _xRes - 2;
+  const int slabPeeled = (_xRes - 2) * (_yRes - 2);
+  for (int z = 0; z < _zRes - 2; z++) {
+    const int zCached = 3 * z * slabPeeled;
+    for (int y = 0; y < _yRes - 2; y++) {
+      const int yzCached = 3 * y * xPeeled + zCached;
+      for (int x = 0; x < _xRes - 2; x++) {
+        const int index = 3 * x + yzCached;
+        const Real fx = U.row(index).dot(q);
+        const Real fy = U.row(index + 1).dot(q);
+        const Real fz = U.row(index + 2).dot(q);
+        (*this)(x + 1, y + 1, z + 1) = VEC3F(fx, fy, fz);
+      }
+    }
+  }
+}

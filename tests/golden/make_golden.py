@@ -22,11 +22,18 @@ configurations and stores what it produced:
   ref_svd_10x12x8.npz   the reference's svdOutOfCoreMultiple (oracle/_ref/svd_ref,
                         its own main) on the six streams of a 12-step moving-box
                         run: the input streams, every U.*.matrix and every
-                        singular-value vector.
+                        singular-value vector;
+  ref_reduced_<case>.npz  the reference's reduced step (oracle/_ref/reduced_ref:
+                        SUBSPACE_FLUID_3D_EIGEN, stepReorderedCubatureStam) on
+                        bases that svd_ref built from a 12-step plume: the
+                        reduced-path files it read or wrote (bases, projected
+                        operators, cubature, cubature cache) and the fields,
+                        reduced coordinates and ground-truth errors after 12
+                        reduced steps.
 
 Needs the reference tree (PLUME_REFERENCE_DIR, default /root/reference) and
 writes nothing outside tests/golden/.
-Usage: python tests/golden/make_golden.py [plume|moving|svd]   (default: all)
+Usage: python tests/golden/make_golden.py [plume|moving|svd|reduced]   (default: all)
 """
 import os
 import shutil
@@ -126,6 +133,53 @@ def main():
         moving_fixtures()
     if what in ("all", "svd"):
         svd_fixtures()
+    if what in ("all", "reduced"):
+        reduced_fixtures()
+
+
+RED_REF = os.path.join(ROOT, "oracle", "_ref", "reduced_ref")
+RED_FILES = ["U.preadvect.matrix", "U.final.matrix", "U.prediffuse.matrix", "damping.peeled.matrix",
+             "projected.ptof.matrix", "inverseProduct.matrix", "cubature", "advection.cubature.cache"]
+
+
+def reduced_fixtures():
+    res, steps = (10, 12, 8), 12
+    nint = (res[0] - 2) * (res[1] - 2) * (res[2] - 2)
+    base = tempfile.mkdtemp(prefix="plume_golden_")
+    snap, red0, scr = base + "/snap_/", base + "/red/", base + "/scratch/"
+    os.makedirs(snap)
+    p = _abi.default_params(res=res, vorticity_eps=1.0)
+    # the full-rank run: streams for the bases, state files as ground truth
+    subprocess.run(ref_args(p, steps, "column", snap) + ["streams=1", "gz=1"], check=True,
+                   capture_output=True)
+    cfg = base + "/svd.cfg"
+    with open(cfg, "w") as f:
+        f.write("snapshot path = %s\nreduced path = %s\nscratch path = %s\nsimulation snapshots = %d\n"
+                "reduced snapshots = %d\ndiscard threshold = 1e-9\n" % (snap, red0, scr, steps, steps))
+    subprocess.run([SVD_REF, cfg], check=True, capture_output=True)
+    rng = np.random.default_rng(3)
+    sparse = np.sort(rng.choice(nint, 40, replace=False)).astype("<i4")
+    cases = {"exact_10x12x8": (np.arange(nint, dtype="<i4"), np.ones(nint)),
+             "sparse_10x12x8": (sparse, (nint / 40.0) * rng.uniform(0.5, 1.5, 40))}
+    for name, (cells, weights) in cases.items():
+        red = base + "/red_" + name + "/"
+        shutil.copytree(red0, red)
+        with open(red + "cubature", "wb") as f:
+            np.array([cells.size], dtype="<i4").tofile(f)
+            cells.astype("<i4").tofile(f)
+            np.asarray(weights, dtype="<f8").tofile(f)
+        out = base + "/out_" + name
+        subprocess.run([RED_REF, "res=%d,%d,%d" % res, "vorticity=1.0", "reduced=" + red, "truth=" + snap,
+                        "steps=%d" % steps, "out=" + out], check=True, capture_output=True)
+        rec = {"res": np.array(res), "steps": steps, "vorticity_eps": 1.0}
+        for fn in RED_FILES:
+            rec["file_" + fn] = np.fromfile(red + fn, dtype=np.uint8)
+        for k in ("velocity", "density", "heat", "qdot"):
+            rec[k] = np.fromfile(out + "." + k + ".f64")
+        rec["errors"] = np.fromfile(out + ".errors.f64").reshape(-1, 4)
+        np.savez_compressed(os.path.join(HERE, "ref_reduced_%s.npz" % name), **rec)
+        print("reduced", name, "qdot", rec["qdot"].size, "errors (last)", rec["errors"][-1])
+    shutil.rmtree(base)
 
 
 def svd_fixtures():

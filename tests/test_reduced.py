@@ -1,0 +1,139 @@
+"""The reduced step (include/plume_reduced.h) against the reference's own
+SUBSPACE_FLUID_3D_EIGEN::stepReorderedCubatureStam (oracle/_ref/reduced_ref,
+fixtures from tests/golden/make_golden.py): bases that the reference's
+svdOutOfCoreMultiple built from a 12-step 10x12x8 plume, the projected
+operators its constructor built, and two cubature schemes (every interior cell
+with weight 1, which makes the reduced advection an exact Galerkin projection;
+40 seeded cells with seeded weights).
+
+Tolerances: FP64 fields after 12 reduced steps within 1e-8 relative L2 of the
+reference's (the reduced products sum in a different order: Eigen's GEMV and
+block products against warp-level FMA reductions); the cubature cache built
+here byte-identical to the reference's; FP32 fields within 1e-3.
+"""
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ["exact_10x12x8", "sparse_10x12x8"]
+FILES = ["U.preadvect.matrix", "U.final.matrix", "U.prediffuse.matrix", "damping.peeled.matrix",
+         "projected.ptof.matrix", "inverseProduct.matrix", "cubature", "advection.cubature.cache"]
+
+
+def _fixture(case):
+    return np.load(os.path.join(GOLDEN, "ref_reduced_%s.npz" % case))
+
+
+def _matrix(raw):
+    hdr = np.frombuffer(raw[:8].tobytes(), dtype="<i4")
+    return np.frombuffer(raw[8:].tobytes(), dtype="<f8").reshape(int(hdr[0]), int(hdr[1]))
+
+
+def _write_model(z, d, with_cache=True):
+    os.makedirs(d, exist_ok=True)
+    for fn in FILES:
+        if fn == "advection.cubature.cache" and not with_cache:
+            continue
+        z["file_" + fn].tofile(os.path.join(d, fn))
+
+
+def rel_l2(a, b):
+    n = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (n if n > 0 else 1.0)
+
+
+# ------------------------------------------------------------------ CPU tests
+@pytest.mark.parametrize("case", CASES)
+def test_reference_cubature_cache_layout(case):
+    """advection.cubature.cache = for each cubature cell its 3 rows of
+    U.preadvect, then weight x its 3 rows of U.prediffuse transposed
+    (SUBSPACE_FLUID_3D_EIGEN.cpp:1256-1299), each as EIGEN::write."""
+    z = _fixture(case)
+    raw = z["file_cubature"].tobytes()
+    n = int(np.frombuffer(raw[:4], dtype="<i4")[0])
+    cells = np.frombuffer(raw[4:4 + 4 * n], dtype="<i4")
+    weights = np.frombuffer(raw[4 + 4 * n:4 + 12 * n], dtype="<f8")
+    Upa = _matrix(z["file_U.preadvect.matrix"])
+    Upd = _matrix(z["file_U.prediffuse.matrix"])
+    cache = z["file_advection.cubature.cache"].tobytes()
+    off = 0
+    for x in range(n):
+        r, c = np.frombuffer(cache[off:off + 8], dtype="<i4")
+        m = np.frombuffer(cache[off + 8:off + 8 + 8 * r * c], dtype="<f8").reshape(r, c)
+        assert np.array_equal(m, Upa[3 * cells[x]:3 * cells[x] + 3])
+        off += 8 + 8 * r * c
+    for x in range(n):
+        r, c = np.frombuffer(cache[off:off + 8], dtype="<i4")
+        m = np.frombuffer(cache[off + 8:off + 8 + 8 * r * c], dtype="<f8").reshape(r, c)
+        assert np.array_equal(m, weights[x] * Upd[3 * cells[x]:3 * cells[x] + 3].T)
+        off += 8 + 8 * r * c
+    assert off == len(cache)
+
+
+def test_exact_cubature_tracks_the_full_rank_run():
+    """With every cell as a cubature point the reference's reduced run stays
+    within 1e-4 (velocity) and 1e-7 (density) of the full-rank run."""
+    e = _fixture("exact_10x12x8")["errors"]
+    assert e[:, 1].max() < 1e-4 and e[:, 3].max() < 1e-7
+
+
+# ------------------------------------------------------------------ GPU tests
+def _run(z, d, precision):
+    from cfs_plume_gb300 import _abi
+    from cfs_plume_gb300.plume import Plume, ReducedModel
+    res = tuple(int(v) for v in z["res"])
+    g = Plume(_abi.default_params(res=res, vorticity_eps=float(z["vorticity_eps"]), precision=precision))
+    m = ReducedModel(g, d)
+    for s in range(int(z["steps"])):
+        g.add_source(s)
+        st = m.step()
+        assert st.launches > 0
+    return g, m
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_reduced_step_matches_reference_fp64(tmp_path, case):
+    from cfs_plume_gb300 import _abi
+    z = _fixture(case)
+    d = str(tmp_path / "red") + "/"
+    # the exact case builds the cubature cache here; the sparse one reads it
+    _write_model(z, d, with_cache=(case != "exact_10x12x8"))
+    g, m = _run(z, d, _abi.PREC_FP64)
+    if case == "exact_10x12x8":
+        built = np.fromfile(d + "advection.cubature.cache", dtype=np.uint8)
+        assert np.array_equal(built, z["file_advection.cubature.cache"])
+    dims = m.dims()
+    assert dims["final"] == z["qdot"].size
+    assert rel_l2(m.qdot(), z["qdot"]) < 1e-8
+    for name in ("velocity", "density", "heat"):
+        err = rel_l2(g.field(name), z[name])
+        assert err < 1e-8, "%s rel L2 %.3e" % (name, err)
+
+
+@pytest.mark.gpu
+def test_reduced_step_fp32(tmp_path):
+    from cfs_plume_gb300 import _abi
+    z = _fixture("exact_10x12x8")
+    d = str(tmp_path / "red") + "/"
+    _write_model(z, d)
+    g, m = _run(z, d, _abi.PREC_FP32)
+    for name in ("velocity", "density", "heat"):
+        err = rel_l2(g.field(name), z[name])
+        assert err < 1e-3, "%s rel L2 %.3e" % (name, err)
+
+
+@pytest.mark.gpu
+def test_reduced_model_rejects_mismatched_files(tmp_path):
+    from cfs_plume_gb300 import _abi
+    from cfs_plume_gb300.plume import Plume, PlumeError, ReducedModel
+    z = _fixture("exact_10x12x8")
+    d = str(tmp_path / "red") + "/"
+    _write_model(z, d)
+    with pytest.raises(PlumeError):  # another grid
+        ReducedModel(Plume(_abi.default_params(res=(12, 12, 8))), d)
+    os.remove(d + "inverseProduct.matrix")
+    with pytest.raises(PlumeError):
+        ReducedModel(Plume(_abi.default_params(res=(10, 12, 8))), d)
