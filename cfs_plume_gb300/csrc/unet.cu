@@ -22,6 +22,7 @@
 #include "engine.h"
 #include "unet.h"
 #include "unet_kernels.cuh"
+#include "unet_tc.cuh"
 
 namespace plume {
 namespace unet {
@@ -102,6 +103,61 @@ cudaError_t conv_t(const Dims& d, int batch, View in, const uint2* wf, const flo
   dim3 grid(conv_bricks<CI, CO, MF>(d), batch);
   k_conv3<CI, CO, MF><<<grid, 256, C::SMEM, s>>>(d, in, wf, bias, out, mask, relu);
   return cudaGetLastError();
+}
+
+// The tensor-core (tcgen05) convolution for a layer shape whose halo brick
+// and weights fit in shared memory, launched as a one-CTA cluster (its
+// mbarrier commit names the cluster window); false if the shape has none.
+template <int CI, int CO>
+cudaError_t conv_tc_t(const Dims& d, int batch, View in, const bf16* wpack, const float* bias, View out,
+                      View mask, int relu, int* err, cudaStream_t s) {
+  using C = TcCfg<CI, CO>;
+  cudaError_t e = cudaFuncSetAttribute(k_conv3_tc<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+  if (e != cudaSuccess) return e;
+  const long long items =
+      (long long)((d.X + C::BX - 1) / C::BX) * ((d.Y + C::BY - 1) / C::BY) * ((d.Z + C::BZ - 1) / C::BZ) * batch;
+  // persistent: as many CTAs as shared memory and TMEM (512 columns per SM)
+  // keep resident at once
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3_tc<CI, CO>, 256, C::SMEM)) != cudaSuccess)
+    return e;
+  per_sm = std::max(1, std::min(per_sm, 512 / C::NCOLS));
+  const long long grid = std::min<long long>(items, (long long)sms * per_sm);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)std::max<long long>(1, grid));
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = C::SMEM;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 1;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_conv3_tc<CI, CO>, d, batch, in, wpack, bias, out, mask, relu, err);
+}
+
+// The shapes that run on tcgen05: measured at 128x192x128 (ncu, serialised),
+// <32,64> 20.1 us against 29-32 us for the best mma.sync tile, <32,32> 66-68
+// against 71-77, <16,32> 45 against 45.  With 16 output channels (N = 16)
+// the tensor-core version loses (<16,16> 262 against 167 us, <48,16> 606
+// against 424): each MMA re-reads a 4 KB A tile for 8 KFLOP-per-row of work,
+// the tensor pipe sits at 7-9 % active and the per-item phases (stage, issue,
+// wait, epilogue) of one resident CTA do not overlap, so those layers keep the
+// mma.sync kernel.
+inline bool conv_tc_supported(int ci, int co) {
+  return (ci == 16 && co == 32) || (ci == 32 && co == 32) || (ci == 32 && co == 64);
+}
+
+cudaError_t conv_tc(int ci, int co, const Dims& d, int batch, View in, const bf16* wpack, const float* bias,
+                    View out, View mask, int relu, int* err, cudaStream_t s) {
+  if (ci == 16 && co == 32) return conv_tc_t<16, 32>(d, batch, in, wpack, bias, out, mask, relu, err, s);
+  if (ci == 32 && co == 32) return conv_tc_t<32, 32>(d, batch, in, wpack, bias, out, mask, relu, err, s);
+  if (ci == 32 && co == 64) return conv_tc_t<32, 64>(d, batch, in, wpack, bias, out, mask, relu, err, s);
+  return cudaErrorInvalidValue;
 }
 
 // Tile shapes (rows per warp) a layer shape may use: accumulators MF*NF*4 <= 64
@@ -290,6 +346,9 @@ class Net : public NetRuntime {
  public:
   ~Net() override {
     if (params_) cudaFree(params_);
+    for (bf16* p : wtc_)
+      if (p) cudaFree(p);
+    if (tc_err_) cudaFree(tc_err_);
     if (s_) cudaStreamDestroy(s_);
   }
 
@@ -325,7 +384,11 @@ class Net : public NetRuntime {
       cur += fb;
       wb_[l] = (uint2*)cur;
       cur += fb;
+      if (conv_tc_supported(kLayers[l].cin, kLayers[l].cout))
+        NT(cudaMalloc((void**)&wtc_[l], 27LL * kLayers[l].cin * kLayers[l].cout * sizeof(bf16)));
     }
+    NT(cudaMalloc((void**)&tc_err_, sizeof(int)));
+    NT(cudaMemsetAsync(tc_err_, 0, sizeof(int), s_));
     // He-normal weights (fan-in 27*cin; the output layer 16), zero biases.
     // Input channels 1..15 of the first layer carry zeros and keep their
     // weights; only channel 0 (the right-hand side) is drawn.
@@ -369,6 +432,10 @@ class Net : public NetRuntime {
       const long long n = 27LL * cin * cout / 4;  // fragment lanes: 4 elements each
       k_prep_fwd<<<blocks_for(n), kThreads, 0, s>>>(w_ + woff_[l], cin, cout, wf_[l]);
       NT_LAUNCH();
+      if (wtc_[l]) {
+        k_prep_tc<<<blocks_for(27LL * cin * cout), kThreads, 0, s>>>(w_ + woff_[l], cin, cout, wtc_[l]);
+        NT_LAUNCH();
+      }
       if (l != E1A) {
         k_prep_bwd<<<blocks_for(n), kThreads, 0, s>>>(w_ + woff_[l], cin, cout, wb_[l]);
         NT_LAUNCH();
@@ -382,6 +449,9 @@ class Net : public NetRuntime {
     const Dims* d = ws.d;
     const View no = none();
     auto cv = [&](int l, View in, View out) {
+      if (wtc_[l] && !tc_off_)
+        return conv_tc(kLayers[l].cin, kLayers[l].cout, d[kLayers[l].level], nb, in, wtc_[l], w_ + boff_[l], out,
+                       no, 1, tc_err_, s);
       return conv_tuned(kLayers[l].cin, kLayers[l].cout, d[kLayers[l].level], nb, in, wf_[l], w_ + boff_[l], out,
                         no, 1, s);
     };
@@ -609,6 +679,9 @@ class Net : public NetRuntime {
   float *w_ = nullptr, *g_ = nullptr, *m_ = nullptr, *v_ = nullptr;
   uint2* wf_[NCONV] = {};
   uint2* wb_[NCONV] = {};
+  bf16* wtc_[NCONV] = {};   // tcgen05 B-operand copies (supported shapes only)
+  int* tc_err_ = nullptr;   // set by a tensor-core convolution whose wait expired
+  bool tc_off_ = getenv("PLUME_CONV_TC") != nullptr && getenv("PLUME_CONV_TC")[0] == '0';
   long long woff_[NCONV + 1] = {}, boff_[NCONV + 1] = {};
   long long nparams_ = 0;
   float scale_c_ = 1.f;

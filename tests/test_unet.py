@@ -289,3 +289,26 @@ def test_tile_shapes_give_identical_outputs(monkeypatch):
         outs.append(n.forward(inp, res))
         n.close()
     np.testing.assert_array_equal(outs[0], outs[1])
+
+
+@pytest.mark.gpu
+def test_tcgen05_convolution_matches_mma_sync(monkeypatch):
+    """The tensor-core (tcgen05) convolutions against the mma.sync ones on the
+    same BF16 inputs and weights: relative L2 below 1e-2 for the whole forward
+    pass, the bound of the oracle comparison (both accumulate 27*CIN products
+    in FP32, in different orders, and every layer rounds its output to BF16,
+    so single elements move by a BF16 ulp and ten layers carry it on), on a
+    grid whose edges cut the 16 x 8 x 2 output bricks."""
+    from cfs_plume_gb300.net import PlumeNet
+    params = random_params(12)
+    rng = np.random.default_rng(13)
+    res = (36, 44, 28)
+    inp = smooth_field(rng, res, 2).astype(np.float32)
+    outs = []
+    for tc in ("0", "1"):
+        monkeypatch.setenv("PLUME_CONV_TC", tc)
+        n = PlumeNet(seed=0)
+        n.params = params
+        outs.append(n.forward(inp, res))
+        n.close()
+    assert rel(outs[1], outs[0]) < 1e-2, rel(outs[1], outs[0])
