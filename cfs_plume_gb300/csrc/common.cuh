@@ -96,6 +96,39 @@ __device__ inline A block_max(A v, A* sh, A ident) {
   return r;
 }
 
+// Block sum of per-thread T values with the warp-level tree in T and the
+// warps' sums in double (result valid in thread 0).  For T = double it is
+// block_sum; for float it keeps the shuffle tree off the FP64 pipe, which
+// issues at 1/64 of the FP32 rate on this part.
+template <typename T>
+__device__ inline double block_sum_w(T v, double* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = (double)v;
+  __syncthreads();
+  double r = 0;
+  if (wid == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  return r;
+}
+template <typename T>
+__device__ inline double block_max_w(T v, double* sh, double ident) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = (double)v;
+  __syncthreads();
+  double r = ident;
+  if (wid == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : ident;
+    r = warp_max(r);
+  }
+  return r;
+}
+
 // SplitMix64 finaliser; identical integer recipe on host (oracle) and device.
 __host__ __device__ inline uint64_t mix64(uint64_t z) {
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;

@@ -107,7 +107,7 @@ __global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState
     }
     r[e] = v;
   }
-  const double s = block_sum((double)bb, sh);
+  const double s = block_sum_w(bb, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (arrive_last(&st->ticket[0])) {
     const double tot = sum_partials(part, sh);
@@ -137,9 +137,9 @@ __global__ void k_cgs_init2(Skew k, const T* r, const T* z, T* d, CgState* st, d
     rz += ri * zi;
     rr += ri * ri;
   }
-  const double s1 = block_sum((double)rz, sh);
+  const double s1 = block_sum_w(rz, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s1;
-  const double s2 = block_sum((double)rr, sh);
+  const double s2 = block_sum_w(rr, sh);
   if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
   if (arrive_last(&st->ticket[0])) {
     const double trz = sum_partials(part, sh);
@@ -179,7 +179,7 @@ __global__ void k_cgs_spmv(Grid g, Skew k, const T* d, T* q, CgState* st, double
     }
     q[e] = v;
   }
-  const double s = block_sum((double)dq, sh);
+  const double s = block_sum_w(dq, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (arrive_last(&st->ticket[0])) {
     const double t = sum_partials(part, sh);
@@ -210,9 +210,9 @@ __global__ void k_cgs_axpy(Skew k, const T* d, const T* q, T* x, T* r, CgState* 
     mx = (ri > mx) ? ri : mx;
     rr += ri * ri;
   }
-  const double s1 = block_max((double)mx, sh, -1.0e308);
+  const double s1 = block_max_w(mx, sh, -1.0e308);
   if (threadIdx.x == 0) part[blockIdx.x] = s1;
-  const double s2 = block_sum((double)rr, sh);
+  const double s2 = block_sum_w(rr, sh);
   if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
   if (arrive_last(&st->ticket[0])) {
     const double tm = max_partials(part, sh);
@@ -238,7 +238,7 @@ __global__ void k_cgs_rz(Skew k, const T* r, const T* z, CgState* st, double* pa
   __shared__ double sh[32];
   T rz = T(0);
   PL_GRID_STRIDE(e, (int)k.total) rz += r[e] * z[e];
-  const double s = block_sum((double)rz, sh);
+  const double s = block_sum_w(rz, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (arrive_last(&st->ticket[0])) {
     const double t = sum_partials(part, sh);
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(SkewRows<C>::THREADS) k_cgs_spmv_dir(Grid g, S
     d_new[e] = dn;
     q[e] = qq;
   }
-  const double sblk = block_sum((double)dq, sh);
+  const double sblk = block_sum_w(dq, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = sblk;
   if (arrive_last(&st->ticket[0])) {
     const double t = sum_partials(part, sh);
@@ -404,9 +404,9 @@ __global__ void k_cgs_axpy_v(Skew k, const T* d, const T* q, T* x, T* r, CgState
     xv[i] = xx;
     rv[i] = ri;
   }
-  const double s1 = block_max((double)mx, sh, -1.0e308);
+  const double s1 = block_max_w(mx, sh, -1.0e308);
   if (threadIdx.x == 0) part[blockIdx.x] = s1;
-  const double s2 = block_sum((double)rr, sh);
+  const double s2 = block_sum_w(rr, sh);
   if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
   if (arrive_last(&st->ticket[0])) {
     const double tm = max_partials(part, sh);
@@ -441,7 +441,7 @@ __global__ void k_cgs_rz_v(Skew k, const T* r, const T* z, CgState* st, double* 
 #pragma unroll
     for (int c = 0; c < NV; c++) rz += vget<T>(a, c) * vget<T>(b, c);
   }
-  const double s = block_sum((double)rz, sh);
+  const double s = block_sum_w(rz, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (arrive_last(&st->ticket[0])) {
     const double t = sum_partials(part, sh);
