@@ -148,19 +148,15 @@ __global__ void k_red_cubature(const double* Upa, size_t n, int rpa, const doubl
     finals[(size_t)p * rpd + k] = A[k * 3] * acc[0] + A[k * 3 + 1] * acc[1] + A[k * 3 + 2] * acc[2];
 }
 
-// final[k] = sum over points, in point order per 256-point chunk, then over
-// chunks in order: one thread per k
+// final[k] = sum over points: a warp per k, lane l adding points l, l + 32, ...
+// in order, then the warp's tree (a fixed order)
 __global__ void k_red_sum(const double* finals, int npts, int rpd, double* out) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.x * kWarps + threadIdx.x / 32, lane = threadIdx.x % 32;
   if (k >= rpd) return;
-  double total = 0.0;
-  for (int c0 = 0; c0 < npts; c0 += 256) {
-    double s = 0.0;
-    const int c1 = min(npts, c0 + 256);
-    for (int p = c0; p < c1; p++) s += finals[(size_t)p * rpd + k];
-    total += s;
-  }
-  out[k] = total;
+  double s = 0.0;
+  for (int p = lane; p < npts; p += 32) s += finals[(size_t)p * rpd + k];
+  s = warp_sum(s);
+  if (lane == 0) out[k] = s;
 }
 
 // y = M x (M rows x cols, row-major), a warp per row; with M2: y = M x + M2 x
@@ -475,7 +471,7 @@ int plume_reduced_step(plume_reduced* r, plume_step_stats* stats) {
   k_red_cubature<<<(r->npts + kWarps - 1) / kWarps, kThreads, 0, s>>>(r->Upa, r->n, r->rpa, r->q, r->cells,
                                                                        r->before, r->after, r->rpd, r->npts, r->X,
                                                                        r->Y, r->Z, r->dt0, r->finals);
-  k_red_sum<<<(r->rpd + 127) / 128, 128, 0, s>>>(r->finals, r->npts, r->rpd, r->q2);
+  k_red_sum<<<(r->rpd + kWarps - 1) / kWarps, kThreads, 0, s>>>(r->finals, r->npts, r->rpd, r->q2);
   // reducedPeeledDiffusion (lines 606-612): q = D q
   k_red_gemv2<<<(r->rpp + kWarps - 1) / kWarps, kThreads, 0, s>>>(r->D, nullptr, r->rpp, r->rpd, r->q2, r->q);
   // reducedStagedProject (lines 700-707): q = ptof q + inverseProduct q
