@@ -300,29 +300,30 @@ def _write_eigen(path, M):
 
 
 def measure_reduced(steps, local, rank, res=(64, 96, 64), rank_r=32, points=2000):
-    """stepReorderedCubatureStam on the GPU with a synthetic reduced model of
-    the reference's file layout (seeded random bases of rank 32, damping 0.99 I,
-    ptof I, inverseProduct 0, 2000 seeded cubature cells), FP32 plume fields."""
+    """buildOutOfCoreMatrices and stepReorderedCubatureStam on the GPU with a
+    synthetic reduced model of the reference's file layout (seeded random
+    bases of rank 32, the projected operators built from them on the device,
+    2000 seeded cubature cells), FP32 plume fields."""
     import numpy as np
     import shutil
     from cfs_plume_gb300 import _abi
-    from cfs_plume_gb300.plume import Plume, ReducedModel
+    from cfs_plume_gb300.plume import Plume, ReducedModel, build_products
     nint = (res[0] - 2) * (res[1] - 2) * (res[2] - 2)
     n = 3 * nint
     rng = np.random.default_rng(7 + rank)
     d = tempfile.mkdtemp(prefix="plume_reduced_bench_")
     try:
-        for fn in ("U.preadvect.matrix", "U.final.matrix", "U.prediffuse.matrix"):
+        for fn in ("U.preadvect.matrix", "U.final.matrix", "U.prediffuse.matrix", "U.preproject.matrix"):
             _write_eigen(os.path.join(d, fn), rng.standard_normal((n, rank_r)) / math.sqrt(n))
-        _write_eigen(os.path.join(d, "damping.peeled.matrix"), 0.99 * np.eye(rank_r))
-        _write_eigen(os.path.join(d, "projected.ptof.matrix"), np.eye(rank_r))
-        _write_eigen(os.path.join(d, "inverseProduct.matrix"), np.zeros((rank_r, rank_r)))
+        _write_eigen(os.path.join(d, "U.pressure.matrix"), rng.standard_normal((nint, rank_r)) / math.sqrt(nint))
         cells = np.sort(rng.choice(nint, points, replace=False)).astype("<i4")
         with open(os.path.join(d, "cubature"), "wb") as f:
             f.write(struct.pack("<i", points))
             cells.tofile(f)
             np.full(points, nint / points, dtype="<f8").tofile(f)
         g = Plume(_abi.plume_config(res, precision=_abi.PREC_FP32, seed=rank, device=local))
+        build_products(g, d)  # warm-up (module load, first allocations)
+        products = build_products(g, d)
         m = ReducedModel(g, d)
         for s in range(3):
             g.add_source(s)
@@ -340,7 +341,20 @@ def measure_reduced(steps, local, rank, res=(64, 96, 64), rank_r=32, points=2000
     finally:
         shutil.rmtree(d, ignore_errors=True)
     return {"res": res, "n": n, "r": rank_r, "points": points, "ms_total": tot / steps, "ms_reduced": red / steps,
-            "launches": launches / steps}
+            "launches": launches / steps, "products": products}
+
+
+def products_record(r, fp64_peak_tflops):
+    """The projected-operator build of the same synthetic model."""
+    p = r["products"]
+    ach = p["gflop"] / p["ms_device"] if p["ms_device"] > 0 else None  # GFLOP/ms = TFLOP/s
+    return {"workload": "buildOutOfCoreMatrices, plume %dx%dx%d walls, four synthetic rank-%d FP64 bases "
+                        "(U.pressure, U.preproject, U.prediffuse, U.final)" % (tuple(r["res"]) + (r["r"],)),
+            "ms_device": p["ms_device"], "ms_total_with_file_io": p["ms_total"], "gflop": p["gflop"],
+            "roofline": {"bound": "fp64", "kernel": "whole build (stencils, k_atb projections, Gauss-Jordan)",
+                         "achieved": ach, "peak": fp64_peak_tflops, "unit": "TFLOP/s",
+                         "frac": (ach / fp64_peak_tflops) if ach else None,
+                         "flops_model": "sum of 2 K a b over the projections + 4 r^3 for the inverse"}}
 
 
 def reduced_record(r, peak):
@@ -522,6 +536,7 @@ def main():
         "moving_box": moving_record(mov, res, N, nint, S, peak, a.steps) if mov else None,
         "snapshot_svd": svd_record(svd, 2 * 2 * 152 * 2.070e9 / 1e12) if svd else None,
         "reduced_step": reduced_record(red, peak) if red else None,
+        "reduced_products": products_record(red, 2 * 2 * 152 * 2.070e9 / 1e12) if red else None,
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": nbox * 8,
                 "d2h_bytes_per_step": 3 * N * 8},
         "clocks": clk,

@@ -143,6 +143,16 @@ class PlumeBox(C.Structure):
     ]
 
 
+class PlumeProductsInfo(C.Structure):
+    """plume_products_info (include/plume_reduced.h)."""
+    _fields_ = [
+        ("ranks", C.c_int32 * 4),
+        ("ms_device", C.c_double),
+        ("ms_total", C.c_double),
+        ("gflop", C.c_double),
+    ]
+
+
 class PlumeSvdInfo(C.Structure):
     """plume_svd_info (include/plume_svd.h)."""
     _fields_ = [

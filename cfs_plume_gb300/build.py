@@ -82,6 +82,7 @@ def build(verbose=False, ptxas_info=False):
         ("unet.cu", [nvcc] + common_nv),
         ("svd.cu", [nvcc] + common_nv),
         ("reduced.cu", [nvcc] + common_nv),
+        ("products.cu", [nvcc] + common_nv),
         ("plume_api.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-I" + os.path.join(cuda, "include")]),
         ("snapshot.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread"] + zc),
         ("batch.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread"]),

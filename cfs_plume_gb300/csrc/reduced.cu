@@ -21,6 +21,7 @@
 #include "../../include/plume.h"
 #include "../../include/plume_reduced.h"
 #include "engine.h"
+#include "matrix_file.cuh"
 
 namespace plume {
 namespace reduced {
@@ -196,28 +197,11 @@ __global__ void k_red_unproject(int X, int Y, int Z, T* vx, T* vy, T* vz, const 
   }
 }
 
-// row-major (rows x cols) -> column-major, 32 x 32 tiles
-__global__ void k_transpose(const double* in, size_t rows, int cols, double* out) {
-  __shared__ double tile[32][33];
-  const size_t r0 = (size_t)blockIdx.x * 32;
-  const int c0 = blockIdx.y * 32;
-  for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
-    const size_t r = r0 + dy;
-    const int c = c0 + threadIdx.x;
-    if (r < rows && c < cols) tile[dy][threadIdx.x] = in[r * cols + c];
-  }
-  __syncthreads();
-  for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
-    const int c = c0 + dy;
-    const size_t r = r0 + threadIdx.x;
-    if (r < rows && c < cols) out[(size_t)c * rows + r] = tile[threadIdx.x][dy];
-  }
-}
-
 }  // namespace reduced
 }  // namespace plume
 
 using namespace plume::reduced;
+using namespace plume::matrix_file;
 
 struct plume_reduced {
   plume_handle* h = nullptr;
@@ -239,76 +223,6 @@ namespace {
 int fail(int code, const std::string& msg) {
   plume::global_error() = msg;
   return code;
-}
-
-// EIGEN::read layout (EIGEN.cpp:195-213): int32 rows, cols, row-major doubles
-bool read_matrix(const std::string& path, int& rows, int& cols, std::vector<double>& data) {
-  FILE* f = fopen(path.c_str(), "rb");
-  if (!f) return false;
-  bool ok = fread(&rows, sizeof(int), 1, f) == 1 && fread(&cols, sizeof(int), 1, f) == 1 && rows >= 0 && cols >= 0;
-  if (ok) {
-    data.resize((size_t)rows * cols);
-    ok = fread(data.data(), sizeof(double), data.size(), f) == data.size();
-  }
-  fclose(f);
-  return ok;
-}
-
-bool read_matrix_file(FILE* f, int& rows, int& cols, std::vector<double>& data) {
-  bool ok = fread(&rows, sizeof(int), 1, f) == 1 && fread(&cols, sizeof(int), 1, f) == 1 && rows >= 0 && cols >= 0;
-  if (ok) {
-    data.resize((size_t)rows * cols);
-    ok = fread(data.data(), sizeof(double), data.size(), f) == data.size();
-  }
-  return ok;
-}
-
-// EIGEN::write layout (EIGEN.cpp:294-310)
-bool write_matrix_file(FILE* f, int rows, int cols, const double* data) {
-  return fwrite(&rows, sizeof(int), 1, f) == 1 && fwrite(&cols, sizeof(int), 1, f) == 1 &&
-         fwrite(data, sizeof(double), (size_t)rows * cols, f) == (size_t)rows * cols;
-}
-
-template <typename Ptr>
-cudaError_t upload(Ptr*& dst, const std::vector<Ptr>& src) {
-  cudaError_t e = cudaMalloc(&dst, std::max<size_t>(1, src.size()) * sizeof(Ptr));
-  if (e == cudaSuccess && !src.empty())
-    e = cudaMemcpy(dst, src.data(), src.size() * sizeof(Ptr), cudaMemcpyHostToDevice);
-  return e;
-}
-
-// An n x r row-major basis from its file, to the device as column-major.
-int upload_basis(const std::string& path, size_t n_expected, double*& dst, int& cols, std::string& err) {
-  int rows = 0;
-  std::vector<double> h;
-  if (!read_matrix(path, rows, cols, h)) {
-    err = "could not read " + path;
-    return PLUME_ERR_IO;
-  }
-  if ((size_t)rows != n_expected) {
-    err = path + " does not match the grid (" + std::to_string(rows) + " rows, expected " +
-          std::to_string(n_expected) + ")";
-    return PLUME_ERR_IO;
-  }
-  double* tmp = nullptr;
-  if (cudaMalloc(&tmp, std::max<size_t>(1, h.size()) * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&dst, std::max<size_t>(1, h.size()) * sizeof(double)) != cudaSuccess) {
-    if (tmp) cudaFree(tmp);
-    err = "basis does not fit on the device";
-    return PLUME_ERR_OOM;
-  }
-  int rc = PLUME_OK;
-  if (!h.empty()) {
-    if (cudaMemcpy(tmp, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) rc = PLUME_ERR_CUDA;
-    if (rc == PLUME_OK) {
-      const dim3 grid((unsigned)((n_expected + 31) / 32), (unsigned)((cols + 31) / 32));
-      k_transpose<<<grid, dim3(32, 8)>>>(tmp, n_expected, cols, dst);
-      if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = PLUME_ERR_CUDA;
-    }
-  }
-  cudaFree(tmp);
-  if (rc != PLUME_OK) err = "basis upload failed";
-  return rc;
 }
 
 }  // namespace
@@ -343,11 +257,31 @@ int plume_reduced_create(plume_handle* h, const char* reduced_path, plume_reduce
   if (cudaSetDevice(p.device) != cudaSuccess) return fail(PLUME_ERR_CUDA, "cudaSetDevice failed");
   const std::string dir = reduced_path;
   std::string err;
+  // initOutOfCore (SUBSPACE_FLUID_3D_EIGEN.cpp:82-136): the six projected
+  // operators make a built model unless projected.ptof no longer has a row per
+  // U.final column; otherwise all six are built (buildOutOfCoreMatrices).
+  {
+    bool built = true;
+    int rr = 0, cc = 0;
+    for (const char* f : {"projected.A.matrix", "projected.ptof.matrix", "projected.vtod.matrix",
+                          "damping.peeled.matrix", "projected.ptov.matrix", "inverseProduct.matrix"}) {
+      FILE* t = fopen((dir + f).c_str(), "rb");
+      if (!t) built = false;
+      if (t) fclose(t);
+    }
+    int ur = 0, uc = 0;
+    if (built && read_matrix_dims(dir + "U.final.matrix", ur, uc) && read_matrix_dims(dir + "projected.ptof.matrix", rr, cc) &&
+        rr != uc)
+      built = false;
+    if (!built) {
+      const int brc = plume_reduced_build_products(h, reduced_path, nullptr);
+      if (brc != PLUME_OK) return brc;
+    }
+  }
   int rc = upload_basis(dir + "U.preadvect.matrix", r->n, r->Upa, r->rpa, err);
   if (rc == PLUME_OK) rc = upload_basis(dir + "U.final.matrix", r->n, r->Uf, r->rf, err);
   if (rc != PLUME_OK) return fail(rc, err);
-  // the projected operators (built by the reference's constructor,
-  // SUBSPACE_FLUID_3D_EIGEN.cpp:82-167)
+  // the projected operators the step uses
   int dr = 0, dc = 0, pr = 0, pc = 0, gr = 0, gc = 0;
   std::vector<double> hd, hp, hg;
   if (!read_matrix(dir + "damping.peeled.matrix", dr, dc, hd) ||

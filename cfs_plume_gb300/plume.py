@@ -16,7 +16,7 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import PlumeBox, PlumeParams, PlumeStepStats, PlumeSvdInfo
+from ._abi import PlumeBox, PlumeParams, PlumeProductsInfo, PlumeStepStats, PlumeSvdInfo
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "lib", "libplume.so")
@@ -85,6 +85,7 @@ def load_library(path=LIB_PATH):
         "plume_reduced_step": (C.c_int, [H, P(PlumeStepStats)]),
         "plume_reduced_qdot": (C.c_int, [H, C.c_void_p, C.c_int32, P(C.c_int32)]),
         "plume_reduced_dims": (C.c_int, [H, P(C.c_int32)]),
+        "plume_reduced_build_products": (C.c_int, [H, C.c_char_p, P(PlumeProductsInfo)]),
         "plume_snapshots_create": (C.c_int, [H, C.c_int32, C.c_int32, P(H)]),
         "plume_snapshots_destroy": (None, [H]),
         "plume_snapshots_append": (C.c_int, [H, P(C.c_int32)]),
@@ -526,10 +527,27 @@ class Snapshots:
         return pca[:r], kept.value, {f: getattr(info, f) for f, _ in PlumeSvdInfo._fields_}
 
 
+def build_products(plume, reduced_path):
+    """The projected operators of a reduced model for the plume's grid and
+    walls (plume_reduced_build_products, include/plume_reduced.h; the
+    reference's buildOutOfCoreMatrices run by buildProducts): reads
+    U.pressure, U.preproject, U.prediffuse and U.final under reduced_path and
+    writes projected.A, projected.vtod, damping.peeled, projected.ptof,
+    projected.ptov and inverseProduct there.  Returns the plume_products_info
+    as a dict."""
+    lib = load_library()
+    d = reduced_path if reduced_path.endswith("/") else reduced_path + "/"
+    info = PlumeProductsInfo()
+    _check(lib.plume_reduced_build_products(plume.h, os.fsencode(d), C.byref(info)))
+    return dict(ranks=tuple(info.ranks), ms_device=info.ms_device, ms_total=info.ms_total, gflop=info.gflop)
+
+
 class ReducedModel:
     """A reduced (subspace) model attached to a plume handle
     (plume_reduced, include/plume_reduced.h): step() is the reference's
-    stepReorderedCubatureStam on the handle's state."""
+    stepReorderedCubatureStam on the handle's state.  Creating it builds the
+    projected operators first when they are missing or stale, as the
+    reference's constructor does."""
 
     def __init__(self, plume, reduced_path):
         self.h = None

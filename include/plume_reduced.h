@@ -11,16 +11,23 @@
  *     (the cubature file and the advection cubature cache, built and written
  *      when missing)
  *   src/integrators/SUBSPACE_FLUID_3D_EIGEN.cpp:1911-1931  loadReducedRuntimeBases
+ *   src/integrators/SUBSPACE_FLUID_3D_EIGEN.cpp:82-167     initOutOfCore (which
+ *     files make a built model; stale operators are rebuilt)
+ *   src/integrators/SUBSPACE_FLUID_3D_EIGEN.cpp:1355-1490  buildOutOfCoreMatrices
+ *     (the projected operators, run by projects/buildProducts through the
+ *      constructor): plume_reduced_build_products
  *   projects/reduced3D/reduced3D.cpp:344-375             the stage's step loop
  *
  * A reduced model is attached to a plume handle (its grid, walls, buoyancy,
  * vorticity and sources): plume_add_source + plume_reduced_step replace
  * addSmokeColumn + stepReorderedCubatureStam.  The model's files are the
  * reference's, under `reduced_path`: U.preadvect.matrix, U.final.matrix,
- * projected.ptof.matrix, inverseProduct.matrix, damping.peeled.matrix (the
- * projected operators that SUBSPACE_FLUID_3D_EIGEN's constructor builds),
- * cubature, and advection.cubature.cache (built from U.preadvect.matrix and
- * U.prediffuse.matrix and written when missing, as the reference does).
+ * the projected operators (projected.A, projected.vtod, damping.peeled,
+ * projected.ptof, projected.ptov, inverseProduct .matrix; built on the
+ * device from U.pressure, U.preproject, U.prediffuse and U.final when one is
+ * missing or projected.ptof no longer matches U.final, as the reference's
+ * constructor does), cubature, and advection.cubature.cache (built from
+ * U.preadvect.matrix and U.prediffuse.matrix and written when missing).
  * The bases and the reduced arithmetic are FP64 in both field precisions.
  */
 #ifndef PLUME_REDUCED_H
@@ -36,6 +43,27 @@ extern "C" {
 #endif
 
 typedef struct plume_reduced plume_reduced;
+
+/* What plume_reduced_build_products did. */
+typedef struct plume_products_info {
+  int32_t ranks[4]; /* columns of U.pressure, U.preproject, U.prediffuse, U.final */
+  double ms_device; /* device time: operator stencils, projections, inverse    */
+  double ms_total;  /* wall time, file reads and writes included               */
+  double gflop;     /* FP64 work of the projections, the inverse and products */
+} plume_products_info;
+
+/* buildOutOfCoreMatrices for the handle's grid and walls: reads U.pressure,
+   U.preproject, U.prediffuse and U.final under reduced_path and writes
+   projected.A  = U_p^T A U_p      (A: the peeled Poisson matrix, buildFlatA)
+   projected.vtod = U_p^T V U_pp   (V: computeVelocityToDivergence)
+   damping.peeled = U_pp^T D U_pd  (D: buildPeeledDampingMatrixFlat)
+   projected.ptof = U_f^T U_pp
+   projected.ptov = U_f^T G U_p    (G: computePressureToVelocity)
+   inverseProduct = ptov projected.A^-1 vtod
+   there (EIGEN::write layout).  PLUME_ERR_IO when a basis is missing or does
+   not match the grid, PLUME_ERR_INVALID when projected.A is singular.
+   info may be NULL. */
+int plume_reduced_build_products(plume_handle* h, const char* reduced_path, plume_products_info* info);
 
 /* Loads the model for the handle's grid; PLUME_ERR_IO when a file is missing
    or does not match the grid, PLUME_ERR_INVALID on inconsistent ranks.  The

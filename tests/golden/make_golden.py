@@ -29,7 +29,10 @@ configurations and stores what it produced:
                         reduced-path files it read or wrote (bases, projected
                         operators, cubature, cubature cache) and the fields,
                         reduced coordinates and ground-truth errors after 12
-                        reduced steps.
+                        reduced steps;
+  ref_products_mixed_10x12x8.npz  the projected operators that the reference's
+                        constructor (buildOutOfCoreMatrices) builds from the
+                        same bases under mixed walls.
 
 Needs the reference tree (PLUME_REFERENCE_DIR, default /root/reference) and
 writes nothing outside tests/golden/.
@@ -138,8 +141,16 @@ def main():
 
 
 RED_REF = os.path.join(ROOT, "oracle", "_ref", "reduced_ref")
-RED_FILES = ["U.preadvect.matrix", "U.final.matrix", "U.prediffuse.matrix", "damping.peeled.matrix",
-             "projected.ptof.matrix", "inverseProduct.matrix", "cubature", "advection.cubature.cache"]
+RED_FILES = ["U.preadvect.matrix", "U.final.matrix", "U.prediffuse.matrix", "U.preproject.matrix",
+             "U.pressure.matrix", "damping.peeled.matrix", "projected.ptof.matrix", "projected.A.matrix",
+             "projected.vtod.matrix", "projected.ptov.matrix", "inverseProduct.matrix", "cubature",
+             "advection.cubature.cache"]
+PRODUCT_FILES = ["projected.A.matrix", "projected.vtod.matrix", "damping.peeled.matrix",
+                 "projected.ptof.matrix", "projected.ptov.matrix", "inverseProduct.matrix"]
+# walls (front, back, left, right, top, bottom) of the second operator build:
+# Neumann on the x-high, z-low and y-low faces, so that every branch of
+# computeVelocityToDivergence and every wall pattern of buildFlatA is taken
+MIXED_BC = (0, 1, 1, 0, 1, 0)
 
 
 def reduced_fixtures():
@@ -179,6 +190,18 @@ def reduced_fixtures():
         rec["errors"] = np.fromfile(out + ".errors.f64").reshape(-1, 4)
         np.savez_compressed(os.path.join(HERE, "ref_reduced_%s.npz" % name), **rec)
         print("reduced", name, "qdot", rec["qdot"].size, "errors (last)", rec["errors"][-1])
+    # the projected operators of the same bases under other walls: the
+    # reference's constructor builds them (buildOutOfCoreMatrices), no steps
+    red = base + "/red_mixed/"
+    shutil.copytree(red0, red)
+    shutil.copy(base + "/red_exact_10x12x8/cubature", red + "cubature")
+    subprocess.run([RED_REF, "res=%d,%d,%d" % res, "bc=" + ",".join(str(b) for b in MIXED_BC),
+                    "vorticity=1.0", "reduced=" + red, "truth=" + snap, "steps=0", "out=" + base + "/out_mixed"],
+                   check=True, capture_output=True)
+    rec = {"res": np.array(res), "bc": np.array(MIXED_BC)}
+    for fn in PRODUCT_FILES:
+        rec["file_" + fn] = np.fromfile(red + fn, dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "ref_products_mixed_10x12x8.npz"), **rec)
     shutil.rmtree(base)
 
 

@@ -54,6 +54,7 @@ def test_struct_sizes_match_header():
     assert C.sizeof(_abi.PlumeParams) == 200
     assert _abi.PlumeParams.seed.offset == 128
     assert C.sizeof(_abi.PlumeStepStats) == 56
+    assert C.sizeof(_abi.PlumeProductsInfo) == 40
 
 
 def test_invalid_params_are_rejected_without_a_device(plume_lib):

@@ -37,7 +37,7 @@ def run_oracle(p, steps):
 
 
 CASES = sorted(os.path.basename(f)[4:-4] for f in glob.glob(os.path.join(GOLDEN, "ref_*.npz"))
-               if not any(k in os.path.basename(f) for k in ("sampled", "moving", "svd", "reduced")))
+               if not any(k in os.path.basename(f) for k in ("sampled", "moving", "svd", "reduced", "products")))
 
 
 @pytest.mark.parametrize("case", CASES)

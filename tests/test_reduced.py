@@ -18,8 +18,12 @@ import pytest
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["exact_10x12x8", "sparse_10x12x8"]
-FILES = ["U.preadvect.matrix", "U.final.matrix", "U.prediffuse.matrix", "damping.peeled.matrix",
-         "projected.ptof.matrix", "inverseProduct.matrix", "cubature", "advection.cubature.cache"]
+# every file of a built model, so that the steps run on the reference's own
+# projected operators (tests/test_products.py covers the GPU-built ones)
+FILES = ["U.preadvect.matrix", "U.final.matrix", "U.prediffuse.matrix", "U.preproject.matrix",
+         "U.pressure.matrix", "damping.peeled.matrix", "projected.ptof.matrix", "projected.A.matrix",
+         "projected.vtod.matrix", "projected.ptov.matrix", "inverseProduct.matrix", "cubature",
+         "advection.cubature.cache"]
 
 
 def _fixture(case):
@@ -134,6 +138,8 @@ def test_reduced_model_rejects_mismatched_files(tmp_path):
     _write_model(z, d)
     with pytest.raises(PlumeError):  # another grid
         ReducedModel(Plume(_abi.default_params(res=(12, 12, 8))), d)
+    # an operator missing and no pressure basis to rebuild it from
     os.remove(d + "inverseProduct.matrix")
+    os.remove(d + "U.pressure.matrix")
     with pytest.raises(PlumeError):
         ReducedModel(Plume(_abi.default_params(res=(10, 12, 8))), d)
