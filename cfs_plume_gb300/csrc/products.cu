@@ -14,8 +14,9 @@
 // stored: k_apply evaluates one operator's row stencil for every column of a
 // basis (W = M U; A and D are symmetric, so M^T U = M U), k_atb forms L^T R
 // split over the long dimension with a fixed-order reduction (k_sum_split),
-// and the inverse is a Gauss-Jordan elimination with partial pivoting
-// (k_gj_pivot, k_gj_update), one pivot column per launch pair.
+// and the inverse is a Gauss-Jordan elimination with partial pivoting: in
+// one block's shared memory up to rank 96 (k_gj_small), above that one pivot
+// column per launch pair (k_gj_pivot, k_gj_update).
 //
 // The bases stay resident for the whole build (the reference reads and drops
 // them one at a time to fit host memory); at 128x192x128 one basis of rank
@@ -206,6 +207,7 @@ __global__ void k_apply(Peeled g, long long rows, const double* __restrict__ U, 
   if (OP == OP_V) row_v(g, row, r);
   if (OP == OP_D) row_d(g, row, r);
   if (OP == OP_G) row_g(g, row, r);
+#pragma unroll 4
   for (int j = 0; j < cols; j++) {
     const double* u = U + (size_t)j * ldu;
     double s = 0.0;
@@ -260,13 +262,25 @@ __global__ void __launch_bounds__(kAtbThreads) k_atb(const double* __restrict__ 
     }
 }
 
-// C = sum over the splits, in split order.
-__global__ void k_sum_split(const double* __restrict__ partial, int nsplit, long long count, double* __restrict__ C) {
-  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= count) return;
+// C = sum over the splits: a block per 32 consecutive outputs, its 8 warps
+// taking every 8th split (reads coalesced along the outputs), then the 8
+// partial sums added in warp order, so the result is the same on every run.
+constexpr int kSumWarps = 8;
+__global__ void __launch_bounds__(32 * kSumWarps) k_sum_split(const double* __restrict__ partial, int nsplit,
+                                                              long long count, double* __restrict__ C) {
+  __shared__ double part[kSumWarps][33];
+  const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
+  const long long e = (long long)blockIdx.x * 32 + lane;
   double s = 0.0;
-  for (int p = 0; p < nsplit; p++) s += partial[(size_t)p * count + e];
-  C[e] = s;
+  if (e < count)
+    for (int p = w; p < nsplit; p += kSumWarps) s += partial[(size_t)p * count + e];
+  part[w][lane] = s;
+  __syncthreads();
+  if (w == 0 && e < count) {
+    double t = part[0][lane];
+    for (int k = 1; k < kSumWarps; k++) t += part[k][lane];
+    C[e] = t;
+  }
 }
 
 // M = [A | I] (r x 2r, column-major) from the column-major A.
@@ -343,6 +357,90 @@ __global__ void k_gj_update(double* __restrict__ M, int r, int k, const double* 
   }
 }
 
+// The whole elimination in one block with [A | I] in shared memory, for
+// ranks whose 2 r^2 doubles fit: one launch in place of r launch pairs.  The
+// same pivot choice (first largest |M(i, k)|, i >= k) and the same update
+// arithmetic as k_gj_pivot + k_gj_update.
+constexpr int kGjSmallMax = 96;  // (2 r^2 + 5 r) doubles = 151 KB at r = 96
+constexpr int kGjThreads = 512;
+__global__ void __launch_bounds__(kGjThreads) k_gj_small(const double* __restrict__ A, int r, double* __restrict__ M,
+                                                         int* __restrict__ status) {
+  extern __shared__ double gj[];
+  double* S = gj;                // r x 2r, column-major
+  double* prow = S + 2 * r * r;  // pivot row, 2r
+  double* krow = prow + 2 * r;   // row k, 2r
+  double* kcol = krow + 2 * r;   // column k, r
+  __shared__ double wv[kGjThreads / 32];
+  __shared__ int wi[kGjThreads / 32];
+  __shared__ int piv;
+  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+  const int n2 = 2 * r * r;
+  for (int e = threadIdx.x; e < n2; e += blockDim.x) {
+    const int i = e % r, j = e / r;
+    S[e] = j < r ? A[e] : (j - r == i ? 1.0 : 0.0);
+  }
+  __syncthreads();
+  for (int k = 0; k < r; k++) {
+    double best = -1.0;
+    int bi = r;
+    for (int i = k + threadIdx.x; i < r; i += blockDim.x) {
+      const double v = fabs(S[k * r + i]);
+      if (v > best) {
+        best = v;
+        bi = i;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_down_sync(0xffffffffu, best, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) {
+        best = ov;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      wv[warp] = best;
+      wi[warp] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double b = wv[0];
+      int ii = wi[0];
+      for (int w = 1; w < kGjThreads / 32; w++)
+        if (wv[w] > b || (wv[w] == b && wi[w] < ii)) {
+          b = wv[w];
+          ii = wi[w];
+        }
+      piv = b > 0.0 ? ii : -1;  // zero or NaN pivot: singular
+    }
+    __syncthreads();
+    const int p = piv;
+    if (p < 0) {  // every thread sees the same p and leaves together
+      if (threadIdx.x == 0) status[0] = 1 + k;
+      return;
+    }
+    for (int j = threadIdx.x; j < 2 * r; j += blockDim.x) {
+      prow[j] = S[j * r + p];
+      krow[j] = S[j * r + k];
+    }
+    for (int i = threadIdx.x; i < r; i += blockDim.x) kcol[i] = S[k * r + i];
+    __syncthreads();
+    for (int e = threadIdx.x; e < n2; e += blockDim.x) {
+      const int i = e % r, j = e / r;
+      const double pr = prow[j] / prow[k];
+      if (i == k)
+        S[e] = pr;
+      else if (i == p)
+        S[e] = krow[j] - krow[k] * pr;
+      else
+        S[e] = S[e] - kcol[i] * pr;
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < n2; e += blockDim.x) M[e] = S[e];
+}
+
 }  // namespace products
 }  // namespace plume
 
@@ -364,11 +462,15 @@ struct DevBuf {
   cudaError_t alloc(size_t count) { return cudaMalloc(&p, std::max<size_t>(1, count) * sizeof(double)); }
 };
 
-// How many splits of the K rows keep about four blocks per SM busy.
+// How many splits of the K rows give four blocks to every SM (chunks of at
+// least 256 rows).  With one output tile, as for rank-32 bases, that is
+// exactly 4 x SMs equal chunks: a whole number of blocks per SM, so no SM
+// waits on a partial last wave (352 splits of a 361,336-row basis left 2 or
+// 3 blocks per SM and 70 % of the SMs' throughput).
 int split_count(long long K, int a, int b, int sms) {
   const long long tiles = (long long)((a + kTile - 1) / kTile) * ((b + kTile - 1) / kTile);
   const long long want = (4LL * sms + tiles - 1) / tiles;
-  const long long most = std::max(1LL, K / 1024);
+  const long long most = std::max(1LL, K / 256);
   return (int)std::max(1LL, std::min(std::min(want, most), 65535LL));
 }
 
@@ -383,15 +485,16 @@ struct Projector {
            int a, int b, double* C) {
     if (a == 0 || b == 0) return;
     const int nsplit = split_count(K, a, b, sms);
-    long long chunk = (K + nsplit - 1) / nsplit;
-    chunk = (chunk + kTile - 1) / kTile * kTile;
+    // equal chunks (not rounded to whole 32-row tiles, which would leave the
+    // last splits empty and the SMs unevenly loaded again)
+    const long long chunk = (K + nsplit - 1) / nsplit;
     const dim3 grid((unsigned)((a + kTile - 1) / kTile), (unsigned)((b + kTile - 1) / kTile), (unsigned)nsplit);
     if (nsplit == 1) {
       k_atb<<<grid, kAtbThreads, 0, s>>>(L, lsk, lsi, R, rsk, rsj, K, a, b, chunk, C);
     } else {
       k_atb<<<grid, kAtbThreads, 0, s>>>(L, lsk, lsi, R, rsk, rsj, K, a, b, chunk, partial);
       const long long count = (long long)a * b;
-      k_sum_split<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(partial, nsplit, count, C);
+      k_sum_split<<<(unsigned)((count + 31) / 32), 32 * kSumWarps, 0, s>>>(partial, nsplit, count, C);
     }
     flops += 2.0 * K * a * b;
   }
@@ -486,10 +589,22 @@ extern "C" int plume_reduced_build_products(plume_handle* h, const char* reduced
   pj.atb(Uf.p, 1, m, W.p, 1, m, m, rf, rp, ptov.p);
   // projected.A^-1: Gauss-Jordan on [A | I]
   const long long mcount = 2LL * rp * rp;
-  k_gj_init<<<(unsigned)((mcount + 255) / 256), 256, 0, s>>>(Ar.p, rp, M.p);
-  for (int k = 0; k < rp; k++) {
-    k_gj_pivot<<<1, 256, 0, s>>>(M.p, rp, k, prow.p, krow.p, kcol.p, status);
-    k_gj_update<<<(unsigned)((mcount + 255) / 256), 256, 0, s>>>(M.p, rp, k, prow.p, krow.p, kcol.p, status);
+  if (rp <= kGjSmallMax) {
+    const size_t smem = (2 * (size_t)rp * rp + 5 * (size_t)rp) * sizeof(double);
+    const cudaError_t attr = cudaFuncSetAttribute(
+        k_gj_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)((2 * kGjSmallMax * kGjSmallMax + 5 * kGjSmallMax) * sizeof(double)));
+    if (attr != cudaSuccess) {
+      release();
+      return fail(PLUME_ERR_CUDA, "cannot reserve shared memory for the elimination");
+    }
+    k_gj_small<<<1, kGjThreads, smem, s>>>(Ar.p, rp, M.p, status);
+  } else {
+    k_gj_init<<<(unsigned)((mcount + 255) / 256), 256, 0, s>>>(Ar.p, rp, M.p);
+    for (int k = 0; k < rp; k++) {
+      k_gj_pivot<<<1, 256, 0, s>>>(M.p, rp, k, prow.p, krow.p, kcol.p, status);
+      k_gj_update<<<(unsigned)((mcount + 255) / 256), 256, 0, s>>>(M.p, rp, k, prow.p, krow.p, kcol.p, status);
+    }
   }
   const double gj_flops = 4.0 * rp * (double)rp * rp;
   // inverseProduct = (ptov A^-1) vtod

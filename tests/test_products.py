@@ -74,10 +74,10 @@ def test_mixed_walls_change_the_wall_dependent_operators():
 
 
 def test_restated_operators_are_the_reference_stencils():
-    """Structure of the restated sparse operators on a 6x7x5 grid: flat A is
-    symmetric with zero row sums away from Dirichlet walls, D is symmetric
-    with rows summing to (1 - w) + w/6 x neighbours, V G is the peeled
-    divergence of the gradient (a Laplacian-like symmetric part)."""
+    """Structure of the restated sparse operators on a 6x7x5 grid: flat A and
+    D are symmetric (so the reference's left^T M^T right equals
+    left^T M right for them), D has 1 - w on its diagonal, V and G have the
+    peeled shapes, and G maps a constant pressure to zero velocity."""
     from oracle import products_oracle as po
     res, bc = (6, 7, 5), DEFAULT_BC
     A = po.flat_a(res, bc).toarray()
@@ -191,3 +191,33 @@ def test_build_rejects_missing_bases_and_a_singular_pressure_matrix(tmp_path):
         Up.tofile(f)
     with pytest.raises(PlumeError, match="singular"):
         build_products(g, d)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rank_p", [64, 120])
+def test_gpu_build_matches_restatement_on_random_bases(tmp_path, rank_p):
+    """Seeded random bases on the 10x12x8 grid under the mixed walls, against
+    the scipy restatement: a pressure rank that the one-block elimination
+    handles (64) and one above its shared-memory limit of 96 (120, one launch
+    pair per pivot column)."""
+    from oracle import products_oracle as po
+    from cfs_plume_gb300.plume import build_products
+    res, bc = (10, 12, 8), (0, 1, 1, 0, 1, 0)
+    nint = 8 * 10 * 6
+    rng = np.random.default_rng(rank_p)
+    U = [rng.standard_normal((nint, rank_p)) / np.sqrt(nint)]
+    U += [rng.standard_normal((3 * nint, r)) / np.sqrt(3 * nint) for r in (40, 33, 25)]
+    d = str(tmp_path / "red") + "/"
+    os.makedirs(d)
+    for fn, M in zip(BASES, U):
+        with open(d + fn, "wb") as f:
+            np.array(M.shape, dtype="<i4").tofile(f)
+            M.astype("<f8").tofile(f)
+    info = build_products(_plume(res, bc), d)
+    assert info["ranks"] == (rank_p, 40, 33, 25)
+    want = po.products(res, bc, *U)
+    for name in PRODUCTS:
+        got = _read(d + name + ".matrix")
+        assert got.shape == want[name].shape, name
+        tol = 1e-10 if name == "inverseProduct" else 1e-12
+        assert _rel(got, want[name]) < tol, (name, _rel(got, want[name]))
