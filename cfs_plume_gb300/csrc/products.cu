@@ -292,8 +292,8 @@ __global__ void k_gj_init(const double* __restrict__ A, int r, double* __restric
 }
 
 // Pivot step k: the row p >= k with the largest |M(p, k)| (the first one on
-// ties); copies of row p, row k and column k for the update, so that the
-// update reads nothing it writes.  status[0] = 1 + k when column k has no
+// ties); row p divided by the pivot (the new row k), row k and column k
+// copied for the update, so that the update reads nothing it writes.  status[0] = 1 + k when column k has no
 // nonzero pivot (the matrix is singular); later steps then do nothing.
 __global__ void k_gj_pivot(const double* __restrict__ M, int r, int k, double* __restrict__ prow,
                            double* __restrict__ krow, double* __restrict__ kcol, int* __restrict__ status) {
@@ -328,15 +328,16 @@ __global__ void k_gj_pivot(const double* __restrict__ M, int r, int k, double* _
     if (threadIdx.x == 0) status[0] = 1 + k;
     return;
   }
+  const double pivot = M[(size_t)k * r + p];
   for (int j = threadIdx.x; j < 2 * r; j += blockDim.x) {
-    prow[j] = M[(size_t)j * r + p];
+    prow[j] = M[(size_t)j * r + p] / pivot;  // the new row k, one division per column
     krow[j] = M[(size_t)j * r + k];
   }
   for (int i = threadIdx.x; i < r; i += blockDim.x) kcol[i] = M[(size_t)k * r + i];
   if (threadIdx.x == 0) status[1] = p;
 }
 
-// Update step k: row k <- row p / pivot; row p (when p != k) <- old row k
+// Update step k: row k <- the new row k; row p (when p != k) <- old row k
 // minus its multiple of the new row k; every other row i <- row i -
 // M(i, k) x new row k.
 __global__ void k_gj_update(double* __restrict__ M, int r, int k, const double* __restrict__ prow,
@@ -347,7 +348,7 @@ __global__ void k_gj_update(double* __restrict__ M, int r, int k, const double* 
   if (e >= 2LL * r * r) return;
   const int i = (int)(e % r), j = (int)(e / r);
   const int p = status[1];
-  const double pr = prow[j] / prow[k];
+  const double pr = prow[j];
   if (i == k) {
     M[e] = pr;
   } else if (i == p) {
@@ -420,15 +421,16 @@ __global__ void __launch_bounds__(kGjThreads) k_gj_small(const double* __restric
       if (threadIdx.x == 0) status[0] = 1 + k;
       return;
     }
+    const double pivot = S[k * r + p];
     for (int j = threadIdx.x; j < 2 * r; j += blockDim.x) {
-      prow[j] = S[j * r + p];
+      prow[j] = S[j * r + p] / pivot;  // the new row k, one division per column
       krow[j] = S[j * r + k];
     }
     for (int i = threadIdx.x; i < r; i += blockDim.x) kcol[i] = S[k * r + i];
     __syncthreads();
     for (int e = threadIdx.x; e < n2; e += blockDim.x) {
       const int i = e % r, j = e / r;
-      const double pr = prow[j] / prow[k];
+      const double pr = prow[j];
       if (i == k)
         S[e] = pr;
       else if (i == p)
