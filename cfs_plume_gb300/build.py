@@ -118,6 +118,12 @@ def build(verbose=False, ptxas_info=False):
     if os.path.exists(svd_src) and not _newer(svd_exe, [svd_src, lib] + headers):
         _run(["g++", "-O2", "-std=c++17", "-o", svd_exe, svd_src, "-L" + LIB, "-lplume",
               "-Wl,-rpath,$ORIGIN/../lib"])
+    # the buildProducts stage binary
+    prod_src = os.path.join(CSRC, "products_main.cpp")
+    prod_exe = os.path.join(BIN, "buildProducts")
+    if os.path.exists(prod_src) and not _newer(prod_exe, [prod_src, lib] + headers):
+        _run(["g++", "-O2", "-std=c++17", "-o", prod_exe, prod_src, "-L" + LIB, "-lplume",
+              "-Wl,-rpath,$ORIGIN/../lib"])
     return lib
 
 

@@ -221,3 +221,56 @@ def test_gpu_build_matches_restatement_on_random_bases(tmp_path, rank_p):
         assert got.shape == want[name].shape, name
         tol = 1e-10 if name == "inverseProduct" else 1e-12
         assert _rel(got, want[name]) < tol, (name, _rel(got, want[name]))
+
+
+# ------------------------------------------------- the buildProducts binary
+EXE = os.path.join(os.path.dirname(HERE), "cfs_plume_gb300", "bin", "buildProducts")
+
+
+@pytest.fixture(scope="module")
+def exe():
+    from cfs_plume_gb300 import build
+    build.build()
+    assert os.path.exists(EXE)
+    return EXE
+
+
+def test_binary_usage_without_cfg(exe):
+    import subprocess
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and "Usage:" in r.stdout
+
+
+def test_binary_rejects_a_malformed_cfg_and_iop(exe, tmp_path):
+    import subprocess
+    bad = tmp_path / "bad.cfg"
+    bad.write_text("xres = 10\nno equals sign here\n")
+    r = subprocess.run([exe, str(bad)], capture_output=True, text=True)
+    assert r.returncode == 1 and "Unable to parse" in r.stderr
+    iop = tmp_path / "iop.cfg"
+    iop.write_text("xRes = 10\nyRes = 12\nzRes = 8\niop = 1\nreduced path = %s/\n" % tmp_path)
+    r = subprocess.run([exe, str(iop)], capture_output=True, text=True)
+    assert r.returncode == 1 and "initOutOfCoreIOP" in r.stderr
+
+
+@pytest.mark.gpu
+def test_binary_builds_the_reference_operators(exe, tmp_path):
+    """bin/buildProducts with the reference's cfg keys on the bases and
+    cubature of the exact fixture: the six operators and the cubature cache
+    written under `reduced path` are the reference's."""
+    import subprocess
+    z = np.load(os.path.join(GOLDEN, "ref_reduced_exact_10x12x8.npz"))
+    d = str(tmp_path / "red") + "/"
+    _write(z, d, BASES + ["U.preadvect.matrix", "cubature"])
+    cfg = tmp_path / "products.cfg"
+    cfg.write_text("xRes = 10\nyRes = 12\nzRes = 8\nreduced path = %s\nsnapshot path = %s/snap/\n"
+                   "simulation snapshots = 12\n" % (d, tmp_path))
+    r = subprocess.run([exe, str(cfg)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    for name in PRODUCTS:
+        got = _read(d + name + ".matrix")
+        ref = _matrix(z["file_%s.matrix" % name])
+        tol = 1e-10 if name == "inverseProduct" else 1e-12
+        assert got.shape == ref.shape and _rel(got, ref) < tol, name
+    built = np.fromfile(d + "advection.cubature.cache", dtype=np.uint8)
+    assert np.array_equal(built, z["file_advection.cubature.cache"])
