@@ -292,6 +292,12 @@ def measure_snapshot_svd(res, prec, local, rank, snaps):
     return {"rows": rows, "cols": cols, "kept": kept, "info": info, "wall_s": wall}
 
 
+def hyperplanes(res):
+    """i + j + k hyperplanes of the interior: the length of the MIC(0)
+    recurrence's dependency chain (440 at 128x192x128)."""
+    return sum(int(v) - 2 for v in res) - 2
+
+
 def _write_eigen(path, M):
     """EIGEN::write layout: int32 rows, cols, then the row-major doubles."""
     with open(path, "wb") as f:
@@ -528,6 +534,10 @@ def main():
                      "launches_timed": sweep_launches,
                      "bytes_model": "N_int*(2S+P) per sweep launch",
                      "note": "latency-bound dependency chain (i+j+k wavefront); HBM roof for reference",
+                     # the recurrence's i+j+k hyperplanes over the interior, and
+                     # the sweep time per hyperplane stage
+                     "hyperplanes_per_sweep": hyperplanes(res),
+                     "ns_per_hyperplane": (sweep_avg_ms * 1e6 / hyperplanes(res)) if sweep_avg_ms else None,
                      "pass": "second pass of K steps with CUDA events around each sweep launch "
                              "(host-driven CG loop); value is timed with the CG loop as a CUDA graph"},
         "solve_roofline": {"kernel": "poisson solve (all MIC-PCG kernels)", "achieved": achieved_solve,

@@ -53,3 +53,14 @@ def test_two_replicas_reduce_timing_over_ranks():
         assert rc == 0
     # value = all ranks' steps / slowest rank's time
     assert abs(res[0][2] / (res[0][1] / 1000.0) - 550.0) < 1e-9
+
+
+def test_hyperplane_count_is_the_recurrence_length():
+    """The sweep's hyperplane count in bench.py's roofline: the interior i+j+k
+    planes of the MIC(0) recurrence at every grid of the benchmark sizes."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    sizes = {(32, 32, 32): 88, (48, 64, 48): 152, (64, 96, 64): 216, (96, 128, 96): 312,
+             (128, 192, 128): 440, (256, 384, 256): 888}
+    for res, want in sizes.items():
+        assert bench.hyperplanes(res) == want
