@@ -85,6 +85,7 @@ def build(verbose=False, ptxas_info=False):
         ("products.cu", [nvcc] + common_nv),
         ("plume_api.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-I" + os.path.join(cuda, "include")]),
         ("snapshot.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread"] + zc),
+        ("state_read.cpp", ["g++", "-O2", "-std=c++17", "-fPIC"] + zc),
         ("batch.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread"]),
         # the box state must round after every operation on Arm hosts too
         ("box.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]),

@@ -216,6 +216,8 @@ struct plume_reduced {
   int nblk = 0;
   double dt0 = 0;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  std::string truth;          // full-rank state files to diff against, or empty
+  std::vector<double> errors; // 4 per diffed step
 };
 
 namespace {
@@ -223,6 +225,36 @@ namespace {
 int fail(int code, const std::string& msg) {
   plume::global_error() = msg;
   return code;
+}
+
+// diffGroundTruth (SUBSPACE_FLUID_3D_EIGEN.cpp:804-835), the last call of
+// stepReorderedCubatureStam: the full-rank state file of the frame just
+// stepped, <path>fluid.%04i.fluid3d.gz with frame = total steps - 1, against
+// this step's velocity and density (peeled norms, host side, as in the
+// reference).
+int diff_ground_truth(plume_reduced* r, plume::Engine* e) {
+  const size_t N = (size_t)r->X * r->Y * r->Z;
+  char name[64];
+  snprintf(name, sizeof(name), "fluid.%04d.fluid3d", (int)e->total_steps() - 1);
+  const std::string path = r->truth + name;
+  std::vector<double> vel(3 * N), dens(N), tvel(3 * N), tdens(N);
+  int rc = e->download(PLUME_F_VELOCITY, vel.data(), vel.size());
+  if (rc == PLUME_OK) rc = e->download(PLUME_F_DENSITY, dens.data(), dens.size());
+  if (rc != PLUME_OK) return fail(rc, e->last_error());
+  int32_t res[3] = {0, 0, 0};
+  rc = plume_state_read_field(path.c_str(), PLUME_F_VELOCITY, nullptr, 0, res);
+  if (rc != PLUME_OK) return rc;
+  if (res[0] != r->X || res[1] != r->Y || res[2] != r->Z)
+    return fail(PLUME_ERR_INVALID, "ground truth " + path + " is another grid");
+  rc = plume_state_read_field(path.c_str(), PLUME_F_VELOCITY, tvel.data(), tvel.size(), nullptr);
+  if (rc == PLUME_OK) rc = plume_state_read_field(path.c_str(), PLUME_F_DENSITY, tdens.data(), tdens.size(), nullptr);
+  if (rc != PLUME_OK) return rc;
+  const int32_t grid[3] = {r->X, r->Y, r->Z};
+  double err[4];
+  rc = plume_peeled_errors(grid, vel.data(), dens.data(), tvel.data(), tdens.data(), err);
+  if (rc != PLUME_OK) return rc;
+  r->errors.insert(r->errors.end(), err, err + 4);
+  return PLUME_OK;
 }
 
 }  // namespace
@@ -433,6 +465,21 @@ int plume_reduced_step(plume_reduced* r, plume_step_stats* stats) {
     cudaEventElapsedTime(&ms, r->ev[2], r->ev[1]);
     stats->ms_total = ms;
   }
+  if (!r->truth.empty()) return diff_ground_truth(r, e);
+  return PLUME_OK;
+}
+
+int plume_reduced_set_ground_truth(plume_reduced* r, const char* full_rank_path) {
+  if (!r) return fail(PLUME_ERR_INVALID, "null model");
+  r->truth = full_rank_path ? full_rank_path : "";
+  return PLUME_OK;
+}
+
+int plume_reduced_errors(plume_reduced* r, double* out, int32_t n, int32_t* count) {
+  if (!r || !count) return fail(PLUME_ERR_INVALID, "bad argument");
+  *count = (int32_t)(r->errors.size() / 4);
+  if (out && n > 0)
+    std::copy(r->errors.begin(), r->errors.begin() + std::min<size_t>((size_t)n / 4 * 4, r->errors.size()), out);
   return PLUME_OK;
 }
 

@@ -86,6 +86,11 @@ def load_library(path=LIB_PATH):
         "plume_reduced_qdot": (C.c_int, [H, C.c_void_p, C.c_int32, P(C.c_int32)]),
         "plume_reduced_dims": (C.c_int, [H, P(C.c_int32)]),
         "plume_reduced_build_products": (C.c_int, [H, C.c_char_p, P(PlumeProductsInfo)]),
+        "plume_reduced_set_ground_truth": (C.c_int, [H, C.c_char_p]),
+        "plume_reduced_errors": (C.c_int, [H, C.c_void_p, C.c_int32, P(C.c_int32)]),
+        "plume_state_read_field": (C.c_int, [C.c_char_p, C.c_int32, C.c_void_p, C.c_size_t, P(C.c_int32)]),
+        "plume_peeled_errors": (C.c_int, [P(C.c_int32), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          P(C.c_double)]),
         "plume_snapshots_create": (C.c_int, [H, C.c_int32, C.c_int32, P(H)]),
         "plume_snapshots_destroy": (None, [H]),
         "plume_snapshots_append": (C.c_int, [H, P(C.c_int32)]),
@@ -527,6 +532,34 @@ class Snapshots:
         return pca[:r], kept.value, {f: getattr(info, f) for f, _ in PlumeSvdInfo._fields_}
 
 
+def read_state_field(path, name):
+    """FLUID_3D_MIC::readGz for one field of a state file, on the host
+    (plume_state_read_field): (values, res) with the values as float64 in
+    the reference layout (N, or 3N interleaved for vector fields)."""
+    lib = load_library()
+    res = (C.c_int32 * 3)()
+    _check(lib.plume_state_read_field(os.fsencode(path), 0, None, 0, res))
+    N = res[0] * res[1] * res[2]
+    a = np.empty(3 * N if name in _abi.VECTOR_FIELDS else N, dtype=np.float64)
+    _check(lib.plume_state_read_field(os.fsencode(path), _abi.FIELD_ID[name], a.ctypes.data, a.size, None))
+    return a, tuple(res)
+
+
+def peeled_errors(res, velocity, density, truth_velocity, truth_density):
+    """diffGroundTruth's norms (plume_peeled_errors): velocity abs, velocity
+    relative, density abs, density relative over the interior cells."""
+    lib = load_library()
+    arrs = [np.ascontiguousarray(a, dtype=np.float64).ravel()
+            for a in (velocity, density, truth_velocity, truth_density)]
+    N = int(res[0]) * int(res[1]) * int(res[2])
+    if arrs[0].size != 3 * N or arrs[2].size != 3 * N or arrs[1].size != N or arrs[3].size != N:
+        raise ValueError("fields do not match the grid")
+    r = (C.c_int32 * 3)(*[int(v) for v in res])
+    out = (C.c_double * 4)()
+    _check(lib.plume_peeled_errors(r, *[a.ctypes.data for a in arrs], out))
+    return np.array(list(out))
+
+
 def build_products(plume, reduced_path):
     """The projected operators of a reduced model for the plume's grid and
     walls (plume_reduced_build_products, include/plume_reduced.h; the
@@ -577,6 +610,22 @@ class ReducedModel:
         q = np.empty(n.value)
         _check(self.lib.plume_reduced_qdot(self.h, q.ctypes.data, n.value, C.byref(n)))
         return q
+
+    def set_ground_truth(self, full_rank_path):
+        """diffGroundTruth after every step against <path>fluid.%04i.fluid3d.gz
+        (plume_reduced_set_ground_truth); None turns it off."""
+        p = None if not full_rank_path else os.fsencode(full_rank_path)
+        _check(self.lib.plume_reduced_set_ground_truth(self.h, p))
+
+    def errors(self):
+        """The recorded ground-truth errors, one row per compared step:
+        velocity abs, velocity relative, density abs, density relative."""
+        n = C.c_int32()
+        _check(self.lib.plume_reduced_errors(self.h, None, 0, C.byref(n)))
+        out = np.empty((n.value, 4))
+        if n.value:
+            _check(self.lib.plume_reduced_errors(self.h, out.ctypes.data, out.size, C.byref(n)))
+        return out
 
     def dims(self):
         d = (C.c_int32 * 5)()

@@ -196,6 +196,25 @@ int plume_get_info(plume_handle* h, int32_t res[3], int32_t* total_steps,
    the reference format (gzip level 1) to `path` ('.gz' appended when missing). */
 int plume_write_state(plume_handle* h, const char* path);
 
+/* FLUID_3D_MIC::readGz (FLUID_3D_MIC.cpp:1115-1246) for one field, on the
+   host only (no handle, no device): opens `path` ('.gz' appended unless the
+   name ends in "gz"), returns the file's grid in res (may be NULL) and, when
+   dst is not NULL, copies the field in the reference layout (n = N or 3N
+   doubles, as the file holds it).  The file holds every field id up to
+   PLUME_F_CACHED_DIVERGENCE, PLUME_F_PREVORTICITY and PLUME_F_POST_IOP (empty
+   unless a moving-box step wrote it).  PLUME_ERR_IO for a missing or
+   truncated file, PLUME_ERR_INVALID when n does not match the field,
+   PLUME_ERR_UNSUPPORTED in a build without zlib. */
+int plume_state_read_field(const char* path, int32_t field, double* dst, size_t n, int32_t res[3]);
+
+/* SUBSPACE_FLUID_3D_EIGEN::diffGroundTruth's norms
+   (SUBSPACE_FLUID_3D_EIGEN.cpp:804-835) for full-grid fields in the reference
+   layout: errors = { |peel(u) - peel(u_t)|, that / |peel(u)|,
+   |peel(rho) - peel(rho_t)|, that / |peel(rho)| } over the interior cells.
+   Host only. */
+int plume_peeled_errors(const int32_t res[3], const double* velocity, const double* density,
+                        const double* truth_velocity, const double* truth_density, double errors[4]);
+
 /* FLUID_3D_MIC::appendStreams (FLUID_3D_MIC.cpp:1329-1477): append this step's
    peeled rows to <dir>velocity.{final,preproject,prediffuse,preadvect}.matrix.transpose
    and <dir>pressure.matrix.transpose, and rewrite the six .dims files. */

@@ -3,6 +3,8 @@
  *
  * Replaces, for a C / ctypes caller:
  *   src/integrators/SUBSPACE_FLUID_3D_EIGEN.cpp:243-304  stepReorderedCubatureStam
+ *     (with its closing diffGroundTruth, lines 804-835, when a full-rank path
+ *      is set)
  *     (full-space buoyancy, vorticity and scalar advection, then the velocity in
  *      reduced coordinates: projection on U.preadvect, cubature advection,
  *      reduced damping, staged reduced pressure projection, unprojection on
@@ -74,6 +76,22 @@ void plume_reduced_destroy(plume_reduced* r);
 /* One stepReorderedCubatureStam on the handle's state.  stats (may be NULL):
    launches and the step's device time. */
 int plume_reduced_step(plume_reduced* r, plume_step_stats* stats);
+
+/* diffGroundTruth (SUBSPACE_FLUID_3D_EIGEN.cpp:804-835), which the reference
+   runs at the end of every reduced step: with a full-rank path set (the
+   `snapshot path` of the fluid3D run, with its trailing '/'), every
+   plume_reduced_step then reads <path>fluid.%04i.fluid3d.gz of the frame it
+   just stepped (the handle's step count - 1) and records the peeled velocity
+   and density errors (plume_peeled_errors).  NULL or "" turns it off.  A
+   missing or mismatched file fails that step's call with PLUME_ERR_IO /
+   PLUME_ERR_INVALID after the step itself has run. */
+int plume_reduced_set_ground_truth(plume_reduced* r, const char* full_rank_path);
+
+/* The recorded errors, 4 per compared step (velocity abs, velocity relative,
+   density abs, density relative: the reference's velocityErrorAbs,
+   velocityErrorRelative, densityErrorAbs, densityErrorRelative): *count
+   steps, the first min(n / 4, *count) of them copied to out. */
+int plume_reduced_errors(plume_reduced* r, double* out, int32_t n, int32_t* count);
 
 /* The reduced coordinates after the last step (the reference's _qDot, in the
    U.final basis): *size values written to q when n >= *size. */

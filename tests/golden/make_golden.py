@@ -29,7 +29,8 @@ configurations and stores what it produced:
                         reduced-path files it read or wrote (bases, projected
                         operators, cubature, cubature cache) and the fields,
                         reduced coordinates and ground-truth errors after 12
-                        reduced steps;
+                        reduced steps, and the full-rank state file of the last
+                        frame that the last error compares against;
   ref_products_mixed_10x12x8.npz  the projected operators that the reference's
                         constructor (buildOutOfCoreMatrices) builds from the
                         same bases under mixed walls.
@@ -188,6 +189,8 @@ def reduced_fixtures():
         for k in ("velocity", "density", "heat", "qdot"):
             rec[k] = np.fromfile(out + "." + k + ".f64")
         rec["errors"] = np.fromfile(out + ".errors.f64").reshape(-1, 4)
+        # the full-rank state file of the last frame (diffGroundTruth's input)
+        rec["truth_last"] = np.fromfile(snap + "fluid.%04d.fluid3d.gz" % (steps - 1), dtype=np.uint8)
         np.savez_compressed(os.path.join(HERE, "ref_reduced_%s.npz" % name), **rec)
         print("reduced", name, "qdot", rec["qdot"].size, "errors (last)", rec["errors"][-1])
     # the projected operators of the same bases under other walls: the

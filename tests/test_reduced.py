@@ -6,6 +6,10 @@ operators its constructor built, and two cubature schemes (every interior cell
 with weight 1, which makes the reduced advection an exact Galerkin projection;
 40 seeded cells with seeded weights).
 
+On the host: the ground-truth comparison that ends the reference's step
+(diffGroundTruth), through plume_state_read_field and plume_peeled_errors,
+reproduces the reference's recorded errors within 1e-12.
+
 Tolerances: FP64 fields after 12 reduced steps within 1e-8 relative L2 of the
 reference's (the reduced products sum in a different order: Eigen's GEMV and
 block products against warp-level FMA reductions); the cubature cache built
@@ -81,6 +85,64 @@ def test_exact_cubature_tracks_the_full_rank_run():
     within 1e-4 (velocity) and 1e-7 (density) of the full-rank run."""
     e = _fixture("exact_10x12x8")["errors"]
     assert e[:, 1].max() < 1e-4 and e[:, 3].max() < 1e-7
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_ground_truth_errors_match_the_reference(tmp_path, case):
+    """diffGroundTruth on the host: the reference's last reduced fields
+    against the full-rank state file of frame 11 (read back by
+    plume_state_read_field), through plume_peeled_errors, give the
+    reference's last recorded errors."""
+    from cfs_plume_gb300.plume import peeled_errors, read_state_field
+    z = _fixture(case)
+    path = str(tmp_path / "fluid.0011.fluid3d.gz")
+    z["truth_last"].tofile(path)
+    tv, res = read_state_field(path, "velocity")
+    td, _ = read_state_field(path, "density")
+    assert res == tuple(int(v) for v in z["res"])
+    err = peeled_errors(res, z["velocity"], z["density"], tv, td)
+    ref = z["errors"][-1]
+    assert np.allclose(err, ref, rtol=1e-12, atol=0), (err, ref)
+
+
+def test_state_reader_follows_concatenated_gzip_members(tmp_path):
+    """The state file cut into several gzip members (as the parallel writer
+    emits it) reads back field for field like the single-member original."""
+    import gzip
+    from cfs_plume_gb300.plume import read_state_field
+    z = _fixture("exact_10x12x8")
+    one = str(tmp_path / "one.fluid3d.gz")
+    z["truth_last"].tofile(one)
+    raw = gzip.decompress(z["truth_last"].tobytes())
+    many = str(tmp_path / "many.fluid3d.gz")
+    with open(many, "wb") as f:
+        for k in range(0, len(raw), 7001):
+            f.write(gzip.compress(raw[k:k + 7001], compresslevel=1))
+    for name in ("density", "velocity", "pressure", "prevorticity"):
+        a, _ = read_state_field(one, name)
+        b, _ = read_state_field(many, name)
+        assert np.array_equal(a, b), name
+
+
+def test_state_reader_reports_missing_and_mismatched_requests(tmp_path):
+    from cfs_plume_gb300.plume import PlumeError, load_library, read_state_field
+    with pytest.raises(PlumeError):
+        read_state_field(str(tmp_path / "absent.fluid3d"), "density")
+    z = _fixture("exact_10x12x8")
+    path = str(tmp_path / "fluid.0011.fluid3d.gz")
+    z["truth_last"].tofile(path)
+    with pytest.raises(PlumeError, match="holds 0 values"):  # no moving-box step wrote postIOP
+        read_state_field(path, "postIOP")
+    lib = load_library()
+    buf = np.empty(10)
+    assert lib.plume_state_read_field(os.fsencode(path), 0, buf.ctypes.data, buf.size, None) != 0
+    cut = str(tmp_path / "cut.fluid3d.gz")
+    import gzip
+    raw = gzip.decompress(z["truth_last"].tobytes())
+    with open(cut, "wb") as f:
+        f.write(gzip.compress(raw[:5000]))
+    with pytest.raises(PlumeError, match="truncated"):
+        read_state_field(cut, "velocity")
 
 
 # ------------------------------------------------------------------ GPU tests
