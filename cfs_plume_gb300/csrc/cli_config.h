@@ -4,6 +4,8 @@
 #include <sys/stat.h>
 
 #include <cctype>
+#include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <fstream>
 #include <map>
@@ -68,6 +70,29 @@ class Config {
   }
   std::map<std::string, std::string> vals_;
 };
+
+// One JSON object per step for the `log file` cfg key: the step index and
+// every plume_step_stats field (non-finite numbers as null).
+template <typename Stats>
+std::string step_json(int step, const Stats& st) {
+  auto num = [](double v) {
+    if (!std::isfinite(v)) return std::string("null");
+    char b[40];
+    snprintf(b, sizeof(b), "%.17g", v);
+    return std::string(b);
+  };
+  std::string s = "{\"step\": " + std::to_string(step);
+  s += ", \"iterations\": " + std::to_string(st.iterations);
+  s += ", \"converged\": " + std::to_string(st.converged);
+  s += ", \"fallback\": " + std::to_string(st.fallback);
+  s += ", \"launches\": " + std::to_string(st.launches);
+  s += ", \"max_residual\": " + num(st.max_residual);
+  s += ", \"rel_residual\": " + num(st.rel_residual);
+  s += ", \"rhs_norm\": " + num(st.rhs_norm);
+  s += ", \"ms_total\": " + num(st.ms_total);
+  s += ", \"ms_solve\": " + num(st.ms_solve) + "}";
+  return s;
+}
 
 // fluid3D.cpp:40-47: create every prefix of the path
 inline void ensure_directory(const std::string& path) {

@@ -743,6 +743,10 @@ class EngineT : public Engine {
     net_ = net;
     return PLUME_OK;
   }
+  void set_clock(int32_t steps, double time) override {
+    total_steps_ = steps;
+    total_time_ = time;
+  }
   int32_t total_steps() const override { return total_steps_; }
   double total_time() const override { return total_time_; }
   double dx() const override { return dx_; }

@@ -74,6 +74,8 @@ class Engine {
   virtual double dx() const = 0;
   virtual const plume_params& params() const = 0;
   virtual std::string& last_error() = 0;
+  // The step counter and time, as a state file being resumed holds them.
+  virtual void set_clock(int32_t steps, double time) = 0;
 };
 
 // box.cpp: half lengths, angular and displacement velocity of a box for the

@@ -17,7 +17,11 @@
 //   mic tau (0.97), mic sigma (0.25), damping (0.9), warm start (zero |
 //   previous | learned), warm start network (path of a trained network for
 //   "learned"; default cfs_plume_gb300/weights/unet_warmstart.bin next to the
-//   binary's ../weights), write state (1), write streams (1), device (0).
+//   binary's ../weights), write state (1), write streams (1), device (0),
+//   resume from (a state file of an earlier run of the same cfg: its fields and
+//   step count are restored, plume_read_state, and the run continues from the
+//   step after it; empty: start from rest), log file (append one JSON object
+//   per step with the step's plume_step_stats; empty: no log).
 #include <sys/stat.h>
 
 #include <cctype>
@@ -108,6 +112,27 @@ int main(int argc, char* argv[]) {
   const bool write_streams = cfg.integer("write streams", 1) != 0;
   std::string snapshot_path = cfg.str("snapshot path", "./data/dummy/");
   const int snapshots = cfg.integer("simulation snapshots", 20);
+  // checkpoint / resume: a state file of an earlier run of the same cfg
+  const std::string resume = cfg.str("resume from", "");
+  // one JSON object per step (step_json)
+  const std::string log_path = cfg.str("log file", "");
+  int first_step = 0;
+  if (!resume.empty()) {  // the file is checked on the host before any device work
+    int32_t ints[10];
+    double consts[7];
+    if (check(plume_state_read_header(resume.c_str(), ints, consts), nullptr, "resume from") != PLUME_OK) return 1;
+    if (ints[0] != p.res[0] || ints[1] != p.res[1] || ints[2] != p.res[2]) {
+      std::cerr << " resume from: " << resume << " holds a " << ints[0] << "x" << ints[1] << "x" << ints[2]
+                << " grid, the cfg a " << p.res[0] << "x" << p.res[1] << "x" << p.res[2] << " one" << std::endl;
+      return 1;
+    }
+    first_step = ints[9];
+  }
+  std::FILE* log = nullptr;
+  if (!log_path.empty() && !(log = std::fopen(log_path.c_str(), "a"))) {
+    std::cerr << " log file: cannot open " << log_path << std::endl;
+    return 1;
+  }
 
   std::cout << " Using resoluion: " << p.res[0] << " " << p.res[1] << " " << p.res[2] << std::endl;
   std::cout << " Using vorticity: " << p.vorticity_eps << std::endl;
@@ -130,7 +155,11 @@ int main(int argc, char* argv[]) {
     std::cout << " Using learned warm start: " << net_path << std::endl;
   }
   int rc = PLUME_OK;
-  for (int step = 0; step < snapshots && rc == PLUME_OK; step++) {  // fluid3D.cpp:357-398
+  if (!resume.empty()) {
+    rc = check(plume_read_state(h, resume.c_str()), h, "resume from");
+    if (rc == PLUME_OK) std::cout << " Resuming after step " << first_step << " from " << resume << std::endl;
+  }
+  for (int step = first_step; step < snapshots && rc == PLUME_OK; step++) {  // fluid3D.cpp:357-398
     std::cout << " Simulation step " << 1 + step << " of " << snapshots << std::endl;
     plume_step_stats st;
     rc = check(plume_add_source(h, step), h, "add_source");
@@ -139,12 +168,17 @@ int main(int argc, char* argv[]) {
     std::cout << "   " << st.iterations << " iterations converged to inf norm: " << st.max_residual
               << " relative two norm: " << st.rel_residual << "  (" << st.ms_total << " ms)"
               << std::endl;
+    if (log) {
+      std::fprintf(log, "%s\n", plume_cli::step_json(step, st).c_str());
+      std::fflush(log);
+    }
     // writeGz + appendStreams (fluid3D.cpp:376-386) on the handle's writer
     // thread, overlapping the next steps
     const int what = (write_state ? 1 : 0) | (write_streams ? 2 : 0);
     if (what) rc = check(plume_snapshot_async(h, snapshot_path.c_str(), step, what), h, "snapshot");
   }
   if (rc == PLUME_OK) rc = check(plume_wait_snapshots(h), h, "snapshot");
+  if (log) std::fclose(log);
   plume_destroy(h);
   plume_net_destroy(net);  // after the handle that used it
   return rc == PLUME_OK ? 0 : 1;

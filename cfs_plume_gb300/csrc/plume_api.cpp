@@ -17,6 +17,7 @@
 #include "../../include/plume_box.h"
 #include "../../include/plume_solver.h"
 #include "engine.h"
+#include "state_read.h"
 #include "snapshot.h"
 
 // Background writer of one handle: snapshot jobs run in call order on one
@@ -231,6 +232,45 @@ int plume_upload(plume_handle* h, int32_t field, const double* src, size_t n) {
 int plume_download_obstacles(plume_handle* h, uint8_t* dst, size_t n) {
   if (!h) return PLUME_ERR_INVALID;
   return from_engine(h, h->eng->download_obstacles(dst, n));
+}
+
+int plume_read_state(plume_handle* h, const char* path) {
+  if (!h) return PLUME_ERR_INVALID;
+  if (!path) return set_err(h, PLUME_ERR_INVALID, "null path");
+  int32_t ints[10];
+  double consts[7];
+  int rc = plume_state_read_header(path, ints, consts);
+  if (rc != PLUME_OK) return set_err(h, rc, plume::global_error());
+  const plume_params& p = h->eng->params();
+  if (ints[0] != p.res[0] || ints[1] != p.res[1] || ints[2] != p.res[2])
+    return set_err(h, PLUME_ERR_INVALID,
+                   std::string("the state file's grid ") + std::to_string(ints[0]) + "x" + std::to_string(ints[1]) +
+                       "x" + std::to_string(ints[2]) + " is not the handle's");
+  // header doubles: dx, totalTime, dt, buoyancy, vorticityEps (lines 1150-1160)
+  if (consts[0] != h->eng->dx() || consts[2] != p.dt || consts[3] != p.buoyancy || consts[4] != p.vorticity_eps)
+    return set_err(h, PLUME_ERR_INVALID,
+                   "the state file was written with another dx, dt, buoyancy or vorticityEps than the handle's");
+  const size_t N = (size_t)p.res[0] * p.res[1] * p.res[2];
+  const int scalars[5] = {PLUME_F_DENSITY, PLUME_F_DENSITY_OLD, PLUME_F_HEAT, PLUME_F_HEAT_OLD, PLUME_F_PRESSURE};
+  const int vectors[2] = {PLUME_F_VELOCITY, PLUME_F_VELOCITY_OLD};
+  std::vector<std::vector<double>> bufs(7);
+  plume::StateRequest req;
+  for (int k = 0; k < 5; k++) {
+    bufs[k].resize(N);
+    req.push_back({scalars[k], bufs[k].data(), N});
+  }
+  for (int k = 0; k < 2; k++) {
+    bufs[5 + k].resize(3 * N);
+    req.push_back({vectors[k], bufs[5 + k].data(), 3 * N});
+  }
+  rc = plume::read_state_fields(path, req, nullptr);
+  if (rc != PLUME_OK) return set_err(h, rc, plume::global_error());
+  for (const plume::StateField& w : req) {
+    rc = from_engine(h, h->eng->upload(w.field, w.dst, w.n));
+    if (rc != PLUME_OK) return rc;
+  }
+  h->eng->set_clock(ints[9], consts[1]);
+  return PLUME_OK;
 }
 
 int plume_get_info(plume_handle* h, int32_t res[3], int32_t* total_steps, double* total_time,

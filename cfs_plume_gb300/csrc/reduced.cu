@@ -22,6 +22,7 @@
 #include "../../include/plume_reduced.h"
 #include "engine.h"
 #include "matrix_file.cuh"
+#include "state_read.h"
 
 namespace plume {
 namespace reduced {
@@ -246,8 +247,8 @@ int diff_ground_truth(plume_reduced* r, plume::Engine* e) {
   if (rc != PLUME_OK) return rc;
   if (res[0] != r->X || res[1] != r->Y || res[2] != r->Z)
     return fail(PLUME_ERR_INVALID, "ground truth " + path + " is another grid");
-  rc = plume_state_read_field(path.c_str(), PLUME_F_VELOCITY, tvel.data(), tvel.size(), nullptr);
-  if (rc == PLUME_OK) rc = plume_state_read_field(path.c_str(), PLUME_F_DENSITY, tdens.data(), tdens.size(), nullptr);
+  rc = plume::read_state_fields(path, {{PLUME_F_DENSITY, tdens.data(), tdens.size()},
+                                       {PLUME_F_VELOCITY, tvel.data(), tvel.size()}}, nullptr);
   if (rc != PLUME_OK) return rc;
   const int32_t grid[3] = {r->X, r->Y, r->Z};
   double err[4];

@@ -19,6 +19,7 @@
 
 #include "../../include/plume.h"
 #include "engine.h"
+#include "state_read.h"
 
 #ifdef PLUME_HAVE_ZLIB
 #include <zlib.h>
@@ -97,21 +98,20 @@ int field_record(gzFile f, bool vec, double* dst, size_t n, bool keep, std::vect
 
 }  // namespace
 
-extern "C" {
+namespace plume {
 
-int plume_state_read_field(const char* path, int32_t field, double* dst, size_t n, int32_t res[3]) {
-  if (!path) return fail(PLUME_ERR_INVALID, "null path");
-  if (dst && (field < 0 || field >= PLUME_F_COUNT)) return fail(PLUME_ERR_INVALID, "unknown field");
+int read_state_fields(const std::string& path, const StateRequest& want, int32_t res[3]) {
 #ifndef PLUME_HAVE_ZLIB
-  (void)field;
-  (void)dst;
-  (void)n;
+  (void)path;
+  (void)want;
   (void)res;
   return fail(PLUME_ERR_UNSUPPORTED, "built without zlib: state files cannot be read");
 #else
   // readGz appends ".gz" unless the name already ends in "gz" (lines 1119-1121)
   std::string fn = path;
   if (fn.size() < 2 || fn[fn.size() - 1] != 'z' || fn[fn.size() - 2] != 'g') fn += ".gz";
+  for (const StateField& w : want)
+    if (w.field < 0 || w.field >= PLUME_F_COUNT || !w.dst) return fail(PLUME_ERR_INVALID, "bad field request");
   gzFile f = gzopen(fn.c_str(), "rb");
   if (!f) return fail(PLUME_ERR_IO, "could not open " + fn);
   std::vector<char> scratch((size_t)1 << 20);
@@ -122,29 +122,62 @@ int plume_state_read_field(const char* path, int32_t field, double* dst, size_t 
     rc = fail(PLUME_ERR_IO, "truncated state file " + fn);
   if (rc == PLUME_OK && res)
     for (int k = 0; k < 3; k++) res[k] = ints[k];
-  if (rc == PLUME_OK && dst) {
-    bool done = false;
-    // the main block, in plume_field order
-    for (int k = PLUME_F_DENSITY; rc == PLUME_OK && !done && k <= PLUME_F_CACHED_DIVERGENCE; k++) {
-      rc = field_record(f, is_vector(k), dst, n, k == field, scratch, fn);
-      done = k == field;
-    }
-    if (rc == PLUME_OK && !done) {
-      // obstacles, center and lengths, the IOP count
-      int32_t iop_count = 0;
-      if (ints[7] < 0 || !skip_bytes(f, (size_t)ints[7] + 6 * sizeof(double), scratch) ||
-          !read_bytes(f, &iop_count, sizeof(iop_count)))
-        rc = fail(PLUME_ERR_IO, "truncated state file " + fn);
-      // prevorticity, midMaccormack (no plume_field), postIOP
-      if (rc == PLUME_OK) rc = field_record(f, true, dst, n, field == PLUME_F_PREVORTICITY, scratch, fn);
-      done = field == PLUME_F_PREVORTICITY;
-      if (rc == PLUME_OK && !done) rc = field_record(f, true, dst, n, false, scratch, fn);
-      if (rc == PLUME_OK && !done) rc = field_record(f, true, dst, n, field == PLUME_F_POST_IOP, scratch, fn);
-    }
+  // the request for one field id, or null
+  auto find = [&](int id) -> const StateField* {
+    for (const StateField& w : want)
+      if (w.field == id) return &w;
+    return nullptr;
+  };
+  size_t left = want.size();
+  auto record = [&](int id, bool vec) {
+    const StateField* w = id >= 0 ? find(id) : nullptr;
+    rc = field_record(f, vec, w ? w->dst : nullptr, w ? w->n : 0, w != nullptr, scratch, fn);
+    if (w) left--;
+  };
+  // the main block, in plume_field order
+  for (int k = PLUME_F_DENSITY; rc == PLUME_OK && left > 0 && k <= PLUME_F_CACHED_DIVERGENCE; k++)
+    record(k, is_vector(k));
+  if (rc == PLUME_OK && left > 0) {
+    // obstacles, center and lengths, the IOP count
+    int32_t iop_count = 0;
+    if (ints[7] < 0 || !skip_bytes(f, (size_t)ints[7] + 6 * sizeof(double), scratch) ||
+        !read_bytes(f, &iop_count, sizeof(iop_count)))
+      rc = fail(PLUME_ERR_IO, "truncated state file " + fn);
+    // prevorticity, midMaccormack (no plume_field), postIOP
+    if (rc == PLUME_OK && left > 0) record(PLUME_F_PREVORTICITY, true);
+    if (rc == PLUME_OK && left > 0) record(-1, true);
+    if (rc == PLUME_OK && left > 0) record(PLUME_F_POST_IOP, true);
   }
   gzclose(f);
   return rc;
 #endif
+}
+
+}  // namespace plume
+
+extern "C" {
+
+int plume_state_read_header(const char* path, int32_t ints[10], double consts[7]) {
+  if (!path || !ints || !consts) return fail(PLUME_ERR_INVALID, "bad argument");
+#ifndef PLUME_HAVE_ZLIB
+  return fail(PLUME_ERR_UNSUPPORTED, "built without zlib: state files cannot be read");
+#else
+  std::string fn = path;
+  if (fn.size() < 2 || fn[fn.size() - 1] != 'z' || fn[fn.size() - 2] != 'g') fn += ".gz";
+  gzFile f = gzopen(fn.c_str(), "rb");
+  if (!f) return fail(PLUME_ERR_IO, "could not open " + fn);
+  const bool ok = read_bytes(f, ints, 10 * sizeof(int32_t)) && read_bytes(f, consts, 7 * sizeof(double));
+  gzclose(f);
+  return ok ? PLUME_OK : fail(PLUME_ERR_IO, "truncated state file " + fn);
+#endif
+}
+
+int plume_state_read_field(const char* path, int32_t field, double* dst, size_t n, int32_t res[3]) {
+  if (!path) return fail(PLUME_ERR_INVALID, "null path");
+  if (dst && (field < 0 || field >= PLUME_F_COUNT)) return fail(PLUME_ERR_INVALID, "unknown field");
+  plume::StateRequest req;
+  if (dst) req.push_back({field, dst, n});
+  return plume::read_state_fields(path, req, res);
 }
 
 int plume_peeled_errors(const int32_t res[3], const double* velocity, const double* density,

@@ -89,6 +89,8 @@ def load_library(path=LIB_PATH):
         "plume_reduced_set_ground_truth": (C.c_int, [H, C.c_char_p]),
         "plume_reduced_errors": (C.c_int, [H, C.c_void_p, C.c_int32, P(C.c_int32)]),
         "plume_state_read_field": (C.c_int, [C.c_char_p, C.c_int32, C.c_void_p, C.c_size_t, P(C.c_int32)]),
+        "plume_state_read_header": (C.c_int, [C.c_char_p, P(C.c_int32), P(C.c_double)]),
+        "plume_read_state": (C.c_int, [H, C.c_char_p]),
         "plume_peeled_errors": (C.c_int, [P(C.c_int32), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           P(C.c_double)]),
         "plume_snapshots_create": (C.c_int, [H, C.c_int32, C.c_int32, P(H)]),
@@ -176,6 +178,12 @@ class Plume:
         a = np.empty(3 * self.N if vec else self.N, dtype=np.float64)
         _check(self.lib.plume_download(self.h, fid, a.ctypes.data, a.size), self.h)
         return a
+
+    def read_state(self, path):
+        """FLUID_3D_MIC::readGz into this plume (plume_read_state): restores
+        the fields and step count of a state file of the same grid and
+        parameters, so that stepping continues the run that wrote it."""
+        _check(self.lib.plume_read_state(self.h, os.fsencode(path)), self.h)
 
     def set_field(self, name, values):
         a = np.ascontiguousarray(values, dtype=np.float64).ravel()
@@ -387,6 +395,9 @@ class FLUID_3D_MIC:
 
     def writeGz(self, filename):
         self.plume.write_state(filename)
+
+    def readGz(self, filename):
+        self.plume.read_state(filename)
 
     def appendStreams(self):
         if not self.snapshotPath:

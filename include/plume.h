@@ -207,6 +207,21 @@ int plume_write_state(plume_handle* h, const char* path);
    PLUME_ERR_UNSUPPORTED in a build without zlib. */
 int plume_state_read_field(const char* path, int32_t field, double* dst, size_t n, int32_t res[3]);
 
+/* The header of a state file (FLUID_3D_MIC.cpp:1134-1160), host only:
+   ints = xRes, yRes, zRes, maxRes, xs, ys, zs, totalCells, slabSize,
+   totalSteps; consts = dx, totalTime, dt, buoyancy, vorticityEps,
+   heatDiffusion, solverEps. */
+int plume_state_read_header(const char* path, int32_t ints[10], double consts[7]);
+
+/* FLUID_3D_MIC::readGz into a handle: the state file as a checkpoint.  The
+   file's grid must be the handle's, and its dx, dt, buoyancy and vorticityEps
+   must equal the handle's parameters (PLUME_ERR_INVALID otherwise; the file
+   holds no wall flags, which stay the handle's).  Restores density, heat,
+   velocity, their Old copies, pressure, and the step count and time; every
+   other field is rebuilt by the next step, so stepping on continues the run
+   that wrote the file (a learned warm start's iteration cap restarts). */
+int plume_read_state(plume_handle* h, const char* path);
+
 /* SUBSPACE_FLUID_3D_EIGEN::diffGroundTruth's norms
    (SUBSPACE_FLUID_3D_EIGEN.cpp:804-835) for full-grid fields in the reference
    layout: errors = { |peel(u) - peel(u_t)|, that / |peel(u)|,

@@ -83,3 +83,60 @@ def test_cli_learned_warm_start(exe, tmp_path):
            for line in r.stdout.splitlines() if "relative two norm:" in line]
     assert len(rel) == 3 and all(v <= 1e-6 for v in rel)
     assert os.path.exists(snap + "fluid.0002.fluid3d.gz")
+
+
+def test_resume_from_a_missing_or_foreign_state_file_is_refused(exe, tmp_path):
+    """`resume from` is checked on the host before any device work: a missing
+    file, and a state file of another grid (the reference's own 8x10x6 file
+    under a 12x14x10 cfg), end the run with status 1 and a message."""
+    cfg = tmp_path / "resume.cfg"
+    cfg.write_text("xRes = 12\nyRes = 14\nzRes = 10\nresume from = %s\nsnapshot path = %s/s/\n"
+                   % (tmp_path / "absent.fluid3d.gz", tmp_path))
+    r = subprocess.run([exe, str(cfg)], capture_output=True, text=True)
+    assert r.returncode == 1 and "resume from" in r.stderr and "could not open" in r.stderr
+    ref = os.path.join(ROOT, "tests", "golden", "ref_state_8x10x6", "fluid.0001.fluid3d.gz")
+    cfg.write_text("xRes = 12\nyRes = 14\nzRes = 10\nresume from = %s\nsnapshot path = %s/s/\n"
+                   % (ref, tmp_path))
+    r = subprocess.run([exe, str(cfg)], capture_output=True, text=True)
+    assert r.returncode == 1 and "8x10x6" in r.stderr
+
+
+def test_step_log_lines_are_json(tmp_path):
+    """The `log file` line format (plume_cli::step_json), compiled from the
+    binary's own header into a tiny program: every stats field, non-finite
+    numbers as null, one parseable JSON object per line."""
+    import json
+    src = tmp_path / "t.cpp"
+    src.write_text(
+        '#include "cli_config.h"\n#include <cmath>\n#include <cstdio>\n'
+        'struct S { int iterations, converged, fallback, launches; double max_residual, rel_residual,'
+        ' rhs_norm, ms_total, ms_solve; };\n'
+        'int main() { S a{93, 1, 0, 471, 8.5e-11, 9.75e-7, 3.25, 29.8125, 21.5};\n'
+        '  S b{1000, 0, 1, 5, NAN, INFINITY, 0.0, 1.0, 0.5};\n'
+        '  std::printf("%s\\n%s\\n", plume_cli::step_json(7, a).c_str(), plume_cli::step_json(8, b).c_str()); }\n')
+    out = tmp_path / "t"
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "cfs_plume_gb300", "csrc"), str(src), "-o",
+                    str(out)], check=True)
+    lines = subprocess.run([str(out)], capture_output=True, text=True, check=True).stdout.splitlines()
+    a, b = (json.loads(l) for l in lines)
+    assert a == {"step": 7, "iterations": 93, "converged": 1, "fallback": 0, "launches": 471,
+                 "max_residual": 8.5e-11, "rel_residual": 9.75e-7, "rhs_norm": 3.25, "ms_total": 29.8125,
+                 "ms_solve": 21.5}
+    assert b["max_residual"] is None and b["rel_residual"] is None and b["step"] == 8 and b["fallback"] == 1
+
+
+def test_state_header_reads_like_the_reference_file():
+    """plume_state_read_header on the reference's own state files: the 10
+    header ints and 7 doubles of FLUID_3D_MIC::readGz."""
+    import ctypes as C
+    from cfs_plume_gb300.plume import load_library
+    lib = load_library()
+    for rel in ("ref_state_8x10x6/fluid.0001.fluid3d.gz", "ref_moving_state_10x12x8/fluid.0001.fluid3d.gz"):
+        path = os.path.join(ROOT, "tests", "golden", rel)
+        ints = (C.c_int32 * 10)()
+        dbls = (C.c_double * 7)()
+        lib.plume_state_read_header.restype = C.c_int
+        assert lib.plume_state_read_header(os.fsencode(path), ints, dbls) == 0
+        ref = read_state(path)
+        assert tuple(ints) == tuple(ref["header_ints"])
+        assert tuple(dbls) == tuple(ref["header_doubles"])
