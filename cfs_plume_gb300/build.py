@@ -119,12 +119,13 @@ def build(verbose=False, ptxas_info=False):
     if os.path.exists(svd_src) and not _newer(svd_exe, [svd_src, lib] + headers):
         _run(["g++", "-O2", "-std=c++17", "-o", svd_exe, svd_src, "-L" + LIB, "-lplume",
               "-Wl,-rpath,$ORIGIN/../lib"])
-    # the buildProducts stage binary
-    prod_src = os.path.join(CSRC, "products_main.cpp")
-    prod_exe = os.path.join(BIN, "buildProducts")
-    if os.path.exists(prod_src) and not _newer(prod_exe, [prod_src, lib] + headers):
-        _run(["g++", "-O2", "-std=c++17", "-o", prod_exe, prod_src, "-L" + LIB, "-lplume",
-              "-Wl,-rpath,$ORIGIN/../lib"])
+    # the buildProducts and reduced3D stage binaries
+    for src_name, exe_name in (("products_main.cpp", "buildProducts"), ("reduced_main.cpp", "reduced3D")):
+        src = os.path.join(CSRC, src_name)
+        exe_path = os.path.join(BIN, exe_name)
+        if os.path.exists(src) and not _newer(exe_path, [src, lib] + headers):
+            _run(["g++", "-O2", "-std=c++17", "-o", exe_path, src, "-L" + LIB, "-lplume",
+                  "-Wl,-rpath,$ORIGIN/../lib"])
     return lib
 
 

@@ -63,7 +63,7 @@ int main(int argc, char* argv[]) {
   plume_handle* h = nullptr;
   if (check(plume_create(&p, &h), nullptr, "plume_create") != PLUME_OK) return 1;
   plume_reduced* m = nullptr;
-  const int rc = check(plume_reduced_create(h, reduced.c_str(), &m), h, "building the reduced model");
+  const int rc = check(plume_reduced_create(h, reduced.c_str(), &m), nullptr, "building the reduced model");
   if (rc == PLUME_OK) {
     int32_t dims[5] = {0, 0, 0, 0, 0};
     plume_reduced_dims(m, dims);

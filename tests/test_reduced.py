@@ -205,3 +205,26 @@ def test_reduced_model_rejects_mismatched_files(tmp_path):
     os.remove(d + "U.pressure.matrix")
     with pytest.raises(PlumeError):
         ReducedModel(Plume(_abi.default_params(res=(10, 12, 8))), d)
+
+
+# ------------------------------------------------------ the reduced3D binary
+RED_EXE = os.path.join(os.path.dirname(GOLDEN), "..", "cfs_plume_gb300", "bin", "reduced3D")
+
+
+def test_reduced3d_binary_command_line(tmp_path):
+    """bin/reduced3D: the reference's usage line, the cfg parser's errors, and
+    the refusal of the IOP model, all before any device work."""
+    import subprocess
+    from cfs_plume_gb300 import build
+    build.build()
+    exe = os.path.abspath(RED_EXE)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and "Usage:" in r.stdout
+    bad = tmp_path / "bad.cfg"
+    bad.write_text("xres = 10\nno equals sign\n")
+    r = subprocess.run([exe, str(bad)], capture_output=True, text=True)
+    assert r.returncode == 1 and "Unable to parse" in r.stderr
+    iop = tmp_path / "iop.cfg"
+    iop.write_text("xRes = 10\nyRes = 12\nzRes = 8\niop = 1\n")
+    r = subprocess.run([exe, str(iop)], capture_output=True, text=True)
+    assert r.returncode == 1 and "initOutOfCoreIOP" in r.stderr
