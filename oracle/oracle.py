@@ -37,6 +37,7 @@ def load():
         "orc_destroy": (None, [H]),
         "orc_add_source": (None, [H, C.c_int32]),
         "orc_step": (None, [H, P(PlumeStepStats)]),
+        "orc_reduced_prestep": (None, [H]),
         "orc_get": (C.c_int, [H, C.c_int32, C.c_void_p, C.c_size_t]),
         "orc_set": (C.c_int, [H, C.c_int32, C.c_void_p, C.c_size_t]),
         "orc_get_obstacles": (C.c_int, [H, C.c_void_p, C.c_size_t]),
@@ -91,6 +92,12 @@ class Oracle:
         st = PlumeStepStats()
         self.lib.orc_step(self.h, C.byref(st))
         return st
+
+    def reduced_prestep(self):
+        """The full-space part of the reference's reduced step (buoyancy,
+        vorticity, density and heat advection); reduced_oracle.py does the
+        rest."""
+        self.lib.orc_reduced_prestep(self.h)
 
     def field(self, name):
         n = 3 * self.N if name in _abi.VECTOR_FIELDS else self.N

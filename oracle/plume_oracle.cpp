@@ -804,6 +804,35 @@ void orc_step(orc_handle* h, plume_step_stats* st) {
   h->totalSteps++;
 }
 
+// SUBSPACE_FLUID_3D_EIGEN::stepReorderedCubatureStam, lines 243-268, up to the
+// projection of the velocity onto the reduced basis
+void orc_reduced_prestep(orc_handle* h) {
+  const Grid& g = h->g;
+  h->dt = 0.1;  // _dt = goalTime (lines 246-250)
+  std::fill(h->force.begin(), h->force.end(), 0.0);
+  vec_set_zero_border(g, h->velocity.data());
+  // addBuoyancy (FLUID_3D_MIC.cpp:491-502) and the axpy
+  const Real beta = h->p.buoyancy;
+  if (beta != 0.)
+    for (int i = 0; i < g.N; i++) h->force[3 * i + 1] += beta * h->heat[i];
+  vec_axpy(g, h->dt, h->velocity.data(), h->force.data());
+  std::fill(h->force.begin(), h->force.end(), 0.0);
+  add_vorticity(*h);
+  vec_axpy(g, h->dt, h->velocity.data(), h->force.data());
+  // advectHeatAndDensityStam (lines 573-601): the velocity's face conditions,
+  // then density and heat advected by the current velocity
+  velocity_bcs(*h, 1);
+  h->density.swap(h->densityOld);
+  h->heat.swap(h->heatOld);
+  const Real dt0 = h->dt / h->dx;
+  advect(g, dt0, h->velocity.data(), h->densityOld.data(), h->density.data(), 1, 0);
+  advect(g, dt0, h->velocity.data(), h->heatOld.data(), h->heat.data(), 1, 0);
+  sca_set_zero_border(g, h->density.data());
+  sca_set_zero_border(g, h->heat.data());
+  h->totalTime += 0.1;
+  h->totalSteps++;
+}
+
 // ------------------------------------------------------------- moving box
 // BOX (src/geometry/BOX.cpp) restated on the plume_box struct.
 namespace {

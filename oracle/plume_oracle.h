@@ -32,6 +32,12 @@ orc_handle* orc_create(const plume_params* p);
 void orc_destroy(orc_handle* h);
 void orc_add_source(orc_handle* h, int32_t step_index);
 void orc_step(orc_handle* h, plume_step_stats* stats);
+
+/* The full-space part of SUBSPACE_FLUID_3D_EIGEN::stepReorderedCubatureStam
+   (SUBSPACE_FLUID_3D_EIGEN.cpp:243-268): velocity border wiped, buoyancy,
+   vorticity confinement, then advectHeatAndDensityStam (573-601).  The
+   reduced part is oracle/reduced_oracle.py; the step counter advances here. */
+void orc_reduced_prestep(orc_handle* h);
 /* field = plume_field; n = N or 3N doubles. Returns 0 on success. */
 int orc_get(orc_handle* h, int32_t field, double* dst, size_t n);
 int orc_set(orc_handle* h, int32_t field, const double* src, size_t n);

@@ -80,6 +80,25 @@ def test_reference_cubature_cache_layout(case):
     assert off == len(cache)
 
 
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_restatement_matches_the_reference(tmp_path, case):
+    """oracle/reduced_oracle.py (the C oracle's full-space prestep and the
+    numpy reduced part) against the reference's own 12-step run: density and
+    heat identical, velocity and q within 1e-12 (the reduced products sum in
+    another order than Eigen's)."""
+    from cfs_plume_gb300 import _abi
+    from oracle import reduced_oracle
+    z = _fixture(case)
+    d = str(tmp_path / "red") + "/"
+    _write_model(z, d)
+    p = _abi.default_params(res=tuple(int(v) for v in z["res"]), vorticity_eps=float(z["vorticity_eps"]))
+    o, q = reduced_oracle.run(p, d, int(z["steps"]))
+    assert np.array_equal(o.field("density"), z["density"])
+    assert np.array_equal(o.field("heat"), z["heat"])
+    assert rel_l2(o.field("velocity"), z["velocity"]) < 1e-12
+    assert rel_l2(q, z["qdot"]) < 1e-12
+
+
 def test_exact_cubature_tracks_the_full_rank_run():
     """With every cell as a cubature point the reference's reduced run stays
     within 1e-4 (velocity) and 1e-7 (density) of the full-rank run."""
