@@ -33,7 +33,8 @@ configurations and stores what it produced:
                         frame that the last error compares against;
   ref_products_mixed_10x12x8.npz  the projected operators that the reference's
                         constructor (buildOutOfCoreMatrices) builds from the
-                        same bases under mixed walls.
+                        same bases under mixed walls, and the fields and reduced
+                        coordinates after 12 reduced steps under those walls.
 
 Needs the reference tree (PLUME_REFERENCE_DIR, default /root/reference) and
 writes nothing outside tests/golden/.
@@ -198,12 +199,16 @@ def reduced_fixtures():
     red = base + "/red_mixed/"
     shutil.copytree(red0, red)
     shutil.copy(base + "/red_exact_10x12x8/cubature", red + "cubature")
+    out = base + "/out_mixed"
     subprocess.run([RED_REF, "res=%d,%d,%d" % res, "bc=" + ",".join(str(b) for b in MIXED_BC),
-                    "vorticity=1.0", "reduced=" + red, "truth=" + snap, "steps=0", "out=" + base + "/out_mixed"],
+                    "vorticity=1.0", "reduced=" + red, "truth=" + snap, "steps=%d" % steps, "out=" + out],
                    check=True, capture_output=True)
-    rec = {"res": np.array(res), "bc": np.array(MIXED_BC)}
+    rec = {"res": np.array(res), "bc": np.array(MIXED_BC), "steps": steps, "vorticity_eps": 1.0}
     for fn in PRODUCT_FILES:
         rec["file_" + fn] = np.fromfile(red + fn, dtype=np.uint8)
+    # the reduced steps under these walls (the bases are the default-wall run's)
+    for k in ("velocity", "density", "heat", "qdot"):
+        rec[k] = np.fromfile(out + "." + k + ".f64")
     np.savez_compressed(os.path.join(HERE, "ref_products_mixed_10x12x8.npz"), **rec)
     shutil.rmtree(base)
 

@@ -99,6 +99,29 @@ def test_oracle_restatement_matches_the_reference(tmp_path, case):
     assert rel_l2(q, z["qdot"]) < 1e-12
 
 
+def test_oracle_restatement_matches_the_reference_under_mixed_walls(tmp_path):
+    """The same under mixed walls (front, back, left, right, top, bottom =
+    0 1 1 0 1 0): the reference's constructor built the operators for those
+    walls, and its prestep takes the other face branches."""
+    from cfs_plume_gb300 import _abi
+    from oracle import reduced_oracle
+    z = _fixture("exact_10x12x8")
+    m = np.load(os.path.join(GOLDEN, "ref_products_mixed_10x12x8.npz"))
+    d = str(tmp_path / "red") + "/"
+    os.makedirs(d)
+    for fn in ("U.preadvect.matrix", "U.final.matrix", "U.prediffuse.matrix", "cubature"):
+        z["file_" + fn].tofile(d + fn)
+    for fn in ("damping.peeled.matrix", "projected.ptof.matrix", "inverseProduct.matrix"):
+        m["file_" + fn].tofile(d + fn)
+    p = _abi.default_params(res=tuple(int(v) for v in m["res"]), bc=tuple(int(b) for b in m["bc"]),
+                            vorticity_eps=float(m["vorticity_eps"]))
+    o, q = reduced_oracle.run(p, d, int(m["steps"]))
+    assert np.array_equal(o.field("density"), m["density"])
+    assert np.array_equal(o.field("heat"), m["heat"])
+    assert rel_l2(o.field("velocity"), m["velocity"]) < 1e-12
+    assert rel_l2(q, m["qdot"]) < 1e-12
+
+
 def test_exact_cubature_tracks_the_full_rank_run():
     """With every cell as a cubature point the reference's reduced run stays
     within 1e-4 (velocity) and 1e-7 (density) of the full-rank run."""
