@@ -32,7 +32,7 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
-bool is_vector(int field) {
+[[maybe_unused]] bool is_vector(int field) {
   switch (field) {
     case PLUME_F_VELOCITY:
     case PLUME_F_VELOCITY_OLD:
