@@ -230,7 +230,8 @@ def measure_arm(g, a, dist, nbox, box_values_seed):
     e2e_s = dist.max(time.perf_counter() - t0)
     dist.barrier()
     iters = [s.iterations for s in stats]
-    return {"ms": ms_max, "value": dist.sum(a.steps) / (ms_max / 1000.0), "iters": iters,
+    stages = {k: statistics.mean(getattr(s, "ms_" + k) for s in stats) for k in _abi.STAGES}
+    return {"ms": ms_max, "value": dist.sum(a.steps) / (ms_max / 1000.0), "iters": iters, "stages": stages,
             "launches": sum(s.launches for s in stats), "ms_solve": sum(s.ms_solve for s in stats),
             "fallbacks": sum(s.fallback for s in stats),
             "max_rel_residual": max(s.rel_residual for s in stats),
@@ -519,9 +520,16 @@ def main():
                          (37 * S * N / 1e6),
                    "parallelism": "replicas" if world > 1 else "single"},
         "pcg_iters_per_step": mean_iters,
+        # the metric's comparison: learned solver over plain MIC-PCG at the
+        # same stop test, steps/s and PCG iterations per step
+        "learned_over_plain": (lrn["value"] / plain["value"]) if lrn else None,
+        "learned_iters_over_plain": (statistics.mean(lrn["iters"]) / statistics.mean(plain["iters"]))
+                                    if lrn else None,
+        "target_learned_over_plain": 3.0,
         "arms": {name: {"value": r["value"], "unit": "steps/s", "ms_per_step": r["ms"] / a.steps,
                         "pcg_iters_per_step": statistics.mean(r["iters"]), "fallbacks": r["fallbacks"],
-                        "max_rel_residual": r["max_rel_residual"], "e2e": r["e2e"]}
+                        "max_rel_residual": r["max_rel_residual"], "e2e": r["e2e"],
+                        "ms_stages": r["stages"]}
                  for name, r in (("plain", plain), ("previous", prev), ("learned", lrn)) if r is not None},
         "achieved_gbs_step": step_bytes / (ms_max / a.steps / 1000.0) / 1e9,
         "gpu_launches": launches,

@@ -7,7 +7,7 @@ struct layout.  The numeric defaults are the reference's
 import ctypes as C
 import struct
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 OK, ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_TIMEOUT, ERR_IO, ERR_NOT_CONVERGED, ERR_UNSUPPORTED, ERR_STATE = range(9)
 
@@ -72,7 +72,18 @@ class PlumeStepStats(C.Structure):
         ("rhs_norm", C.c_double),
         ("ms_total", C.c_double),
         ("ms_solve", C.c_double),
+        ("ms_forces", C.c_double),
+        ("ms_vorticity", C.c_double),
+        ("ms_advection", C.c_double),
+        ("ms_damping", C.c_double),
+        ("ms_divergence", C.c_double),
+        ("ms_guess", C.c_double),
+        ("ms_gradient", C.c_double),
     ]
+
+
+# the per-stage device times of plume_step_stats, in step order
+STAGES = ("forces", "vorticity", "advection", "damping", "divergence", "guess", "solve", "gradient")
 
 
 def default_params(**kw):

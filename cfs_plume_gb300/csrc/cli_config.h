@@ -71,10 +71,26 @@ class Config {
   std::map<std::string, std::string> vals_;
 };
 
+// Algorithmic bytes per interior cell of each stage of the step, for field
+// scalars of S bytes (the canonical model: every pass reads its operands and
+// writes its results once; stencil neighbours come from cache; the wall
+// flags are one byte): forces 4S (k_forces: T and u_y in, u_y out, walls),
+// vorticity 18S+2 (curl pass 7S+1, confinement and axpy 11S+1), advection
+// 10S, damping 6S, divergence 5S+1, gradient 7S, and the solve
+// (5S+2S+2) + iterations (16S+2S+3) with the MIC diagonal stored in S bytes.
+struct StageBytes {
+  double forces, vorticity, advection, damping, divergence, gradient, solve0, solve_iter;
+  explicit StageBytes(int S)
+      : forces(4.0 * S), vorticity(18.0 * S + 2), advection(10.0 * S), damping(6.0 * S),
+        divergence(5.0 * S + 1), gradient(7.0 * S), solve0(7.0 * S + 2), solve_iter(18.0 * S + 3) {}
+};
+
 // One JSON object per step for the `log file` cfg key: the step index and
-// every plume_step_stats field (non-finite numbers as null).
+// every plume_step_stats field (non-finite numbers as null).  With the
+// interior cell count n_int and the field scalar size S (4 or 8 bytes), a
+// "gbs" object adds each stage's algorithmic GB/s (StageBytes / its ms).
 template <typename Stats>
-std::string step_json(int step, const Stats& st) {
+std::string step_json(int step, const Stats& st, double n_int = 0.0, int S = 0) {
   auto num = [](double v) {
     if (!std::isfinite(v)) return std::string("null");
     char b[40];
@@ -90,7 +106,28 @@ std::string step_json(int step, const Stats& st) {
   s += ", \"rel_residual\": " + num(st.rel_residual);
   s += ", \"rhs_norm\": " + num(st.rhs_norm);
   s += ", \"ms_total\": " + num(st.ms_total);
-  s += ", \"ms_solve\": " + num(st.ms_solve) + "}";
+  s += ", \"ms_solve\": " + num(st.ms_solve);
+  s += ", \"ms_forces\": " + num(st.ms_forces);
+  s += ", \"ms_vorticity\": " + num(st.ms_vorticity);
+  s += ", \"ms_advection\": " + num(st.ms_advection);
+  s += ", \"ms_damping\": " + num(st.ms_damping);
+  s += ", \"ms_divergence\": " + num(st.ms_divergence);
+  s += ", \"ms_guess\": " + num(st.ms_guess);
+  s += ", \"ms_gradient\": " + num(st.ms_gradient);
+  if (n_int > 0 && S > 0) {
+    const StageBytes b(S);
+    auto gbs = [&](double per_cell, double ms) {
+      return ms > 0 ? num(per_cell * n_int / (ms * 1e6)) : std::string("null");
+    };
+    s += ", \"gbs\": {\"forces\": " + gbs(b.forces, st.ms_forces);
+    s += ", \"vorticity\": " + gbs(b.vorticity, st.ms_vorticity);
+    s += ", \"advection\": " + gbs(b.advection, st.ms_advection);
+    s += ", \"damping\": " + gbs(b.damping, st.ms_damping);
+    s += ", \"divergence\": " + gbs(b.divergence, st.ms_divergence);
+    s += ", \"solve\": " + gbs(b.solve0 + st.iterations * b.solve_iter, st.ms_solve);
+    s += ", \"gradient\": " + gbs(b.gradient, st.ms_gradient) + "}";
+  }
+  s += "}";
   return s;
 }
 

@@ -99,7 +99,8 @@ __device__ inline A block_max(A v, A* sh, A ident) {
 // Block sum of per-thread T values with the warp-level tree in T and the
 // warps' sums in double (result valid in thread 0).  For T = double it is
 // block_sum; for float it keeps the shuffle tree off the FP64 pipe, which
-// issues at 1/64 of the FP32 rate on this part.
+// issues at 1/64 of the FP32 rate on this part.  (The CG dot products use
+// DotAcc below instead.)
 template <typename T>
 __device__ inline double block_sum_w(T v, double* sh) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -114,6 +115,65 @@ __device__ inline double block_sum_w(T v, double* sh) {
   }
   return r;
 }
+// Compensated FP32 dot-product accumulation: algorithm Dot2 of Ogita, Rump and
+// Oishi ("Accurate sum and dot product", SIAM J. Sci. Comput. 26(6), 2005).
+// Each product a*b is split exactly into p + e by one FMA (TwoProduct) and p
+// is added with Knuth's TwoSum, so the pair (s, c) holds the sum as if it had
+// been accumulated in twice the working precision (about 48 significand
+// bits), at a few FP32 operations per element instead of an FP64 operation.
+// The _rn intrinsics keep the compiler from contracting or reassociating.
+__device__ inline void ff_add(float& s, float& c, float p) {
+  const float t = __fadd_rn(s, p);
+  const float z = __fsub_rn(t, s);
+  c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z)));
+  s = t;
+}
+__device__ inline void ff_prod(float& s, float& c, float a, float b) {
+  const float p = __fmul_rn(a, b);
+  const float e = __fmaf_rn(a, b, -p);
+  ff_add(s, c, p);
+  c = __fadd_rn(c, e);
+}
+
+// Per-thread dot-product accumulator of the CG reductions.  FP64 fields
+// accumulate in FP64 in the plain order (bit-for-bit the serial expression
+// r += a*b); FP32 fields use the compensated pair above, so the FP32 engine's
+// dot products carry FP64-class precision.  block() sums over the block
+// (result valid in thread 0); the float pairs stay pairs through the warp
+// tree and become doubles per warp.
+template <typename T>
+struct DotAcc;
+template <>
+struct DotAcc<double> {
+  double s = 0.0;
+  __device__ void prod(double a, double b) { s += a * b; }
+  __device__ double block(double* sh) { return block_sum_w(s, sh); }
+};
+template <>
+struct DotAcc<float> {
+  float s = 0.f, c = 0.f;
+  __device__ void prod(float a, float b) { ff_prod(s, c, a, b); }
+  __device__ double block(double* sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float s2 = __shfl_down_sync(0xffffffffu, s, o);
+      const float c2 = __shfl_down_sync(0xffffffffu, c, o);
+      ff_add(s, c, s2);
+      c = __fadd_rn(c, c2);
+    }
+    __syncthreads();
+    if (lane == 0) sh[wid] = (double)s + (double)c;
+    __syncthreads();
+    double r = 0;
+    if (wid == 0) {
+      r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+      r = warp_sum(r);
+    }
+    return r;
+  }
+};
+
 template <typename T>
 __device__ inline double block_max_w(T v, double* sh, double ident) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;

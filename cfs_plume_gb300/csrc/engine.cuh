@@ -7,6 +7,7 @@
 // pointer rotation instead of separate full-array copies.
 #pragma once
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -14,6 +15,8 @@
 #include <string>
 #include <type_traits>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "common.cuh"
 #include "engine.h"
@@ -35,6 +38,17 @@ namespace plume {
     ++launches_;          \
     PL_TRY(cudaGetLastError()); \
   } while (0)
+
+// NVTX range around the host code that enqueues one stage of the step, named
+// after the reference's TIMER bucket for it (src/util/TIMER.cpp:33-149 keys
+// its buckets by function name, FLUID_3D_MIC.cpp:316-1253); a profiler maps
+// the kernels launched inside onto the range.  No cost without a tool.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 inline int grid_for(long long n, int threads = 256, int cap = 152 * 32) {
   long long b = (n + threads - 1) / threads;
@@ -80,15 +94,31 @@ __global__ void k_planes_to_host(const T* a, const T* b, const T* c, int ncomp, 
   }
 }
 
+// Runs `set` (a kernel's cudaFuncSetAttribute calls) once per device: the
+// attributes belong to the current device, so a flag per process would leave
+// a second GPU without them.  `done` holds one bit per device ordinal below
+// 64 (higher ordinals set the attributes on every launch); threads that race
+// on a device's first launch may both set them, which is harmless.
+template <typename F>
+inline cudaError_t once_per_device(std::atomic<unsigned long long>& done, F&& set) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = set();
+  if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
+
 template <typename T, int C, bool EXACT>
 cudaError_t launch_wave_c(const WaveArgs<T>& a, int grid, size_t smem, cudaStream_t s) {
   void (*kf)(WaveArgs<T>) = a.backward ? k_mic_wave<T, C, EXACT, true> : k_mic_wave<T, C, EXACT, false>;
-  static bool attr_set[2] = {false, false};
-  if (!attr_set[a.backward]) {
-    cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e != cudaSuccess) return e;
-    attr_set[a.backward] = true;
-  }
+  static std::atomic<unsigned long long> attr_done[2];
+  cudaError_t ea = once_per_device(attr_done[a.backward ? 1 : 0], [&] {
+    return cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  });
+  if (ea != cudaSuccess) return ea;
   // launched as explicit one-CTA clusters: the ring hand-off uses
   // shared::cluster forms (st.async, cluster-scope barrier waits)
   cudaLaunchConfig_t cfg = {};
@@ -111,14 +141,13 @@ cudaError_t launch_wave_cl_c(const WaveArgs<T>& a, size_t smem, cudaStream_t s, 
                              int* max_clusters) {
   void (*kf)(WaveArgs<T>) =
       a.backward ? k_mic_wave_cl<T, C, EXACT, true> : k_mic_wave_cl<T, C, EXACT, false>;
-  static bool attr_set[2] = {false, false};
-  if (!attr_set[a.backward]) {
+  static std::atomic<unsigned long long> attr_done[2];
+  cudaError_t ea = once_per_device(attr_done[a.backward ? 1 : 0], [&] {
     cudaError_t e = cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(kf, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e != cudaSuccess) return e;
-    attr_set[a.backward] = true;
-  }
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kf, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    return e;
+  });
+  if (ea != cudaSuccess) return ea;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(a.nslabs, 1, 1);
   cfg.blockDim = dim3(32 * a.BZ, 1, 1);
@@ -220,6 +249,7 @@ class EngineT : public Engine {
     }
     PL_TRY(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
     for (auto* e : {&ev_[0], &ev_[1], &ev_[2], &ev_[3]}) PL_TRY(cudaEventCreate(e));
+    for (auto& e : evs_) PL_TRY(cudaEventCreate(&e));
 
     // one pool: 13 scalar planes + 8 vector fields (24 planes) of T, the FP64
     // MIC diagonal, the obstacle bytes, solver state and reduction partials.
@@ -463,32 +493,48 @@ class EngineT : public Engine {
     const int nfaces = 2 * (g_.Y * g_.Z + g_.X * g_.Z + g_.X * g_.Y);
     const int gF = grid_for(nfaces);
     launches_ = 0;
+    NvtxRange step_range(box ? "stepWithMovingObstacle" : "step");
     PL_TRY(cudaEventRecord(ev_[0], s_));
     // forces: walls, buoyancy, prevorticity (FLUID_3D_MIC.cpp:188-199)
     StepConsts<T> cf = c_;
     if (box) cf.has_beta = 0;  // the moving step adds no buoyancy (lines 247-254)
-    k_forces<T><<<gN, 256, 0, s_>>>(g_, vel_, dens_, heat_, prevort_, cf, cache);
-    PL_CHECK_LAUNCH();
+    {
+      NvtxRange r("addBuoyancy");
+      k_forces<T><<<gN, 256, 0, s_>>>(g_, vel_, dens_, heat_, prevort_, cf, cache);
+      PL_CHECK_LAUNCH();
+    }
+    PL_TRY(cudaEventRecord(evs_[0], s_));
     if (c_.has_vort) {  // addVorticity returns early when eps <= 0 (line 527)
+      NvtxRange r("addVorticity");
       k_vort1<T><<<gN, 256, 0, s_>>>(g_, vel_, vort_, mag_, c_);
       PL_CHECK_LAUNCH();
       k_vort2<T><<<gN, 256, 0, s_>>>(g_, vel_, vort_, mag_, force_, c_, cache);
       PL_CHECK_LAUNCH();
     }
+    PL_TRY(cudaEventRecord(evs_[1], s_));
     // advectStam (lines 595-650): boundary copy, swap, advect + fix-up
     const int ox = p_.bc[2] == 0, oy = p_.bc[4] == 0, oz = p_.bc[0] == 0;
-    k_face_bc<T><<<gF, 256, 0, s_>>>(g_, vel_, ox ? 1 : 0, oy ? 1 : 0, oz ? 1 : 0);
-    PL_CHECK_LAUNCH();
-    std::swap(vel_, vel_old_);
-    std::swap(dens_, dens_old_);
-    std::swap(heat_, heat_old_);
-    k_advect<T><<<gN, 256, 0, s_>>>(g_, c_, vel_old_, dens_old_, heat_old_, vel_, dens_, heat_,
-                                    postadv_, cache, ox, oy, oz);
-    PL_CHECK_LAUNCH();
+    {
+      NvtxRange r("advectStam");
+      k_face_bc<T><<<gF, 256, 0, s_>>>(g_, vel_, ox ? 1 : 0, oy ? 1 : 0, oz ? 1 : 0);
+      PL_CHECK_LAUNCH();
+      std::swap(vel_, vel_old_);
+      std::swap(dens_, dens_old_);
+      std::swap(heat_, heat_old_);
+      k_advect<T><<<gN, 256, 0, s_>>>(g_, c_, vel_old_, dens_old_, heat_old_, vel_, dens_, heat_,
+                                      postadv_, cache, ox, oy, oz);
+      PL_CHECK_LAUNCH();
+    }
+    PL_TRY(cudaEventRecord(evs_[2], s_));
     // damping (lines 209-212); the input buffer becomes `prediffusion`
-    k_damping<T><<<gN, 256, 0, s_>>>(g_, c_, vel_, spare_, preproj_, cache);
-    PL_CHECK_LAUNCH();
+    {
+      NvtxRange r("buildPeeledDampingMatrixFull");
+      k_damping<T><<<gN, 256, 0, s_>>>(g_, c_, vel_, spare_, preproj_, cache);
+      PL_CHECK_LAUNCH();
+    }
     std::swap(vel_, spare_);
+    PL_TRY(cudaEventRecord(evs_[3], s_));
+    NvtxRange project_range("project");
     if (box) {
       // the IOP stomp u <- N [u; 1], cached as postIOP (lines 276-284)
       if (prof_on_) PL_TRY(cudaEventRecord(stomp_ev_[0], s_));
@@ -513,9 +559,10 @@ class EngineT : public Engine {
       k_copy_border_all<T><<<gF, 256, 0, s_>>>(g_, pres_);
       PL_CHECK_LAUNCH();
     }
-    PL_TRY(cudaEventRecord(ev_[1], s_));
+    PL_TRY(cudaEventRecord(evs_[4], s_));
     last_fallback_ = 0;
     if (learned) {
+      NvtxRange r("learned initial guess");
       // x0 = p_prev + g c with c = net(r0), r0 = b - A p_prev: the network
       // (an approximate inverse of A) applied to the previous pressure's
       // residual, scaled by the 1-D A-norm Galerkin factor g = c.r0 / c.A c;
@@ -540,13 +587,18 @@ class EngineT : public Engine {
       k_guess_apply<T><<<gI, 256, 0, s_>>>(g_, corr ? pres_ : nullptr, z_, z_, st_, pres_);
       PL_CHECK_LAUNCH();
     }
+    PL_TRY(cudaEventRecord(ev_[1], s_));
+    NvtxRange solve_range("solvePoisson");
     // a learned-start solve gets at most twice the previous step's
     // iterations: a guess that does not pay off falls back early
     int cap = p_.max_iters;
     if (learned && last_iters_ > 0) cap = std::min(p_.max_iters, std::max(20, 2 * last_iters_));
     int rc = solve_device(div_, pres_, cap, !learned && keep_p == 0);
     if (rc != PLUME_OK) return rc;
-    if (learned && !st_host_->converged) {
+    // a convolution whose bounded wait expired left the guess invalid (the
+    // solve above has synchronised the stream): treat it as a rejected guess
+    const bool net_failed = learned && net_->take_error(err_) != PLUME_OK;
+    if (learned && (!st_host_->converged || net_failed)) {
       // the guess did not lead to convergence: plain MIC-PCG from p = 0
       last_fallback_ = 1;
       PL_TRY(cudaMemsetAsync(pres_, 0, (size_t)g_.N * sizeof(T), s_));
@@ -558,6 +610,7 @@ class EngineT : public Engine {
     k_gradient<T><<<gI, 256, 0, s_>>>(g_, c_, vel_, pres_);
     PL_CHECK_LAUNCH();
     PL_TRY(cudaEventRecord(ev_[3], s_));
+    stages_valid_ = true;
     total_time_ += 0.1;  // FLUID_3D_MIC.cpp:221 (goalTime)
     total_steps_ += 1;
     if (box && prof_on_) {
@@ -663,6 +716,7 @@ class EngineT : public Engine {
     int rc = put_plane(div_, b, 1, 0);
     if (rc == PLUME_OK) rc = put_plane(pres_, x, 1, 0);
     if (rc != PLUME_OK) return rc;
+    stages_valid_ = false;
     PL_TRY(cudaEventRecord(ev_[1], s_));
     rc = solve_device(div_, pres_);
     if (rc != PLUME_OK) return rc;
@@ -895,7 +949,20 @@ class EngineT : public Engine {
     a.ctl = wave_ctl_;
     a.progress = wave_prog_;
     a.st = st_;
+    a.gate = gate_closed_ ? (const int*)(wave_ctl_ + 3) : nullptr;  // ctl[3]: never written
+    a.gate_spins = gate_spins_;
     return a;
+  }
+
+  int set_wait_gate(int closed, long long polls) override {
+    if (closed && polls <= 0) return fail(PLUME_ERR_INVALID, "the gate's poll limit must be positive");
+    PL_TRY(cudaStreamSynchronize(s_));
+    gate_closed_ = closed != 0;
+    gate_spins_ = closed ? polls : 0;
+    // the CG-loop graph holds the sweeps' arguments by value: build it anew
+    if (cg_exec_) cudaGraphExecDestroy(cg_exec_);
+    cg_exec_ = nullptr;
+    return PLUME_OK;
   }
 
   // MIC forward then backward sweep on skewed vectors (wavefront kernels).
@@ -1130,6 +1197,16 @@ class EngineT : public Engine {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, ev_[0], ev_[3]) == cudaSuccess) st->ms_total = ms;
     if (cudaEventElapsedTime(&ms, ev_[1], ev_[2]) == cudaSuccess) st->ms_solve = ms;
+    if (stages_valid_) {
+      // stage boundaries in step order: start, forces, vorticity, advection,
+      // damping, divergence (guess start), guess (solve start), ..., end
+      const cudaEvent_t b[8] = {ev_[0], evs_[0], evs_[1], evs_[2], evs_[3], evs_[4], ev_[1], ev_[2]};
+      double* out[6] = {&st->ms_forces, &st->ms_vorticity, &st->ms_advection, &st->ms_damping,
+                        &st->ms_divergence, &st->ms_guess};
+      for (int k = 0; k < 6; k++)
+        if (cudaEventElapsedTime(&ms, b[k], b[k + 1]) == cudaSuccess) *out[k] = ms;
+      if (cudaEventElapsedTime(&ms, ev_[2], ev_[3]) == cudaSuccess) st->ms_gradient = ms;
+    }
     (void)cudaGetLastError();
     return PLUME_OK;
   }
@@ -1288,6 +1365,8 @@ class EngineT : public Engine {
     if (stage_) cudaFreeHost(stage_);
     for (auto e : ev_)
       if (e) cudaEventDestroy(e);
+    for (auto e : evs_)
+      if (e) cudaEventDestroy(e);
     for (auto& buf : prof_ev_)
       for (auto e : buf)
         if (e) cudaEventDestroy(e);
@@ -1306,6 +1385,10 @@ class EngineT : public Engine {
   int launches_ = 0;
   cudaStream_t s_ = nullptr;
   cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+  // stage boundaries inside a step: after forces, vorticity, advection,
+  // damping and the divergence (plume_step_stats' per-stage times)
+  cudaEvent_t evs_[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  bool stages_valid_ = false;
   char* pool_ = nullptr;
   T *dens_ = nullptr, *dens_old_ = nullptr, *heat_ = nullptr, *heat_old_ = nullptr;
   T *pres_ = nullptr, *div_ = nullptr, *mag_ = nullptr;
@@ -1324,8 +1407,10 @@ class EngineT : public Engine {
   char* spool_ = nullptr;
   T *sr_ = nullptr, *sd_ = nullptr, *sq_ = nullptr, *sz_ = nullptr, *sqf_ = nullptr, *sx_ = nullptr,
     *sb_ = nullptr, *sP_ = nullptr, *sd2_ = nullptr;
-  unsigned* wave_ctl_ = nullptr;
+  unsigned* wave_ctl_ = nullptr;  // [0] slab ticket, [1] exited CTAs, [3] the test gate (0)
   int* wave_prog_ = nullptr;
+  bool gate_closed_ = false;  // plume_set_wait_gate
+  long long gate_spins_ = 0;
   int bz_ = 8, wave_k_ = 8, nslabs_ = 1, wave_grid_ = 1, num_sms_ = 1;
   bool use_cluster_ = false;
   size_t wave_smem_ = 0;

@@ -55,6 +55,8 @@ class Engine {
   // and starts recording, 0 stops; sweep_times returns the summed device ms
   // and the number of timed launches.
   virtual int profile_sweeps(int on) = 0;
+  // Test hook of the sweeps' bounded waits (plume_set_wait_gate).
+  virtual int set_wait_gate(int closed, long long polls) = 0;
   virtual int sweep_times(double* ms, int64_t* launches) = 0;
   // Device pointer of a scalar field (field type: float or double as the
   // engine's precision), the engine's cudaStream_t, and the network used by

@@ -169,7 +169,9 @@ int main(int argc, char* argv[]) {
               << " relative two norm: " << st.rel_residual << "  (" << st.ms_total << " ms)"
               << std::endl;
     if (log) {
-      std::fprintf(log, "%s\n", plume_cli::step_json(step, st).c_str());
+      const double n_int = (double)(p.res[0] - 2) * (p.res[1] - 2) * (p.res[2] - 2);
+      const int S = p.precision == PLUME_PREC_FP32 ? 4 : 8;
+      std::fprintf(log, "%s\n", plume_cli::step_json(step, st, n_int, S).c_str());
       std::fflush(log);
     }
     // writeGz + appendStreams (fluid3D.cpp:376-386) on the handle's writer

@@ -10,6 +10,7 @@
 //
 // Built without multiply-add contraction (like the FP64 engine), so the result
 // is bit-identical to plume_mic_apply on an FP64 handle.
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -82,6 +83,18 @@ extern "C" int plume_mic_apply_noalloc(const int32_t res[3], const int32_t bc[6]
     if (res[k] < 4) return PLUME_ERR_INVALID;
   for (int k = 0; k < 6; k++)
     if (bc[k] != 0 && bc[k] != 1) return PLUME_ERR_INVALID;
+  {
+    // the fixed scratch bounds the grid: reject rather than overrun it (sizes
+    // in 64 bits, before any of the int geometry below is formed)
+    const long long nx = (long long)res[0] - 2, ny = (long long)res[1] - 2, nz = (long long)res[2] - 2;
+    const long long C = (nx + 31) / 32;
+    if (C > 8) return PLUME_ERR_INVALID;  // x resolution above 258 cells
+    if (nz > PLUME_NOALLOC_MAX_PLANES) return PLUME_ERR_INVALID;
+    const long long row = 32 * C, rows = ny + 31;
+    if (rows > (long long)PLUME_NOALLOC_MAX_ELEMS / row ||
+        nz * rows * row > (long long)PLUME_NOALLOC_MAX_ELEMS)
+      return PLUME_ERR_INVALID;
+  }
   Grid g;
   g.X = res[0];
   g.Y = res[1];
@@ -98,14 +111,10 @@ extern "C" int plume_mic_apply_noalloc(const int32_t res[3], const int32_t bc[6]
   k.ny = g.ny;
   k.nz = g.nz;
   k.C = (g.nx + 31) / 32;
-  if (k.C > 8) return PLUME_ERR_INVALID;  // x resolution above 258 cells
   k.W = 32 * k.C;
   k.R = g.ny + 31;
   k.plane = (long long)k.R * k.W;
   k.total = (long long)g.nz * k.plane;
-  // the fixed scratch bounds the grid: reject rather than overrun it
-  if (k.total > (long long)PLUME_NOALLOC_MAX_ELEMS || g.nz > PLUME_NOALLOC_MAX_PLANES)
-    return PLUME_ERR_INVALID;
 
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -139,6 +148,17 @@ extern "C" int plume_mic_apply_noalloc(const int32_t res[3], const int32_t bc[6]
   a.ctl = ctl;
   a.progress = progress;
   a.st = st;
+  // Test hook of the sweeps' bounded waits: PLUME_NOALLOC_WAIT_GATE=<polls>
+  // makes each sweep CTA first poll ctl[3] (cleared above, never set) that
+  // many times before it issues any copy; the wait expires and z comes back
+  // NaN.  Unset in normal use.
+  if (const char* gate = getenv("PLUME_NOALLOC_WAIT_GATE")) {
+    const long long polls = atoll(gate);
+    if (polls > 0) {
+      a.gate = (const int*)(ctl + 3);
+      a.gate_spins = polls;
+    }
+  }
   bool cluster = false;
   int bz = (g.nz + 15) / 16;
   if (bz < 4) bz = 4;

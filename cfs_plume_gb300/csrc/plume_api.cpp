@@ -13,6 +13,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_runtime_api.h>
+
 #include "../../include/plume.h"
 #include "../../include/plume_box.h"
 #include "../../include/plume_solver.h"
@@ -124,6 +126,14 @@ int from_engine(plume_handle* h, int code) {
   if (code != PLUME_OK) h->err = h->eng->last_error();
   return code;
 }
+// A handle's engine with the handle's device made current: every call on a
+// handle runs on its own GPU, so one thread may drive handles on several
+// GPUs (cudaSetDevice returns at once when the device is already current;
+// if it fails, the engine's next CUDA call reports the error).
+plume::Engine* eng(plume_handle* h) {
+  if (cudaSetDevice(h->eng->params().device) != cudaSuccess) (void)cudaGetLastError();
+  return h->eng;
+}
 }  // namespace
 
 extern "C" {
@@ -185,53 +195,54 @@ int plume_create(const plume_params* p, plume_handle** out) {
 void plume_destroy(plume_handle* h) {
   if (!h) return;
   h->writer.reset();  // waits for pending snapshots
+  (void)eng(h);       // frees on the handle's device
   delete h->eng;
   delete h;
 }
 
 int plume_add_source(plume_handle* h, int32_t step_index) {
   if (!h) return PLUME_ERR_INVALID;
-  return from_engine(h, h->eng->add_source(step_index));
+  return from_engine(h, eng(h)->add_source(step_index));
 }
 
 int plume_add_source_values(plume_handle* h, const double* values, size_t n) {
   if (!h) return PLUME_ERR_INVALID;
-  return from_engine(h, h->eng->add_source_values(values, n));
+  return from_engine(h, eng(h)->add_source_values(values, n));
 }
 
 int plume_run_timed(plume_handle* h, int32_t first_step_index, int32_t n, double* ms_device,
                     plume_step_stats* stats) {
   if (!h || !ms_device) return PLUME_ERR_INVALID;
   if (n < 0) return set_err(h, PLUME_ERR_INVALID, "negative step count");
-  return from_engine(h, h->eng->run_timed(first_step_index, n, ms_device, stats));
+  return from_engine(h, eng(h)->run_timed(first_step_index, n, ms_device, stats));
 }
 
 int plume_step(plume_handle* h, plume_step_stats* stats) {
   if (!h) return PLUME_ERR_INVALID;
-  return from_engine(h, h->eng->step(stats));
+  return from_engine(h, eng(h)->step(stats));
 }
 
 int plume_run(plume_handle* h, int32_t first_step_index, int32_t n, plume_step_stats* stats) {
   if (!h) return PLUME_ERR_INVALID;
   if (n < 0) return set_err(h, PLUME_ERR_INVALID, "negative step count");
-  return from_engine(h, h->eng->run(first_step_index, n, stats));
+  return from_engine(h, eng(h)->run(first_step_index, n, stats));
 }
 
 int plume_download(plume_handle* h, int32_t field, double* dst, size_t n) {
   if (!h) return PLUME_ERR_INVALID;
   if (field < 0 || field >= PLUME_F_COUNT) return set_err(h, PLUME_ERR_INVALID, "unknown field");
-  return from_engine(h, h->eng->download(field, dst, n));
+  return from_engine(h, eng(h)->download(field, dst, n));
 }
 
 int plume_upload(plume_handle* h, int32_t field, const double* src, size_t n) {
   if (!h) return PLUME_ERR_INVALID;
   if (field < 0 || field >= PLUME_F_COUNT) return set_err(h, PLUME_ERR_INVALID, "unknown field");
-  return from_engine(h, h->eng->upload(field, src, n));
+  return from_engine(h, eng(h)->upload(field, src, n));
 }
 
 int plume_download_obstacles(plume_handle* h, uint8_t* dst, size_t n) {
   if (!h) return PLUME_ERR_INVALID;
-  return from_engine(h, h->eng->download_obstacles(dst, n));
+  return from_engine(h, eng(h)->download_obstacles(dst, n));
 }
 
 int plume_read_state(plume_handle* h, const char* path) {
@@ -241,13 +252,13 @@ int plume_read_state(plume_handle* h, const char* path) {
   double consts[7];
   int rc = plume_state_read_header(path, ints, consts);
   if (rc != PLUME_OK) return set_err(h, rc, plume::global_error());
-  const plume_params& p = h->eng->params();
+  const plume_params& p = eng(h)->params();
   if (ints[0] != p.res[0] || ints[1] != p.res[1] || ints[2] != p.res[2])
     return set_err(h, PLUME_ERR_INVALID,
                    std::string("the state file's grid ") + std::to_string(ints[0]) + "x" + std::to_string(ints[1]) +
                        "x" + std::to_string(ints[2]) + " is not the handle's");
   // header doubles: dx, totalTime, dt, buoyancy, vorticityEps (lines 1150-1160)
-  if (consts[0] != h->eng->dx() || consts[2] != p.dt || consts[3] != p.buoyancy || consts[4] != p.vorticity_eps)
+  if (consts[0] != eng(h)->dx() || consts[2] != p.dt || consts[3] != p.buoyancy || consts[4] != p.vorticity_eps)
     return set_err(h, PLUME_ERR_INVALID,
                    "the state file was written with another dx, dt, buoyancy or vorticityEps than the handle's");
   const size_t N = (size_t)p.res[0] * p.res[1] * p.res[2];
@@ -266,22 +277,22 @@ int plume_read_state(plume_handle* h, const char* path) {
   rc = plume::read_state_fields(path, req, nullptr);
   if (rc != PLUME_OK) return set_err(h, rc, plume::global_error());
   for (const plume::StateField& w : req) {
-    rc = from_engine(h, h->eng->upload(w.field, w.dst, w.n));
+    rc = from_engine(h, eng(h)->upload(w.field, w.dst, w.n));
     if (rc != PLUME_OK) return rc;
   }
-  h->eng->set_clock(ints[9], consts[1]);
+  eng(h)->set_clock(ints[9], consts[1]);
   return PLUME_OK;
 }
 
 int plume_get_info(plume_handle* h, int32_t res[3], int32_t* total_steps, double* total_time,
                    double* dx) {
   if (!h) return PLUME_ERR_INVALID;
-  const plume_params& p = h->eng->params();
+  const plume_params& p = eng(h)->params();
   if (res)
     for (int k = 0; k < 3; k++) res[k] = p.res[k];
-  if (total_steps) *total_steps = h->eng->total_steps();
-  if (total_time) *total_time = h->eng->total_time();
-  if (dx) *dx = h->eng->dx();
+  if (total_steps) *total_steps = eng(h)->total_steps();
+  if (total_time) *total_time = eng(h)->total_time();
+  if (dx) *dx = eng(h)->dx();
   return PLUME_OK;
 }
 
@@ -289,17 +300,17 @@ int plume_get_info(plume_handle* h, int32_t res[3], int32_t* total_steps, double
 static int fetch_iop(plume_handle* h, plume::IopRecord& iop) {
   iop.inside.clear();
   iop.values.clear();
-  if (!h->eng->has_iop()) return PLUME_OK;
-  const plume_params& p = h->eng->params();
+  if (!eng(h)->has_iop()) return PLUME_OK;
+  const plume_params& p = eng(h)->params();
   const size_t N = (size_t)p.res[0] * p.res[1] * p.res[2];
   iop.inside.resize(N);
   iop.values.resize(3 * N);
-  return h->eng->download_iop(iop.inside.data(), iop.values.data(), N);
+  return eng(h)->download_iop(iop.inside.data(), iop.values.data(), N);
 }
 
 static plume::FieldFetch make_fetch(plume_handle* h) {
   return [h](int field, std::vector<double>& buf) {
-    const plume_params& p = h->eng->params();
+    const plume_params& p = eng(h)->params();
     const size_t N = (size_t)p.res[0] * p.res[1] * p.res[2];
     const bool vec = field == PLUME_F_VELOCITY || field == PLUME_F_VELOCITY_OLD ||
                      field == PLUME_F_FORCE || field == PLUME_F_VORTICITY ||
@@ -307,30 +318,30 @@ static plume::FieldFetch make_fetch(plume_handle* h) {
                      field == PLUME_F_PREADVECTION || field == PLUME_F_CACHED_QUADRATIC ||
                      field == PLUME_F_POSTADVECTION || field == PLUME_F_PREVORTICITY ||
                      field == PLUME_F_POST_IOP;
-    if (field == PLUME_F_POST_IOP && !h->eng->has_iop()) {
+    if (field == PLUME_F_POST_IOP && !eng(h)->has_iop()) {
       buf.clear();  // never assigned: written as an empty field
       return (int)PLUME_OK;
     }
     buf.resize(vec ? 3 * N : N);
-    return h->eng->download(field, buf.data(), buf.size());
+    return eng(h)->download(field, buf.data(), buf.size());
   };
 }
 
 int plume_write_state(plume_handle* h, const char* path) {
   if (!h) return PLUME_ERR_INVALID;
   if (!path) return set_err(h, PLUME_ERR_INVALID, "null path");
-  const plume_params& p = h->eng->params();
+  const plume_params& p = eng(h)->params();
   if (!p.cache_fields) return set_err(h, PLUME_ERR_STATE, "state file needs cache_fields = 1");
   plume::StateHeader hd;
   for (int k = 0; k < 3; k++) hd.res[k] = p.res[k];
-  hd.total_steps = h->eng->total_steps();
-  hd.dx = h->eng->dx();
-  hd.total_time = h->eng->total_time();
+  hd.total_steps = eng(h)->total_steps();
+  hd.dx = eng(h)->dx();
+  hd.total_time = eng(h)->total_time();
   hd.dt = p.dt;
   hd.buoyancy = p.buoyancy;
   hd.vorticity_eps = p.vorticity_eps;
   std::vector<uint8_t> ob((size_t)p.res[0] * p.res[1] * p.res[2]);
-  int rc = h->eng->download_obstacles(ob.data(), ob.size());
+  int rc = eng(h)->download_obstacles(ob.data(), ob.size());
   if (rc != PLUME_OK) return from_engine(h, rc);
   plume::IopRecord iop;
   rc = fetch_iop(h, iop);
@@ -341,7 +352,7 @@ int plume_write_state(plume_handle* h, const char* path) {
 int plume_append_streams(plume_handle* h, const char* dir) {
   if (!h) return PLUME_ERR_INVALID;
   if (!dir) return set_err(h, PLUME_ERR_INVALID, "null directory");
-  const plume_params& p = h->eng->params();
+  const plume_params& p = eng(h)->params();
   if (!p.cache_fields) return set_err(h, PLUME_ERR_STATE, "streams need cache_fields = 1");
   plume::IopRecord iop;
   const int rc = fetch_iop(h, iop);
@@ -372,22 +383,22 @@ const char* plume_last_error(plume_handle* h) {
 // ---- solver-level entry points (include/plume_solver.h) ----
 int plume_solve_poisson(plume_handle* h, const double* b, double* x, plume_step_stats* stats) {
   if (!h) return PLUME_ERR_INVALID;
-  return from_engine(h, h->eng->solve(b, x, stats));
+  return from_engine(h, eng(h)->solve(b, x, stats));
 }
 
 int plume_mic_apply(plume_handle* h, const double* r, double* z, double* q) {
   if (!h || !r || !z) return PLUME_ERR_INVALID;
-  return from_engine(h, h->eng->mic_apply(r, z, q));
+  return from_engine(h, eng(h)->mic_apply(r, z, q));
 }
 
 int plume_mic_diagonal(plume_handle* h, double* precon) {
   if (!h || !precon) return PLUME_ERR_INVALID;
-  return from_engine(h, h->eng->mic_precon(precon));
+  return from_engine(h, eng(h)->mic_precon(precon));
 }
 
 int plume_sync(plume_handle* h) {
   if (!h) return PLUME_ERR_INVALID;
-  const int rc = from_engine(h, h->eng->sync());
+  const int rc = from_engine(h, eng(h)->sync());
   if (rc != PLUME_OK) return rc;
   return plume_wait_snapshots(h);
 }
@@ -404,7 +415,7 @@ int plume_snapshot_async(plume_handle* h, const char* dir, int32_t step, int32_t
   if (!h) return PLUME_ERR_INVALID;
   if (!dir || step < 0 || (what & 3) == 0 || (what & ~3) != 0)
     return set_err(h, PLUME_ERR_INVALID, "need a directory, step >= 0 and what in 1..3");
-  const plume_params& p = h->eng->params();
+  const plume_params& p = eng(h)->params();
   if (!p.cache_fields) return set_err(h, PLUME_ERR_STATE, "snapshots need cache_fields = 1");
   if (!h->writer) h->writer.reset(new (std::nothrow) SnapshotWriter());
   if (!h->writer) return set_err(h, PLUME_ERR_OOM, "writer thread");
@@ -423,16 +434,16 @@ int plume_snapshot_async(plume_handle* h, const char* dir, int32_t step, int32_t
     if (rc != PLUME_OK) return from_engine(h, rc);
   }
   auto ob = std::make_shared<std::vector<uint8_t>>(N);
-  int rc = h->eng->download_obstacles(ob->data(), ob->size());
+  int rc = eng(h)->download_obstacles(ob->data(), ob->size());
   if (rc != PLUME_OK) return from_engine(h, rc);
   auto iop = std::make_shared<plume::IopRecord>();
   rc = fetch_iop(h, *iop);
   if (rc != PLUME_OK) return from_engine(h, rc);
   plume::StateHeader hd;
   for (int k = 0; k < 3; k++) hd.res[k] = p.res[k];
-  hd.total_steps = h->eng->total_steps();
-  hd.dx = h->eng->dx();
-  hd.total_time = h->eng->total_time();
+  hd.total_steps = eng(h)->total_steps();
+  hd.dx = eng(h)->dx();
+  hd.total_time = eng(h)->total_time();
   hd.dt = p.dt;
   hd.buoyancy = p.buoyancy;
   hd.vorticity_eps = p.vorticity_eps;
@@ -459,40 +470,45 @@ int plume_snapshot_async(plume_handle* h, const char* dir, int32_t step, int32_t
 int plume_step_moving_box(plume_handle* h, const plume_box* box, plume_step_stats* stats) {
   if (!h) return PLUME_ERR_INVALID;
   if (!box) return set_err(h, PLUME_ERR_INVALID, "null box");
-  return from_engine(h, h->eng->step_moving_box(*box, stats));
+  return from_engine(h, eng(h)->step_moving_box(*box, stats));
 }
 
 int plume_set_initial_velocity_box(plume_handle* h, const plume_box* box) {
   if (!h) return PLUME_ERR_INVALID;
   if (!box) return set_err(h, PLUME_ERR_INVALID, "null box");
-  return from_engine(h, h->eng->set_initial_velocity_box(*box));
+  return from_engine(h, eng(h)->set_initial_velocity_box(*box));
 }
 
 int plume_run_moving_timed(plume_handle* h, plume_box* box, int32_t first_step_index, int32_t n,
                            double* ms_device, plume_step_stats* stats) {
   if (!h) return PLUME_ERR_INVALID;
   if (!box || !ms_device || n < 0) return set_err(h, PLUME_ERR_INVALID, "bad argument");
-  return from_engine(h, h->eng->run_moving_timed(*box, first_step_index, n, ms_device, stats));
+  return from_engine(h, eng(h)->run_moving_timed(*box, first_step_index, n, ms_device, stats));
 }
 
 int plume_box_stomp_times(plume_handle* h, double* ms_total, int64_t* launches) {
   if (!h || !ms_total || !launches) return PLUME_ERR_INVALID;
-  return from_engine(h, h->eng->stomp_times(ms_total, launches));
+  return from_engine(h, eng(h)->stomp_times(ms_total, launches));
 }
 
 int plume_download_iop(plume_handle* h, uint8_t* inside, double* values, size_t n) {
   if (!h) return PLUME_ERR_INVALID;
-  return from_engine(h, h->eng->download_iop(inside, values, n));
+  return from_engine(h, eng(h)->download_iop(inside, values, n));
 }
 
 int plume_profile_sweeps(plume_handle* h, int on) {
   if (!h) return PLUME_ERR_INVALID;
-  return from_engine(h, h->eng->profile_sweeps(on));
+  return from_engine(h, eng(h)->profile_sweeps(on));
 }
 
 int plume_sweep_times(plume_handle* h, double* ms_total, int64_t* launches) {
   if (!h || !ms_total || !launches) return PLUME_ERR_INVALID;
-  return from_engine(h, h->eng->sweep_times(ms_total, launches));
+  return from_engine(h, eng(h)->sweep_times(ms_total, launches));
+}
+
+int plume_set_wait_gate(plume_handle* h, int32_t closed, int64_t poll_limit) {
+  if (!h) return PLUME_ERR_INVALID;
+  return from_engine(h, eng(h)->set_wait_gate(closed, (long long)poll_limit));
 }
 
 }  // extern "C"

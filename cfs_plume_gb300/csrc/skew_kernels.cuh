@@ -10,10 +10,11 @@
 
 namespace plume {
 
-// Per-thread partial sums are kept in the field type T (FP32 in FP32 mode:
-// GB300's FP64 rate is a small fraction of its FP32 rate, so one FP64 operation
-// per element would bound these kernels) and are promoted to FP64 for the
-// block and grid reductions, which run in a fixed order.
+// Dot products accumulate per thread in DotAcc<T> (common.cuh): plain FP64 for
+// FP64 fields; for FP32 fields a compensated FP32 pair (Dot2), which carries
+// FP64-class precision at FP32 cost (GB300's FP64 rate is a small fraction of
+// its FP32 rate, so one FP64 operation per element would bound these
+// kernels).  Block and grid reductions run in FP64 in a fixed order.
 // Stored element e -> interior cell (ix, iy, iz); false for padding.
 __device__ inline bool skew_cell(const Skew& k, int e, int& ix, int& iy, int& iz) {
   iz = e / (int)k.plane;
@@ -87,7 +88,7 @@ template <typename T>
 __global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState* st, double* part,
                            double tol, int max_iters, int criterion, int x_zero) {
   __shared__ double sh[32];
-  T bb = T(0);
+  DotAcc<T> bb;
   PL_GRID_STRIDE(e, (int)k.total) {
     int ix, iy, iz;
     T v = T(0);
@@ -103,11 +104,11 @@ __global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState
       } else {
         v = bi - mult_a_skew(g, k, x, e, ix, iy, iz);
       }
-      bb += bi * bi;
+      bb.prod(bi, bi);
     }
     r[e] = v;
   }
-  const double s = block_sum_w(bb, sh);
+  const double s = bb.block(sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (arrive_last(&st->ticket[0])) {
     const double tot = sum_partials(part, sh);
@@ -130,16 +131,16 @@ __global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState
 template <typename T>
 __global__ void k_cgs_init2(Skew k, const T* r, const T* z, T* d, CgState* st, double* part) {
   __shared__ double sh[32];
-  T rz = T(0), rr = T(0);
+  DotAcc<T> rz, rr;
   PL_GRID_STRIDE(e, (int)k.total) {
     const T zi = z[e], ri = r[e];
     if (d) d[e] = zi;
-    rz += ri * zi;
-    rr += ri * ri;
+    rz.prod(ri, zi);
+    rr.prod(ri, ri);
   }
-  const double s1 = block_sum_w(rz, sh);
+  const double s1 = rz.block(sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s1;
-  const double s2 = block_sum_w(rr, sh);
+  const double s2 = rr.block(sh);
   if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
   if (arrive_last(&st->ticket[0])) {
     const double trz = sum_partials(part, sh);
@@ -169,17 +170,17 @@ template <typename T>
 __global__ void k_cgs_spmv(Grid g, Skew k, const T* d, T* q, CgState* st, double* part) {
   if (st->done) return;
   __shared__ double sh[32];
-  T dq = T(0);
+  DotAcc<T> dq;
   PL_GRID_STRIDE(e, (int)k.total) {
     int ix, iy, iz;
     T v = T(0);
     if (skew_cell(k, e, ix, iy, iz)) {
       v = mult_a_skew(g, k, d, e, ix, iy, iz);
-      dq += d[e] * v;
+      dq.prod(d[e], v);
     }
     q[e] = v;
   }
-  const double s = block_sum_w(dq, sh);
+  const double s = dq.block(sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (arrive_last(&st->ticket[0])) {
     const double t = sum_partials(part, sh);
@@ -202,17 +203,18 @@ __global__ void k_cgs_axpy(Skew k, const T* d, const T* q, T* x, T* r, CgState* 
   if (st->done) return;
   __shared__ double sh[32];
   const T alpha = (T)st->alpha;
-  T mx = T(-3.0e38), rr = T(0);
+  T mx = T(-3.0e38);
+  DotAcc<T> rr;
   PL_GRID_STRIDE(e, (int)k.total) {
     x[e] += alpha * d[e];
     const T ri = r[e] + (-alpha) * q[e];
     r[e] = ri;
     mx = (ri > mx) ? ri : mx;
-    rr += ri * ri;
+    rr.prod(ri, ri);
   }
   const double s1 = block_max_w(mx, sh, -1.0e308);
   if (threadIdx.x == 0) part[blockIdx.x] = s1;
-  const double s2 = block_sum_w(rr, sh);
+  const double s2 = rr.block(sh);
   if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
   if (arrive_last(&st->ticket[0])) {
     const double tm = max_partials(part, sh);
@@ -236,9 +238,9 @@ template <typename T>
 __global__ void k_cgs_rz(Skew k, const T* r, const T* z, CgState* st, double* part) {
   if (st->done) return;
   __shared__ double sh[32];
-  T rz = T(0);
-  PL_GRID_STRIDE(e, (int)k.total) rz += r[e] * z[e];
-  const double s = block_sum_w(rz, sh);
+  DotAcc<T> rz;
+  PL_GRID_STRIDE(e, (int)k.total) rz.prod(r[e], z[e]);
+  const double s = rz.block(sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (arrive_last(&st->ticket[0])) {
     const double t = sum_partials(part, sh);
@@ -297,7 +299,7 @@ __global__ void __launch_bounds__(SkewRows<C>::THREADS) k_cgs_spmv_dir(Grid g, S
   const T beta = (T)st->beta;
   const int plane = (int)k.plane;
   const int nrows = k.nz * k.R;
-  T dq = T(0);
+  DotAcc<T> dq;
   for (int row = blockIdx.x * RPB + lr; row < nrows; row += gridDim.x * RPB) {
     const int iz = row / k.R;
     const int sr = row - iz * k.R;
@@ -320,12 +322,12 @@ __global__ void __launch_bounds__(SkewRows<C>::THREADS) k_cgs_spmv_dir(Grid g, S
       qq = adiag<T>(g, x, y, zz) * dn + vxm * coef<T>(wall_xm(g, x)) + vxp * coef<T>(wall_xp(g, x)) +
            vym * coef<T>(wall_ym(g, y)) + vyp * coef<T>(wall_yp(g, y)) +
            vzm * coef<T>(wall_zm(g, zz)) + vzp * coef<T>(wall_zp(g, zz));
-      dq += dn * qq;
+      dq.prod(dn, qq);
     }
     d_new[e] = dn;
     q[e] = qq;
   }
-  const double sblk = block_sum_w(dq, sh);
+  const double sblk = dq.block(sh);
   if (threadIdx.x == 0) part[blockIdx.x] = sblk;
   if (arrive_last(&st->ticket[0])) {
     const double t = sum_partials(part, sh);
@@ -384,7 +386,8 @@ __global__ void k_cgs_axpy_v(Skew k, const T* d, const T* q, T* x, T* r, CgState
   constexpr int NV = Vec16<T>::n;
   __shared__ double sh[32];
   const T alpha = (T)st->alpha;
-  T mx = T(-3.0e38), rr = T(0);
+  T mx = T(-3.0e38);
+  DotAcc<T> rr;
   const int nvec = (int)(k.total / NV);
   const V* dv = reinterpret_cast<const V*>(d);
   const V* qv = reinterpret_cast<const V*>(q);
@@ -399,14 +402,14 @@ __global__ void k_cgs_axpy_v(Skew k, const T* d, const T* q, T* x, T* r, CgState
       const T rn = vget<T>(ri, c) + (-alpha) * vget<T>(qq, c);
       vset<T>(ri, c, rn);
       mx = (rn > mx) ? rn : mx;
-      rr += rn * rn;
+      rr.prod(rn, rn);
     }
     xv[i] = xx;
     rv[i] = ri;
   }
   const double s1 = block_max_w(mx, sh, -1.0e308);
   if (threadIdx.x == 0) part[blockIdx.x] = s1;
-  const double s2 = block_sum_w(rr, sh);
+  const double s2 = rr.block(sh);
   if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
   if (arrive_last(&st->ticket[0])) {
     const double tm = max_partials(part, sh);
@@ -432,16 +435,16 @@ __global__ void k_cgs_rz_v(Skew k, const T* r, const T* z, CgState* st, double* 
   typedef typename Vec16<T>::type V;
   constexpr int NV = Vec16<T>::n;
   __shared__ double sh[32];
-  T rz = T(0);
+  DotAcc<T> rz;
   const int nvec = (int)(k.total / NV);
   const V* rv = reinterpret_cast<const V*>(r);
   const V* zv = reinterpret_cast<const V*>(z);
   PL_GRID_STRIDE(i, nvec) {
     const V a = rv[i], b = zv[i];
 #pragma unroll
-    for (int c = 0; c < NV; c++) rz += vget<T>(a, c) * vget<T>(b, c);
+    for (int c = 0; c < NV; c++) rz.prod(vget<T>(a, c), vget<T>(b, c));
   }
-  const double s = block_sum_w(rz, sh);
+  const double s = rz.block(sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (arrive_last(&st->ticket[0])) {
     const double t = sum_partials(part, sh);

@@ -47,11 +47,15 @@ std::string cuda_msg(cudaError_t e, const char* what) {
   return s;
 }
 
+// A failed CUDA call: its text goes to `err` and to the calling thread's
+// error detail (plume_last_error(NULL)), which the handle-less C entry points
+// below report.
 #define NT(x)                                     \
   do {                                            \
     cudaError_t e_ = (x);                         \
     if (e_ != cudaSuccess) {                      \
       err = cuda_msg(e_, #x);                     \
+      plume::global_error() = err;                \
       (void)cudaGetLastError();                   \
       return e_ == cudaErrorMemoryAllocation ? PLUME_ERR_OOM : PLUME_ERR_CUDA; \
     }                                             \
@@ -348,7 +352,7 @@ class Net : public NetRuntime {
     if (params_) cudaFree(params_);
     for (bf16* p : wtc_)
       if (p) cudaFree(p);
-    if (tc_err_) cudaFree(tc_err_);
+    if (tc_err_host_) cudaFreeHost(tc_err_host_);
     if (s_) cudaStreamDestroy(s_);
   }
 
@@ -387,8 +391,9 @@ class Net : public NetRuntime {
       if (conv_tc_supported(kLayers[l].cin, kLayers[l].cout))
         NT(cudaMalloc((void**)&wtc_[l], 27LL * kLayers[l].cin * kLayers[l].cout * sizeof(bf16)));
     }
-    NT(cudaMalloc((void**)&tc_err_, sizeof(int)));
-    NT(cudaMemsetAsync(tc_err_, 0, sizeof(int), s_));
+    NT(cudaHostAlloc((void**)&tc_err_host_, sizeof(int), cudaHostAllocMapped));
+    *tc_err_host_ = 0;
+    NT(cudaHostGetDevicePointer((void**)&tc_err_, tc_err_host_, 0));
     // He-normal weights (fan-in 27*cin; the output layer 16), zero biases.
     // Input channels 1..15 of the first layer carry zeros and keep their
     // weights; only channel 0 (the right-hand side) is drawn.
@@ -673,6 +678,17 @@ class Net : public NetRuntime {
   int launches_per_predict() const override { return 19; }
   int kind() const override { return kind_; }
 
+  // PLUME_ERR_TIMEOUT (and clears the flag) if a tensor-core convolution's
+  // bounded wait expired since the last call; the caller has synchronised
+  // the stream the convolutions ran on.
+  int take_error(std::string& err) override {
+    if (!tc_err_host_ || *(volatile int*)tc_err_host_ == 0) return PLUME_OK;
+    *(volatile int*)tc_err_host_ = 0;
+    err = "tensor-core convolution: a bounded wait for its MMAs expired (output invalid)";
+    plume::global_error() = err;
+    return PLUME_ERR_TIMEOUT;
+  }
+
   int device_ = 0;
   cudaStream_t s_ = nullptr;
   char* params_ = nullptr;
@@ -680,7 +696,10 @@ class Net : public NetRuntime {
   uint2* wf_[NCONV] = {};
   uint2* wb_[NCONV] = {};
   bf16* wtc_[NCONV] = {};   // tcgen05 B-operand copies (supported shapes only)
-  int* tc_err_ = nullptr;   // set by a tensor-core convolution whose wait expired
+  // set by a tensor-core convolution whose wait expired: host memory mapped
+  // into the device, read after the stream is synchronised (take_error)
+  int* tc_err_host_ = nullptr;
+  int* tc_err_ = nullptr;
   bool tc_off_ = getenv("PLUME_CONV_TC") != nullptr && getenv("PLUME_CONV_TC")[0] == '0';
   long long woff_[NCONV + 1] = {}, boff_[NCONV + 1] = {};
   long long nparams_ = 0;
@@ -855,7 +874,7 @@ int plume_net_forward(plume_net* net, const int32_t res[3], int32_t batch, const
   if (rc != PLUME_OK) return fail(rc, err);
   NT(cudaMemcpyAsync(output, ws.y, ws.d[0].cells * batch * 4, cudaMemcpyDeviceToHost, m.s_));
   NT(cudaStreamSynchronize(m.s_));
-  return PLUME_OK;
+  return m.take_error(err);
 }
 
 int plume_net_loss_grad(plume_net* net, const int32_t res[3], int32_t batch, int32_t loss_kind,
@@ -879,7 +898,7 @@ int plume_net_loss_grad(plume_net* net, const int32_t res[3], int32_t batch, int
   NT(cudaMemcpyAsync(grad, m.g_, m.nparams_ * 4, cudaMemcpyDeviceToHost, m.s_));
   NT(cudaStreamSynchronize(m.s_));
   *loss = sum / count;
-  return PLUME_OK;
+  return m.take_error(err);
 }
 
 int plume_dataset_generate(const plume_dataset_spec* spec, plume_dataset** out) {
@@ -1160,6 +1179,8 @@ int plume_net_train(plume_net* net, plume_dataset* dsh, const plume_train_spec* 
     }
   }
   if (cudaStreamSynchronize(s) != cudaSuccess) return fail_free(PLUME_ERR_CUDA, "training");
+  rc = m.take_error(err);
+  if (rc != PLUME_OK) return fail_free(rc, err);
   cudaFreeHost(hidx);
   if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return PLUME_OK;

@@ -18,6 +18,10 @@ class NetRuntime {
   // 0: maps a right-hand side b to the solution; 1: maps the residual of the
   // previous step's pressure to the pressure change
   virtual int kind() const = 0;
+  // After the caller synchronised the prediction's stream: PLUME_ERR_TIMEOUT
+  // (flag cleared, err set) if a convolution's bounded wait expired, so that
+  // its output is invalid; PLUME_OK otherwise.
+  virtual int take_error(std::string& err) = 0;
 };
 
 }  // namespace plume

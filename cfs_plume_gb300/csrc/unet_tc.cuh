@@ -18,8 +18,8 @@
 // (t+1) COUT) of the item's accumulator buffer, commits to an mbarrier, and
 // the 8 warps read the accumulators back with tcgen05.ld (warp w: z-plane
 // w / 4, TMEM lanes 32 (w % 4) ...).
-// Every wait is bounded: on expiry the CTA records an error, still frees its
-// TMEM and returns.
+// Every wait is bounded: on expiry the CTA records an error, waits (bounded,
+// much longer) for the MMAs it issued to retire, frees its TMEM and returns.
 #pragma once
 #include "unet_kernels.cuh"
 
@@ -111,6 +111,7 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
 }
 
 constexpr long long kTcSpinLimit = 1ll << 22;
+constexpr long long kTcDrainLimit = 1ll << 26;  // MMAs still in flight after an expired wait
 
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
@@ -148,7 +149,8 @@ __device__ __forceinline__ void tc_stage(const Dims& d, const View& in, long lon
 
 // out = act(conv3(in, W) + bias) [* (mask > 0)]
 //   wpack : weights in the B-operand layout above (k_prep_tc)
-//   err   : set to 1 if a wait expired
+//   err   : set to 1 if a wait expired (host-mapped: plain stores, read by
+//           the host after it synchronises the stream)
 // Persistent: CTA c takes work items (brick, sample) c, c + gridDim.x, ...;
 // the weights are staged once, the halo in two buffers: while one item's
 // MMAs and epilogue run, the next item's halo is in flight.  The two TMEM
@@ -193,6 +195,8 @@ __global__ void __launch_bounds__(256) k_conv3_tc(Dims d, int batch, View in, co
   constexpr uint32_t idesc = tc_idesc<128, COUT>();
 
   int j = 0;
+  int fail_bar = -1;  // commit barrier and phase of an item whose wait expired
+  unsigned fail_parity = 0;
   for (long long item = blockIdx.x; item < items; item += gridDim.x, j++) {
     const int cur = j & 1;
     const long long next = item + gridDim.x;
@@ -236,7 +240,9 @@ __global__ void __launch_bounds__(256) k_conv3_tc(Dims d, int batch, View in, co
     ok = __syncthreads_and(ok) != 0;  // the TMEM loads below are warp-collective
     tc_fence_after();
     if (!ok) {
-      if (threadIdx.x == 0) atomicExch(err, 1);
+      if (threadIdx.x == 0) *(volatile int*)err = 1;
+      fail_bar = cur;
+      fail_parity = parity;
       break;
     }
     // epilogue: warp w reads TMEM lanes 32 (w % 4) .. of z-plane w / 4
@@ -291,6 +297,9 @@ __global__ void __launch_bounds__(256) k_conv3_tc(Dims d, int batch, View in, co
     }
   }
   cp_async_wait<0>();
+  // the accumulators must not be freed under MMAs that are still running
+  if (fail_bar >= 0 && threadIdx.x == 0)
+    (void)tc_mbar_wait(smem_u32addr(&bars[fail_bar]), fail_parity, kTcDrainLimit);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();

@@ -49,7 +49,13 @@ constexpr int kWaveD = 8;      // inter-warp ring depth (steps)
 constexpr long long kSpinLimit = 1ll << 24;     // shared-memory polls (~0.3 s)
 constexpr long long kSpinLimitSlow = 1ll << 21; // global-flag polls and TMA waits (~2 s)
 
-enum WaveError { WAVE_OK = 0, WAVE_TIMEOUT_RING = 1, WAVE_TIMEOUT_TMA = 2, WAVE_TIMEOUT_FLAG = 3 };
+enum WaveError {
+  WAVE_OK = 0,
+  WAVE_TIMEOUT_RING = 1,
+  WAVE_TIMEOUT_TMA = 2,
+  WAVE_TIMEOUT_FLAG = 3,
+  WAVE_TIMEOUT_GATE = 4
+};
 
 template <typename T>
 struct WaveArgs {
@@ -64,7 +70,32 @@ struct WaveArgs {
   unsigned* ctl;    // [0] slab ticket, [1] exited CTAs
   int* progress;    // [nz] steps completed, for planes read by another slab
   CgState* st;      // skip when st->done; wave_err recorded here
+  // Test hook for the bounded waits: when `gate` is set, one thread per CTA
+  // first polls *gate (a device word that nothing sets) at most gate_spins
+  // times, before any copy is issued; on expiry the CTA records
+  // WAVE_TIMEOUT_GATE and skips its planes, so the sweep ends with nothing in
+  // flight.  Null in normal runs.
+  const int* gate = nullptr;
+  long long gate_spins = 0;
 };
+
+// The entry gate of a sweep CTA (see WaveArgs::gate); false when it expired.
+template <typename T>
+__device__ inline bool wave_pass_gate(const WaveArgs<T>& a, int* failed) {
+  if (!a.gate) return true;
+  if (threadIdx.x == 0) {
+    long long spins = 0;
+    while (*((volatile const int*)a.gate) == 0) {
+      if (++spins > a.gate_spins) {
+        atomicCAS(&a.st->wave_err, 0, (int)WAVE_TIMEOUT_GATE);
+        *((volatile int*)failed) = 1;
+        break;
+      }
+    }
+  }
+  __syncthreads();
+  return *((volatile int*)failed) == 0;
+}
 
 // ------------------------------------------------------------- PTX helpers
 __device__ inline unsigned smem_u32(const void* p) {
@@ -502,7 +533,8 @@ __global__ void __launch_bounds__(32 * 16) k_mic_wave_cl(WaveArgs<T> a) {
   fence_mbar_init();
   __syncthreads();
   cluster_sync_all();  // every CTA's barriers exist before any remote st.async
-  if (warp < nw) {
+  const bool gate_ok = wave_pass_gate(a, failed);
+  if (warp < nw && gate_ok) {
     const int z = BWD ? (zend - 1 - warp) : (z0 + warp);
     RingDst d{0u, 0u, 0u, false};
     bool has_dst = false;
@@ -548,6 +580,7 @@ __global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
   if (threadIdx.x == 0) sm.misc[1] = 0;
   fence_mbar_init();
   __syncthreads();
+  (void)wave_pass_gate(a, failed);  // on expiry the ticket loop below exits at once
   unsigned tpar = 0u, rpar = 0u;  // barrier phases carry over between slabs
   for (;;) {
     if (threadIdx.x == 0) {

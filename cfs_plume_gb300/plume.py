@@ -64,6 +64,7 @@ def load_library(path=LIB_PATH):
         "plume_snapshot_async": (C.c_int, [H, C.c_char_p, C.c_int32, C.c_int32]),
         "plume_wait_snapshots": (C.c_int, [H]),
         "plume_sweep_times": (C.c_int, [H, P(C.c_double), P(C.c_int64)]),
+        "plume_set_wait_gate": (C.c_int, [H, C.c_int32, C.c_int64]),
         "plume_box_init": (C.c_int, [P(PlumeBox), P(C.c_double), P(C.c_double), C.c_double, C.c_double]),
         "plume_box_spin": (C.c_int, [P(PlumeBox)]),
         "plume_box_translate": (C.c_int, [P(PlumeBox)]),
@@ -239,6 +240,11 @@ class Plume:
         ms, n = C.c_double(), C.c_int64()
         _check(self.lib.plume_sweep_times(self.h, C.byref(ms), C.byref(n)), self.h)
         return ms.value, n.value
+
+    def set_wait_gate(self, closed, poll_limit=1000):
+        """Test hook of the MIC sweeps' bounded waits (plume_set_wait_gate):
+        closed=True makes every later sweep time out at its entry gate."""
+        _check(self.lib.plume_set_wait_gate(self.h, 1 if closed else 0, int(poll_limit)), self.h)
 
     def mic_diagonal(self):
         p = np.zeros(self.N)

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define PLUME_ABI_VERSION 1
+#define PLUME_ABI_VERSION 2
 
 typedef enum plume_status {
   PLUME_OK = 0,
@@ -133,6 +133,19 @@ typedef struct plume_step_stats {
   double rhs_norm;          /* ||b||_2                                         */
   double ms_total;          /* device time of the step, CUDA events            */
   double ms_solve;          /* device time of the Poisson solve                */
+  /* Device time of each stage of the step (CUDA events on the handle's
+     stream): the reference's TIMER buckets (src/util/TIMER.cpp:33-149, one
+     per FLUID_3D_MIC member) measured on the device.  The stages and
+     ms_solve add up to ms_total. */
+  double ms_forces;         /* walls, addBuoyancy (FLUID_3D_MIC.cpp:188-199)   */
+  double ms_vorticity;      /* addVorticity and its axpy (524-590, 202)        */
+  double ms_advection;      /* advectStam (595-650)                            */
+  double ms_damping;        /* the damping product (209-212)                   */
+  double ms_divergence;     /* project up to the solve: boundary conditions and
+                               divergence (314-360), the moving box's stomp    */
+  double ms_guess;          /* learned initial guess (residual, network,
+                               Galerkin step); 0 for the other starts         */
+  double ms_gradient;       /* project after the solve: gradient (372-398)     */
 } plume_step_stats;
 
 typedef struct plume_handle plume_handle;

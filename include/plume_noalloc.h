@@ -30,20 +30,27 @@ extern "C" {
                  plume_mic_diagonal; border entries of r are ignored).
    z           : device pointer, N doubles; the interior receives M^-1 r and
                  the border is set to 0.
-   stream      : cudaStream_t to order the work on (NULL = legacy default).
+   stream      : cudaStream_t to order the work on (NULL = legacy default);
+                 it must belong to the current device, whose copy of the
+                 scratch array the call uses.
 
    Work vectors live in one file-scope device array (sizes above); grids that
    do not fit are rejected with PLUME_ERR_INVALID, as are x resolutions above
    258.  The first call on each device looks up that array's device address
-   with the device current, so make the first call on a device before any
-   stream capture.  Every call uses the same array and clears the parts that
+   with the device current and keeps it for the life of the process, so make
+   the first call on a device before any stream capture, and make no call on
+   a device after cudaDeviceReset on it (the kept address would be stale).  Every call uses the same array and clears the parts that
    must start at zero; calls whose work overlaps on the GPU (different streams
    or threads, no ordering between them) race on the array and must not be
    issued.  Returns a plume_status for the checks and launches; the work is
    only queued, so the caller orders or synchronizes on `stream` before
    reading z.  If a sweep's inter-CTA wait expires on the GPU, z is set to NaN
-   everywhere.  Otherwise z equals plume_mic_apply on an FP64 handle of the
-   same grid bit for bit. */
+   everywhere, and the next call starts afresh (it clears the state it
+   needs).  Otherwise z equals plume_mic_apply on an FP64 handle of the same
+   grid bit for bit.  Test hook: with PLUME_NOALLOC_WAIT_GATE=<polls> in the
+   environment, each sweep first polls a device flag that nothing sets, at
+   most <polls> times, before it issues any copy, so the wait expires and z
+   comes back NaN. */
 int plume_mic_apply_noalloc(const int32_t res[3], const int32_t bc[6],
                             const double* precon, const double* r, double* z,
                             void* stream);

@@ -44,6 +44,16 @@ int plume_profile_sweeps(plume_handle* h, int on);
    timed sweep launches and their number.  Waits for the handle's stream. */
 int plume_sweep_times(plume_handle* h, double* ms_total, int64_t* launches);
 
+/* Test hook for the bounded device waits of the MIC sweeps (no counterpart in
+   the reference, whose sweeps are serial loops).  With closed != 0, every
+   later sweep of this handle first polls a device flag that nothing sets, at
+   most poll_limit times (> 0), before it issues any copy; the wait then
+   expires, the sweep records it and returns without touching the vectors, and
+   the solve or step returns PLUME_ERR_TIMEOUT with the handle still usable.
+   closed = 0 restores normal sweeps (poll_limit is ignored).  The sweeps'
+   real waits keep their own, fixed limits. */
+int plume_set_wait_gate(plume_handle* h, int32_t closed, int64_t poll_limit);
+
 #ifdef __cplusplus
 }
 #endif

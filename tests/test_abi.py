@@ -48,13 +48,31 @@ def test_default_params_are_the_reference_defaults(plume_lib):
     assert p.buoyancy == float.fromhex("0x1.99999a0000000p-4")  # (double)0.1f
 
 
-def test_struct_sizes_match_header():
-    # plume_params: see include/plume.h; offsets must agree with the C layout
-    # (checked against sizeof/offsetof of the C header compiled with gcc)
-    assert C.sizeof(_abi.PlumeParams) == 200
-    assert _abi.PlumeParams.seed.offset == 128
-    assert C.sizeof(_abi.PlumeStepStats) == 56
-    assert C.sizeof(_abi.PlumeProductsInfo) == 40
+def test_struct_sizes_match_header(tmp_path):
+    """The ctypes mirrors in _abi.py against sizeof/offsetof of the C header
+    structs, compiled with gcc."""
+    import subprocess
+    checks = [("plume_params", _abi.PlumeParams, "plume.h"),
+              ("plume_step_stats", _abi.PlumeStepStats, "plume.h"),
+              ("plume_products_info", _abi.PlumeProductsInfo, "plume_reduced.h")]
+    lines = ['#include <stdio.h>', '#include <stddef.h>']
+    lines += ['#include "%s"' % h for h in sorted({c[2] for c in checks})]
+    lines.append("int main(void) {")
+    for cname, ct, _ in checks:
+        lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _t in ct._fields_:
+            lines.append('  printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines.append("  return 0; }")
+    src = tmp_path / "sizes.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                   check=True).stdout.splitlines())
+    for cname, ct, _ in checks:
+        assert int(got[cname]) == C.sizeof(ct), cname
+        for fname, _t in ct._fields_:
+            assert int(got[cname + "." + fname]) == getattr(ct, fname).offset, (cname, fname)
 
 
 def test_invalid_params_are_rejected_without_a_device(plume_lib):

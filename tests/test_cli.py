@@ -110,19 +110,33 @@ def test_step_log_lines_are_json(tmp_path):
     src.write_text(
         '#include "cli_config.h"\n#include <cmath>\n#include <cstdio>\n'
         'struct S { int iterations, converged, fallback, launches; double max_residual, rel_residual,'
-        ' rhs_norm, ms_total, ms_solve; };\n'
-        'int main() { S a{93, 1, 0, 471, 8.5e-11, 9.75e-7, 3.25, 29.8125, 21.5};\n'
-        '  S b{1000, 0, 1, 5, NAN, INFINITY, 0.0, 1.0, 0.5};\n'
-        '  std::printf("%s\\n%s\\n", plume_cli::step_json(7, a).c_str(), plume_cli::step_json(8, b).c_str()); }\n')
+        ' rhs_norm, ms_total, ms_solve, ms_forces, ms_vorticity, ms_advection, ms_damping, ms_divergence,'
+        ' ms_guess, ms_gradient; };\n'
+        'int main() { S a{93, 1, 0, 471, 8.5e-11, 9.75e-7, 3.25, 29.8125, 21.5, 0.25, 0.5, 0.5, 0.25, 0.125,'
+        ' 0.0, 0.25};\n'
+        '  S b{1000, 0, 1, 5, NAN, INFINITY, 0.0, 1.0, 0.5, 0, 0, 0, 0, 0, 0, 0};\n'
+        '  std::printf("%s\\n%s\\n", plume_cli::step_json(7, a, 1e6, 4).c_str(),'
+        ' plume_cli::step_json(8, b).c_str()); }\n')
     out = tmp_path / "t"
     subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "cfs_plume_gb300", "csrc"), str(src), "-o",
                     str(out)], check=True)
     lines = subprocess.run([str(out)], capture_output=True, text=True, check=True).stdout.splitlines()
     a, b = (json.loads(l) for l in lines)
+    gbs = a.pop("gbs")
     assert a == {"step": 7, "iterations": 93, "converged": 1, "fallback": 0, "launches": 471,
                  "max_residual": 8.5e-11, "rel_residual": 9.75e-7, "rhs_norm": 3.25, "ms_total": 29.8125,
-                 "ms_solve": 21.5}
+                 "ms_solve": 21.5, "ms_forces": 0.25, "ms_vorticity": 0.5, "ms_advection": 0.5,
+                 "ms_damping": 0.25, "ms_divergence": 0.125, "ms_guess": 0.0, "ms_gradient": 0.25}
+    # algorithmic bytes per interior cell (S = 4) x 1e6 cells / ms
+    assert gbs["forces"] == pytest.approx(16 * 1e6 / 0.25e6)
+    assert gbs["vorticity"] == pytest.approx(74 * 1e6 / 0.5e6)
+    assert gbs["advection"] == pytest.approx(40 * 1e6 / 0.5e6)
+    assert gbs["damping"] == pytest.approx(24 * 1e6 / 0.25e6)
+    assert gbs["divergence"] == pytest.approx(21 * 1e6 / 0.125e6)
+    assert gbs["solve"] == pytest.approx((30 + 93 * 75) * 1e6 / 21.5e6)
+    assert gbs["gradient"] == pytest.approx(28 * 1e6 / 0.25e6)
     assert b["max_residual"] is None and b["rel_residual"] is None and b["step"] == 8 and b["fallback"] == 1
+    assert "gbs" not in b
 
 
 def test_state_header_reads_like_the_reference_file():
