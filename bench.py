@@ -433,6 +433,8 @@ def main():
                     help="both: plain MIC-PCG and the learned warm start (the headline value)")
     ap.add_argument("--weights", default=None, help="warm-start network (default: the committed one)")
     ap.add_argument("--no-moving", action="store_true", help="skip the moving-box step measurement")
+    ap.add_argument("--no-learned-pc", action="store_true",
+                    help="skip the arm with the network as the flexible-CG preconditioner")
     ap.add_argument("--svd-snapshots", type=int, default=48,
                     help="snapshots for the device snapshot-SVD measurement (0: skip)")
     ap.add_argument("--no-reduced", action="store_true", help="skip the reduced-step measurement")
@@ -471,7 +473,7 @@ def main():
                                      warm_start=_abi.WARM_PREVIOUS))
         prev = measure_arm(gp, a, dist, nbox, rank)
         gp.close()
-    lrn = None
+    lrn = lpc = None
     if learned:
         from cfs_plume_gb300.net import PlumeNet
         net = PlumeNet(device=local, path=weights)
@@ -480,6 +482,14 @@ def main():
         net.attach(gl)
         lrn = measure_arm(gl, a, dist, nbox, rank)
         gl.close()
+        if not a.no_learned_pc:
+            # the network as the preconditioner stage: flexible CG with
+            # z = net(r), started from the previous pressure
+            gpc = Plume(_abi.plume_config(res, precision=prec, seed=rank, device=local,
+                                          warm_start=_abi.WARM_PREVIOUS, preconditioner=_abi.PRECOND_NET))
+            net.attach(gpc)
+            lpc = measure_arm(gpc, a, dist, nbox, rank)
+            gpc.close()
         net.close()
     mov = None if a.no_moving else measure_moving(a, dist, res, prec, local, rank)
     svd = measure_snapshot_svd(res, prec, local, rank, a.svd_snapshots) if a.svd_snapshots > 0 else None
@@ -526,11 +536,13 @@ def main():
         "learned_iters_over_plain": (statistics.mean(lrn["iters"]) / statistics.mean(plain["iters"]))
                                     if lrn else None,
         "target_learned_over_plain": 3.0,
+        "learned_pc_over_plain": (lpc["value"] / plain["value"]) if lpc else None,
         "arms": {name: {"value": r["value"], "unit": "steps/s", "ms_per_step": r["ms"] / a.steps,
                         "pcg_iters_per_step": statistics.mean(r["iters"]), "fallbacks": r["fallbacks"],
                         "max_rel_residual": r["max_rel_residual"], "e2e": r["e2e"],
                         "ms_stages": r["stages"]}
-                 for name, r in (("plain", plain), ("previous", prev), ("learned", lrn)) if r is not None},
+                 for name, r in (("plain", plain), ("previous", prev), ("learned", lrn), ("learned_pc", lpc))
+                 if r is not None},
         "achieved_gbs_step": step_bytes / (ms_max / a.steps / 1000.0) / 1e9,
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "k_mic_wave_cl (MIC(0) forward/backward sweep)",

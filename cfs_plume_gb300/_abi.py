@@ -15,6 +15,7 @@ PREC_FP64, PREC_FP32 = 0, 1
 CRIT_REFERENCE, CRIT_REL2 = 0, 1
 SRC_COLUMN, SRC_BOX, SRC_NONE = 0, 1, 2
 WARM_ZERO, WARM_PREVIOUS, WARM_LEARNED = 0, 1, 2
+PRECOND_MIC, PRECOND_NET = 0, 1
 
 # plume_field, in the state-file order of FLUID_3D_MIC::writeGz (FLUID_3D_MIC.cpp:1057-1103)
 FIELDS = [
@@ -57,7 +58,8 @@ class PlumeParams(C.Structure):
         ("warm_start", C.c_int32),
         ("cache_fields", C.c_int32),
         ("device", C.c_int32),
-        ("reserved", C.c_int32 * 8),
+        ("preconditioner", C.c_int32),
+        ("reserved", C.c_int32 * 7),
     ]
 
 

@@ -222,6 +222,8 @@ class EngineT : public Engine {
     if (p.warm_start != PLUME_WARM_ZERO && p.warm_start != PLUME_WARM_PREVIOUS &&
         p.warm_start != PLUME_WARM_LEARNED)
       return fail(PLUME_ERR_INVALID, "unknown warm start");
+    if (p.preconditioner != PLUME_PRECOND_MIC && p.preconditioner != PLUME_PRECOND_NET)
+      return fail(PLUME_ERR_INVALID, "unknown preconditioner");
     g_.X = p.res[0];
     g_.Y = p.res[1];
     g_.Z = p.res[2];
@@ -589,16 +591,22 @@ class EngineT : public Engine {
     }
     PL_TRY(cudaEventRecord(ev_[1], s_));
     NvtxRange solve_range("solvePoisson");
-    // a learned-start solve gets at most twice the previous step's
-    // iterations: a guess that does not pay off falls back early
+    // a learned-start or network-preconditioned solve gets at most twice the
+    // previous step's iterations: a network that does not pay off falls back
+    // early
+    const bool flex = p_.preconditioner == PLUME_PRECOND_NET;
+    if (flex && !net_) return fail(PLUME_ERR_STATE, "network preconditioner without an attached network");
+    const bool uses_net = learned || flex;
     int cap = p_.max_iters;
-    if (learned && last_iters_ > 0) cap = std::min(p_.max_iters, std::max(20, 2 * last_iters_));
-    int rc = solve_device(div_, pres_, cap, !learned && keep_p == 0);
+    if (uses_net && last_iters_ > 0) cap = std::min(p_.max_iters, std::max(20, 2 * last_iters_));
+    int rc = flex ? solve_fcg(div_, pres_, cap, !learned && keep_p == 0)
+                  : solve_device(div_, pres_, cap, !learned && keep_p == 0);
     if (rc != PLUME_OK) return rc;
-    // a convolution whose bounded wait expired left the guess invalid (the
-    // solve above has synchronised the stream): treat it as a rejected guess
-    const bool net_failed = learned && net_->take_error(err_) != PLUME_OK;
-    if (learned && (!st_host_->converged || net_failed)) {
+    // a convolution whose bounded wait expired left the guess or a
+    // preconditioner output invalid (the solve above has synchronised the
+    // stream): treat it as a rejected solve
+    const bool net_failed = uses_net && net_->take_error(err_) != PLUME_OK;
+    if (uses_net && (!st_host_->converged || net_failed)) {
       // the guess did not lead to convergence: plain MIC-PCG from p = 0
       last_fallback_ = 1;
       PL_TRY(cudaMemsetAsync(pres_, 0, (size_t)g_.N * sizeof(T), s_));
@@ -718,7 +726,13 @@ class EngineT : public Engine {
     if (rc != PLUME_OK) return rc;
     stages_valid_ = false;
     PL_TRY(cudaEventRecord(ev_[1], s_));
-    rc = solve_device(div_, pres_);
+    if (p_.preconditioner == PLUME_PRECOND_NET) {
+      if (!net_) return fail(PLUME_ERR_STATE, "network preconditioner without an attached network");
+      rc = solve_fcg(div_, pres_, -1, false);
+      if (rc == PLUME_OK && net_->take_error(err_) != PLUME_OK) return PLUME_ERR_TIMEOUT;
+    } else {
+      rc = solve_device(div_, pres_);
+    }
     if (rc != PLUME_OK) return rc;
     PL_TRY(cudaEventRecord(ev_[2], s_));
     PL_TRY(cudaEventRecord(ev_[0], s_));
@@ -1087,6 +1101,62 @@ class EngineT : public Engine {
       prof_cur_ ^= 1;
       if (st_host_->done) break;
       if (chunk < 16) chunk *= 2;
+    }
+    return finish_solve(x, false);
+  }
+
+  // The network as the preconditioner stage: z = net(r) on skewed vectors
+  // (through the natural-layout planes r_ and z_, whose borders the network
+  // neither reads nor writes).
+  int precondition_net(const T* rs, T* zs) {
+    const int gK = grid_for(k_.total);
+    k_from_skew<T><<<gK, 256, 0, s_>>>(g_, k_, rs, r_);
+    PL_CHECK_LAUNCH();
+    const int prc = net_->predict(net_ws_, r_, z_, std::is_same<T, double>::value ? 1 : 0, s_, err_);
+    if (prc != PLUME_OK) return prc;
+    launches_ += net_->launches_per_predict();
+    k_to_skew<T, T><<<gK, 256, 0, s_>>>(g_, k_, z_, zs);
+    PL_CHECK_LAUNCH();
+    return PLUME_OK;
+  }
+
+  // Flexible CG (FCG(1), k_cgs_rz_fcg) with the network as the
+  // preconditioner stage, the reference's loop (FLUID_3D_MIC.cpp:951-1013)
+  // with z = net(r) in place of applyMICPreconditioner and the direction
+  // update made A-orthogonal.  The same set-up, stop tests and state as
+  // solve_device.  Host-driven: one synchronisation per iteration, after the
+  // update, so that no network pass runs once the stop test is met (a pass
+  // costs several MIC-PCG iterations).
+  int solve_fcg(const T* b, T* x, int max_iters, bool x_zero) {
+    if (max_iters < 0) max_iters = p_.max_iters;
+    const int gK = grid_for(k_.total);
+    k_to_skew<T, T><<<gK, 256, 0, s_>>>(g_, k_, b, sb_);
+    PL_CHECK_LAUNCH();
+    k_to_skew<T, T><<<gK, 256, 0, s_>>>(g_, k_, x, sx_);
+    PL_CHECK_LAUNCH();
+    k_cgs_init<T><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, k_, sb_, sx_, sr_, st_, part_, p_.tol,
+                                                      max_iters, p_.criterion, x_zero ? 1 : 0);
+    PL_CHECK_LAUNCH();
+    int rc = precondition_net(sr_, sz_);
+    if (rc != PLUME_OK) return rc;
+    k_cgs_init2<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sr_, sz_, (T*)nullptr, st_, part_);
+    PL_CHECK_LAUNCH();
+    PL_TRY(cudaMemsetAsync(sd_, 0, (size_t)k_.total * sizeof(T), s_));
+    T* dcur = sd_;
+    T* dnext = sd2_;
+    for (int it = 0; it <= max_iters; it++) {
+      rc = launch_spmv_dir(sz_, dcur, dnext, sq_);
+      if (rc != PLUME_OK) return rc;
+      k_cgs_axpy_v<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, dnext, sq_, sx_, sr_, st_, part_);
+      PL_CHECK_LAUNCH();
+      PL_TRY(cudaMemcpyAsync(st_host_, st_, sizeof(CgState), cudaMemcpyDeviceToHost, s_));
+      PL_TRY(cudaStreamSynchronize(s_));
+      if (st_host_->done) break;
+      rc = precondition_net(sr_, sz_);
+      if (rc != PLUME_OK) return rc;
+      k_cgs_rz_fcg<T><<<kRedBlocks, kRedThreads, 0, s_>>>(k_, sr_, sz_, sq_, dnext, st_, part_);
+      PL_CHECK_LAUNCH();
+      std::swap(dcur, dnext);
     }
     return finish_solve(x, false);
   }

@@ -465,4 +465,64 @@ __global__ void k_cgs_rz_v(Skew k, const T* r, const T* z, CgState* st, double* 
   }
 }
 
+// Flexible CG, iteration part 3 (Notay, "Flexible conjugate gradients",
+// SIAM J. Sci. Comput. 22(4), 2000: FCG(1)).  After z = M(r) with a
+// preconditioner M that may change from one application to the next (the
+// network), the next direction d' = z + beta d is made A-orthogonal to the
+// last one: beta = -(z.q) / (d.q) with q = A d of the iteration that just
+// ended (st->dq).  deltaNew = d'.r = z.r + beta (d.r), so that the next
+// k_cgs_spmv_dir takes alpha = d'.r / d'.q, the exact line search along d',
+// which never increases the A-norm error whatever M returned.  With a fixed
+// SPD M and exact arithmetic d.r = 0 and this is the PCG iteration.  The
+// exit tests are those of k_cgs_rz_v.
+template <typename T>
+__global__ void k_cgs_rz_fcg(Skew k, const T* r, const T* z, const T* q, const T* d, CgState* st,
+                             double* part) {
+  if (st->done) return;
+  typedef typename Vec16<T>::type V;
+  constexpr int NV = Vec16<T>::n;
+  __shared__ double sh[32];
+  DotAcc<T> zr, zq, dr;
+  const int nvec = (int)(k.total / NV);
+  const V* rv = reinterpret_cast<const V*>(r);
+  const V* zv = reinterpret_cast<const V*>(z);
+  const V* qv = reinterpret_cast<const V*>(q);
+  const V* dv = reinterpret_cast<const V*>(d);
+  PL_GRID_STRIDE(i, nvec) {
+    const V a = rv[i], b = zv[i], c = qv[i], e = dv[i];
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+      zr.prod(vget<T>(b, j), vget<T>(a, j));
+      zq.prod(vget<T>(b, j), vget<T>(c, j));
+      dr.prod(vget<T>(e, j), vget<T>(a, j));
+    }
+  }
+  const double s1 = zr.block(sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s1;
+  const double s2 = zq.block(sh);
+  if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
+  const double s3 = dr.block(sh);
+  if (threadIdx.x == 0) part[2 * kRedBlocks + blockIdx.x] = s3;
+  if (arrive_last(&st->ticket[0])) {
+    const double tzr = sum_partials(part, sh);
+    const double tzq = sum_partials(part + kRedBlocks, sh);
+    const double tdr = sum_partials(part + 2 * kRedBlocks, sh);
+    if (threadIdx.x == 0) {
+      const double beta = st->dq != 0.0 ? -tzq / st->dq : 0.0;
+      st->deltaOld = st->deltaNew;
+      st->deltaNew = tzr + beta * tdr;
+      st->beta = beta;
+      st->iter += 1;
+      if (st->wave_err) st->done = 3;
+      if (st->criterion == 0) {
+        const double relative = fabs((st->maxR - st->oldMaxR) / st->oldMaxR);
+        if (relative < 1e-7) st->done = st->done ? st->done : 2;
+        if (!(st->maxR > st->tol)) st->converged = 1;
+      }
+      if (st->converged || st->iter >= st->max_iters) st->done = st->done ? st->done : 1;
+      st->ticket[0] = 0;
+    }
+  }
+}
+
 }  // namespace plume

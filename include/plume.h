@@ -69,6 +69,17 @@ typedef enum plume_warm_start {
   PLUME_WARM_LEARNED = 2   /* learned initial guess; plain MIC-PCG still judges */
 } plume_warm_start;
 
+typedef enum plume_preconditioner {
+  /* MIC(0)-PCG, the reference's solve (FLUID_3D_MIC.cpp:918-1015) */
+  PLUME_PRECOND_MIC = 0,
+  /* flexible CG (Notay's FCG(1): each new direction A-orthogonal to the last,
+     exact line search) with the attached network as the preconditioner
+     stage, z = net(r); no counterpart in the reference.  Same stop test; a
+     solve that misses it within its iteration cap reruns as MIC-PCG from
+     p = 0, so plain MIC-PCG stays the fallback and the judge. */
+  PLUME_PRECOND_NET = 1
+} plume_preconditioner;
+
 typedef enum plume_field {
   /* order = the state file order of FLUID_3D_MIC::writeGz (FLUID_3D_MIC.cpp:1057-1103) */
   PLUME_F_DENSITY = 0,
@@ -120,7 +131,8 @@ typedef struct plume_params {
                               (prevorticity, preadvection, ... , FLUID_3D_MIC.h:156-190);
                               0: keep only what the step itself needs          */
   int32_t device;          /* CUDA device ordinal                               */
-  int32_t reserved[8];
+  int32_t preconditioner;  /* plume_preconditioner (0: MIC(0), the reference's) */
+  int32_t reserved[7];
 } plume_params;
 
 typedef struct plume_step_stats {
