@@ -396,6 +396,90 @@ def svd_record(r, fp64_peak_tflops):
                          "achieved_gbs": qr_bytes / qr_s / 1e9 if qr_s > 0 else None}}
 
 
+def measure_batched(steps, warmup, seed=0, n=64):
+    """The batched-plume configuration: `n` randomised plumes of uneven grids
+    (plume_batch_params: 32^3 .. 96x128x96, source position, buoyancy and
+    vorticity drawn per instance), FP32 fields, MIC(0)-PCG rel-L2 1e-6,
+    stepped together (plume_batch_run).  Aggregate interior cell-steps/s."""
+    import numpy as np
+    from cfs_plume_gb300.batch import PlumeBatch, batch_params
+    params = [batch_params(seed, i) for i in range(n)]
+    cells = np.array([(p.res[0] - 2) * (p.res[1] - 2) * (p.res[2] - 2) for p in params], dtype=np.float64)
+    b = PlumeBatch(params)
+    b.run(0, warmup, stats=False)
+    secs, stats = b.run(warmup, steps, stats=True)
+    b.close()
+    grids = {}
+    for p in params:
+        k = "x".join(str(v) for v in p.res)
+        grids[k] = grids.get(k, 0) + 1
+    return {"value": cells.sum() * steps / secs, "unit": "interior cell-steps/s", "instances": n,
+            "steps": steps, "warmup": warmup, "seconds": secs, "instance_steps_per_s": n * steps / secs,
+            "pcg_iters_per_step_mean": float(np.mean([[s.iterations for s in st] for st in stats])),
+            "all_converged": all(s.converged for st in stats for s in st), "grids": grids,
+            "interior_cells_total": float(cells.sum()),
+            "workload": "%d randomised closed-box plumes of the batched configuration, FP32 fields, "
+                        "MIC(0)-PCG rel-L2 1e-6, one handle and CUDA stream per instance" % n}
+
+
+def net_forward_mode(spec, warmup=3, iters=5):
+    """--net-forward X,Y,Z: wall time of the warm-start network's forward pass
+    (host input in, host output out) on a seeded standard-normal field with
+    the committed weights: `warmup` untimed passes, then `iters` timed ones.
+    PLUME_CONV_TC=0 runs every convolution on the mma.sync kernel."""
+    import numpy as np
+    from cfs_plume_gb300.net import PlumeNet
+    res = tuple(int(v) for v in spec.split(","))
+    net = PlumeNet(seed=0, path=os.path.join(ROOT, "cfs_plume_gb300", "weights", "unet_warmstart.bin"))
+    x = np.random.default_rng(0).standard_normal((1, res[2], res[1], res[0])).astype(np.float32)
+    for _ in range(warmup):
+        net.forward(x, res)
+    t0 = time.perf_counter()
+    for _ in range(iters):
+        y = net.forward(x, res)
+    ms = (time.perf_counter() - t0) / max(1, iters) * 1000.0
+    net.close()
+    print(json.dumps({"res": res, "forward_ms_wall": ms, "mean_abs_output": float(np.abs(y).mean()),
+                      "tcgen05": os.environ.get("PLUME_CONV_TC", "1") != "0"}), flush=True)
+    return 0
+
+
+def products_mode(spec, rank=32, warmup=1, iters=1):
+    """--products X,Y,Z: the projected-operator build of a reduced model
+    (buildOutOfCoreMatrices, plume_reduced_build_products) on seeded
+    synthetic bases of `rank` columns (U.pressure N_int rows, U.preproject,
+    U.prediffuse, U.final 3 N_int), reference default walls."""
+    import numpy as np
+    import shutil
+    from cfs_plume_gb300 import _abi
+    from cfs_plume_gb300.plume import Plume, build_products
+    res = tuple(int(v) for v in spec.split(","))
+    nint = (res[0] - 2) * (res[1] - 2) * (res[2] - 2)
+    rng = np.random.default_rng(11)
+    d = tempfile.mkdtemp(prefix="plume_products_") + "/"
+    try:
+        _write_eigen(d + "U.pressure.matrix", rng.standard_normal((nint, rank)) / math.sqrt(nint))
+        for fn in ("U.preproject.matrix", "U.prediffuse.matrix", "U.final.matrix"):
+            _write_eigen(d + fn, rng.standard_normal((3 * nint, rank)) / math.sqrt(3 * nint))
+        g = Plume(_abi.default_params(res=res))
+        for _ in range(warmup):
+            build_products(g, d)
+        dev = wall = 0.0
+        info = None
+        for _ in range(iters):
+            info = build_products(g, d)
+            dev += info["ms_device"]
+            wall += info["ms_total"]
+        g.close()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    n = max(1, iters)
+    print(json.dumps({"res": res, "rank": rank, "ms_device": dev / n, "ms_total": wall / n,
+                      "gflop": info["gflop"], "tflops": info["gflop"] / (dev / n) if dev > 0 else None}),
+          flush=True)
+    return 0
+
+
 def moving_record(m, res, N, nint, S, peak, steps):
     # the stomp reads every velocity (border cells for the postIOP copy), writes
     # postIOP everywhere, the inside mask on the interior, and inside the box
@@ -438,10 +522,20 @@ def main():
     ap.add_argument("--svd-snapshots", type=int, default=48,
                     help="snapshots for the device snapshot-SVD measurement (0: skip)")
     ap.add_argument("--no-reduced", action="store_true", help="skip the reduced-step measurement")
+    ap.add_argument("--batch-steps", type=int, default=10,
+                    help="timed steps of the 64-plume batched configuration (0: skip)")
+    ap.add_argument("--net-forward", default=None, metavar="X,Y,Z",
+                    help="only time the network's forward pass at this grid")
+    ap.add_argument("--products", default=None, metavar="X,Y,Z",
+                    help="only time the projected-operator build at this grid")
     a = ap.parse_args()
     rank, world, local = dist_env()
     if a.impl == "reference":
         return run_reference(a, rank, world)
+    if a.net_forward:
+        return net_forward_mode(a.net_forward)
+    if a.products:
+        return products_mode(a.products)
     a.warmup = max(a.warmup, 3)
 
     from cfs_plume_gb300 import _abi
@@ -494,6 +588,7 @@ def main():
     mov = None if a.no_moving else measure_moving(a, dist, res, prec, local, rank)
     svd = measure_snapshot_svd(res, prec, local, rank, a.svd_snapshots) if a.svd_snapshots > 0 else None
     red = None if a.no_reduced else measure_reduced(a.steps, local, rank)
+    bat = measure_batched(a.batch_steps, 3, seed=rank) if a.batch_steps > 0 else None
     clk = clocks.stop()
     head = lrn if lrn is not None else plain
     ms_max, value, iters = head["ms"], head["value"], head["iters"]
@@ -566,6 +661,7 @@ def main():
         "snapshot_svd": svd_record(svd, 2 * 2 * 152 * 2.070e9 / 1e12) if svd else None,
         "reduced_step": reduced_record(red, peak) if red else None,
         "reduced_products": products_record(red, 2 * 2 * 152 * 2.070e9 / 1e12) if red else None,
+        "batched": bat,
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": nbox * 8,
                 "d2h_bytes_per_step": 3 * N * 8},
         "clocks": clk,

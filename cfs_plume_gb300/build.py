@@ -131,12 +131,18 @@ def build(verbose=False, ptxas_info=False):
 
 def build_oracle(with_reference=True):
     """CPU oracle (test infrastructure): oracle/_build/libplume_oracle.so, and
-    oracle/_ref/fluid3d_ref when the reference sources are present."""
+    oracle/_ref/ (the reference's own step, SVD and reduced stages) when the
+    reference sources are present (PLUME_REFERENCE_DIR, else the location the
+    oracle's Makefile names)."""
     odir = os.path.join(ROOT, "oracle")
     _run(["make", "-s", "-C", odir, "-j8"])
-    ref = os.environ.get("PLUME_REFERENCE_DIR", "/root/reference")
-    if with_reference and os.path.isdir(os.path.join(ref, "src", "integrators")):
+    if not with_reference:
+        return
+    ref = os.environ.get("PLUME_REFERENCE_DIR")
+    if ref:
         _run(["make", "-s", "-C", odir, "-j8", "ref", "REF=" + ref])
+    else:  # the oracle recipe's own location of the reference tree, if present
+        _run(["make", "-s", "-C", odir, "-j8", "ref-if-present"])
 
 
 def main():

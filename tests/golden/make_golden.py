@@ -8,8 +8,9 @@ configurations and stores what it produced:
                         the reference's own FLUID_3D_MIC::readGz) and the PCG
                         iteration count of every step;
   ref_cfg1_sampled.npz  the 48x64x48 plume (box source, closed box, FP64,
-                        reference criterion 1e-10), 3 steps: iteration counts,
-                        per-field sums / L2 norms and every 97th value;
+                        reference criterion 1e-10), all 100 steps of its
+                        configuration: iteration counts, per-field sums / L2
+                        norms and every 97th value;
   ref_state_8x10x6/     the reference's own state file (writeGz, gzip level 1)
                         and appendStreams output after 2 steps, as format
                         fixtures;
@@ -36,9 +37,9 @@ configurations and stores what it produced:
                         same bases under mixed walls, and the fields and reduced
                         coordinates after 12 reduced steps under those walls.
 
-Needs the reference tree (PLUME_REFERENCE_DIR, default /root/reference) and
+Needs the reference built by `make -C oracle ref REF=<reference tree>` and
 writes nothing outside tests/golden/.
-Usage: python tests/golden/make_golden.py [plume|moving|svd|reduced]   (default: all)
+Usage: python tests/golden/make_golden.py [plume|cfg1|moving|svd|reduced]   (default: all)
 """
 import os
 import shutil
@@ -134,6 +135,8 @@ def main():
     what = sys.argv[1] if len(sys.argv) > 1 else "all"
     if what in ("all", "plume"):
         plume_fixtures()
+    if what in ("all", "plume", "cfg1"):
+        cfg1_fixture()
     if what in ("all", "moving"):
         moving_fixtures()
     if what in ("all", "svd"):
@@ -257,20 +260,6 @@ def plume_fixtures():
         shutil.rmtree(d)
         print(name, "iters", iters)
 
-    # the benchmark plume at 48x64x48, summarised
-    res = (48, 64, 48)
-    p = _abi.plume_config(res, precision=_abi.PREC_FP64, criterion=_abi.CRIT_REFERENCE, tol=1e-10)
-    d, iters, fields = run_ref(p, 3, "box")
-    out = dict(iters=np.array(iters), steps=3, **params_record(p))
-    for n in _abi.FIELDS:
-        a = fields[n]
-        out["sum_" + n] = a.sum()
-        out["l2_" + n] = np.sqrt((a * a).sum())
-        out["sample_" + n] = a[::97].copy()
-    np.savez_compressed(os.path.join(HERE, "ref_cfg1_sampled.npz"), **out)
-    shutil.rmtree(d)
-    print("cfg1 iters", iters)
-
     # format fixtures: the reference's own state file and streams
     fx = os.path.join(HERE, "ref_state_8x10x6")
     shutil.rmtree(fx, ignore_errors=True)
@@ -288,6 +277,23 @@ def plume_fixtures():
     np.savez_compressed(os.path.join(fx, "fields.npz"), **fields, **params_record(p))
     shutil.rmtree(d)
     print("format fixture:", sorted(os.listdir(fx)))
+
+
+def cfg1_fixture(steps=100):
+    """The benchmark plume at 48x64x48 (configuration 1: FP64, the reference's
+    own 1e-10 stop test), all of its steps, summarised."""
+    res = (48, 64, 48)
+    p = _abi.plume_config(res, precision=_abi.PREC_FP64, criterion=_abi.CRIT_REFERENCE, tol=1e-10)
+    d, iters, fields = run_ref(p, steps, "box")
+    out = dict(iters=np.array(iters), steps=steps, **params_record(p))
+    for n in _abi.FIELDS:
+        a = fields[n]
+        out["sum_" + n] = a.sum()
+        out["l2_" + n] = np.sqrt((a * a).sum())
+        out["sample_" + n] = a[::97].copy()
+    np.savez_compressed(os.path.join(HERE, "ref_cfg1_sampled.npz"), **out)
+    shutil.rmtree(d)
+    print("cfg1 iters", iters)
 
 
 def moving_fixtures():

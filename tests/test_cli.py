@@ -154,3 +154,52 @@ def test_state_header_reads_like_the_reference_file():
         ref = read_state(path)
         assert tuple(ints) == tuple(ref["header_ints"])
         assert tuple(dbls) == tuple(ref["header_doubles"])
+
+
+@pytest.mark.gpu
+def test_read_state_resumes_bit_exact(tmp_path):
+    """plume_read_state (FLUID_3D_MIC::readGz into a handle) as a checkpoint:
+    two FP64 steps, the state written, a new handle reads it and takes the
+    third step; its fields equal those of three straight steps bit for bit,
+    and the step count and time come back from the file."""
+    from cfs_plume_gb300.plume import Plume
+    p = _abi.default_params(res=(16, 20, 12), vorticity_eps=2.0)
+    straight = Plume(p)
+    for s in range(2):
+        straight.add_source(s)
+        straight.step()
+    path = str(tmp_path / "fluid.0001.fluid3d.gz")
+    straight.write_state(path)
+    straight.add_source(2)
+    straight.step()
+    resumed = Plume(p)
+    resumed.read_state(path)
+    info = resumed.info()
+    assert info["total_steps"] == 2
+    resumed.add_source(2)
+    resumed.step()
+    for name in ("velocity", "density", "heat", "pressure", "divergence", "vorticity"):
+        assert np.array_equal(resumed.field(name), straight.field(name)), name
+    straight.close()
+    resumed.close()
+
+
+@pytest.mark.gpu
+def test_cli_resume_from_continues_the_run(exe, tmp_path):
+    """`resume from` in fluid3D: a run of 2 steps, then a second run resumed
+    from its last state file for one more step, writes the same third state
+    file as a straight 3-step run (FP64, reference stop test)."""
+    base = "xRes = 12\nyRes = 14\nzRes = 10\nvorticity = 1.5\nwrite streams = 0\n"
+    a, b = str(tmp_path) + "/a/", str(tmp_path) + "/b/"
+    (tmp_path / "a.cfg").write_text(base + "snapshot path = %s\nsimulation snapshots = 3\n" % a)
+    (tmp_path / "b1.cfg").write_text(base + "snapshot path = %s\nsimulation snapshots = 2\n" % b)
+    (tmp_path / "b2.cfg").write_text(base + "snapshot path = %s\nsimulation snapshots = 3\n"
+                                     "resume from = %sfluid.0001.fluid3d.gz\n" % (b, b))
+    for c in ("a.cfg", "b1.cfg", "b2.cfg"):
+        r = subprocess.run([exe, str(tmp_path / c)], capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, (c, r.stderr)
+    assert "Resuming after step 2" in r.stdout
+    sa, sb = read_state(a + "fluid.0002.fluid3d.gz"), read_state(b + "fluid.0002.fluid3d.gz")
+    assert tuple(sa["header_ints"]) == tuple(sb["header_ints"])
+    for name in _abi.FIELDS:
+        assert np.array_equal(sa[name], sb[name]), name

@@ -139,10 +139,11 @@ def test_solve_fp64_vs_oracle():
 
 
 def test_fp32_plume_against_fp64_oracle():
-    """FP32 fields with FP64 CG scalars at rel-residual 1e-6 against the FP64
-    oracle at the same residual, 48x64x48 plume, 20 steps.  Bound: 1e-3
-    relative L2 on velocity and density (the solver tolerance itself admits
-    per-step pressure differences of ~1e-6 that the flow then carries)."""
+    """FP32 fields with FP64-class CG reductions at rel-residual 1e-6 against
+    the FP64 oracle at the same residual, 48x64x48 plume, 20 steps.  Bound:
+    1e-4 relative L2 on velocity and density, the bound of the FP32
+    configuration (the 128x192x128 plume is held to it over 200 steps in
+    test_parity_plume.py)."""
     res = (48, 64, 48)
     pg = _abi.plume_config(res, precision=_abi.PREC_FP32)
     po = _abi.plume_config(res, precision=_abi.PREC_FP64)
@@ -157,7 +158,7 @@ def test_fp32_plume_against_fp64_oracle():
     ev = rel_l2(g.field("velocity"), o.field("velocity"))
     ed = rel_l2(g.field("density"), o.field("density"))
     print("fp32 vs fp64 oracle after 20 steps: velocity %.3e density %.3e" % (ev, ed))
-    assert ev < 1e-3 and ed < 1e-3
+    assert ev < 1e-4 and ed < 1e-4
 
 
 def test_state_file_is_reference_format(tmp_path):

@@ -270,3 +270,77 @@ def test_reduced3d_binary_command_line(tmp_path):
     iop.write_text("xRes = 10\nyRes = 12\nzRes = 8\niop = 1\n")
     r = subprocess.run([exe, str(iop)], capture_output=True, text=True)
     assert r.returncode == 1 and "initOutOfCoreIOP" in r.stderr
+
+
+def _full_rank_truth(z, d):
+    """The full-rank FP64 run of the fixture's plume on the GPU, its state
+    file written after every step (fluid.%04i.fluid3d.gz, as fluid3D writes
+    them): the ground truth diffGroundTruth reads."""
+    from cfs_plume_gb300 import _abi
+    from cfs_plume_gb300.plume import Plume
+    res = tuple(int(v) for v in z["res"])
+    g = Plume(_abi.default_params(res=res, vorticity_eps=float(z["vorticity_eps"])))
+    os.makedirs(d, exist_ok=True)
+    for s in range(int(z["steps"])):
+        g.add_source(s)
+        g.step()
+        g.write_state(os.path.join(d, "fluid.%04d.fluid3d.gz" % s))
+    g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_ground_truth_errors_on_gpu_state_files(tmp_path, case):
+    """The reduced step's ground-truth comparison (diffGroundTruth,
+    SUBSPACE_FLUID_3D_EIGEN.cpp:804-835) on the GPU against state files this
+    build's FP64 full-rank run wrote: every step's four errors agree with
+    those the reference recorded against its own full-rank files (both runs
+    and both reduced models agree to 1e-8, so the errors to 1e-3 relative)."""
+    from cfs_plume_gb300 import _abi
+    z = _fixture(case)
+    d = str(tmp_path / "red") + "/"
+    truth = str(tmp_path / "truth") + "/"
+    _write_model(z, d)
+    _full_rank_truth(z, truth)
+    from cfs_plume_gb300.plume import Plume, ReducedModel
+    res = tuple(int(v) for v in z["res"])
+    g = Plume(_abi.default_params(res=res, vorticity_eps=float(z["vorticity_eps"])))
+    m = ReducedModel(g, d)
+    m.set_ground_truth(truth)
+    for s in range(int(z["steps"])):
+        g.add_source(s)
+        m.step()
+    e = m.errors()
+    assert e.shape == z["errors"].shape
+    np.testing.assert_allclose(e, z["errors"], rtol=1e-3, atol=1e-12)
+    m.close()
+    g.close()
+
+
+@pytest.mark.gpu
+def test_reduced3d_binary_runs_the_reference_model(tmp_path):
+    """bin/reduced3D on the reference's sparse-cubature model with the
+    reference's cfg keys, against this build's full-rank state files: it
+    prints the reference's error vectors (every 10 steps and at the end) and
+    the last ones equal the reference's recorded errors to 1e-3 relative."""
+    import subprocess
+    from cfs_plume_gb300 import build
+    build.build()
+    z = _fixture("sparse_10x12x8")
+    d = str(tmp_path / "red") + "/"
+    truth = str(tmp_path / "truth") + "/"
+    _write_model(z, d)
+    _full_rank_truth(z, truth)
+    cfg = tmp_path / "reduced.cfg"
+    cfg.write_text("xRes = 10\nyRes = 12\nzRes = 8\nvorticity = %r\nreduced path = %s\nsnapshot path = %s\n"
+                   "simulation snapshots = %d\n" % (float(z["vorticity_eps"]), d, truth, int(z["steps"])))
+    r = subprocess.run([os.path.abspath(RED_EXE), str(cfg)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    vals = {}
+    for line in r.stdout.splitlines():
+        for k in ("velocityAbs", "velocityRelative", "densityAbs", "densityRelative"):
+            if line.strip().startswith(k + " = ["):
+                vals[k] = [float(v) for v in line.split("[")[1].split("]")[0].split()]
+    last = [vals[k][-1] for k in ("velocityAbs", "velocityRelative", "densityAbs", "densityRelative")]
+    assert len(vals["velocityAbs"]) == int(z["steps"])
+    np.testing.assert_allclose(last, z["errors"][-1], rtol=1e-3, atol=1e-12)
