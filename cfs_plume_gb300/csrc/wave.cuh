@@ -46,6 +46,7 @@ __host__ __device__ inline long long skew_index(const Skew& k, int ix, int iy, i
 constexpr int kWaveKB = 8;     // rows per TMA block (contiguous in the skewed layout)
 constexpr int kWavePF = 3;     // TMA ring depth (blocks)
 constexpr int kWaveD = 8;      // inter-warp ring depth (steps)
+static_assert(kWaveD == kWaveKB, "sweep_plane maps step u of a TMA block to ring slot u");
 constexpr long long kSpinLimit = 1ll << 24;     // shared-memory polls (~0.3 s)
 constexpr long long kSpinLimitSlow = 1ll << 21; // global-flag polls and TMA waits (~2 s)
 
@@ -356,9 +357,9 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
     for (int j = 0; j < issued; j++) issue(j);
   bool ok = true;
   const T* din = tma;
-  // make step t's block current (issue ahead, wait for it); false on timeout
-  auto enter_block = [&](int t) -> bool {
-    const int j = t / kWaveKB;
+  // make block j current (issue the block kWavePF - 1 ahead, wait for j's
+  // copies); false on timeout
+  auto enter_block = [&](int j) -> bool {
     if (j + kWavePF - 1 < nblocks) {
       if (lane == 0) issue(j + kWavePF - 1);
       issued = j + kWavePF;
@@ -376,42 +377,43 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
     din = tma + (size_t)slot * 2 * kWaveKB * W;
     return true;
   };
-  T vin[C], vp[C];
-  auto load_step = [&](int t) {
-    const int tb = t % kWaveKB;
-    const int n_blk = min(kWaveKB, R - (t - tb));
-    const int rib = BWD ? (n_blk - 1 - tb) : tb;
-    lds_row<T, C>(din + (size_t)rib * W + lane * C, vin);
-    lds_row<T, C>(din + (size_t)(kWaveKB + rib) * W + lane * C, vp);
-  };
-  // the consumer may be at most D steps behind; arm its slot for step t
-  int next_seen = 0;
-  auto open_dst = [&](int t) -> bool {
-    if (next_seen <= t - kWaveD) {
-      long long spins = 0;
-      for (;;) {
-        next_seen = ld_remote_relaxed(dst.prog);  // a shared::cta address is valid here too
-        if (next_seen > t - kWaveD) break;
-        if (++spins > kSpinLimit || ld_vol(failed)) {
-          if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_RING, failed);
-          return false;
-        }
-      }
-    }
-    if (lane == 0) mbar_arm_remote(dst.rbar + (unsigned)((t % kWaveD) * sizeof(uint64_t)), rowb);
-    return true;
-  };
-  if (!enter_block(0)) ok = false;
-  if (ok) load_step(0);
-  if (ok && has_dst) ok = open_dst(0);
   T cy[C];
 #pragma unroll
   for (int j = 0; j < C; j++) cy[j] = T(0);
   T edge = T(0);
-  for (int t = 0; t < R && ok; t++) {
+  int next_seen = 0;
+  // Step t, the u-th of its block (the block's rows at `blk`, n_blk of
+  // them); false after an expired wait.  Blocks start at multiples of
+  // kWaveKB == kWaveD, so the ring slot of step t is u: in a full block,
+  // which the caller unrolls, every slot index, row offset and bookkeeping
+  // test below is a compile-time constant.
+  auto step = [&](const int t, const int u, const T* blk, const int n_blk) -> bool {
+    const int rs = u;
+    if (has_dst) {
+      // the consumer may be at most D steps behind.  Its consumed-step
+      // counter moves in fours, so the test is made for four steps at a
+      // time: before steps t .. t+3 the consumer must have consumed step
+      // t + 3 - D.  Then this step's slot is armed.
+      if ((u & 3) == 0 && next_seen <= t + 3 - kWaveD) {
+        long long spins = 0;
+        for (;;) {
+          next_seen = ld_remote_relaxed(dst.prog);  // a shared::cta address is valid here too
+          if (next_seen > t + 3 - kWaveD) break;
+          if (++spins > kSpinLimit || ld_vol(failed)) {
+            if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_RING, failed);
+            return false;
+          }
+        }
+      }
+      if (lane == 0) mbar_arm_remote(dst.rbar + (unsigned)(rs * sizeof(uint64_t)), rowb);
+    }
+    // this step's inputs from the block's TMA slot
+    const int rib = BWD ? (n_blk - 1 - u) : u;
+    T vin[C], vp[C];
+    lds_row<T, C>(blk + (size_t)rib * W + lane * C, vin);
+    lds_row<T, C>(blk + (size_t)(kWaveKB + rib) * W + lane * C, vp);
     // ---- critical chain: neighbour value -> cell updates -> hand-off ----
     T cz[C];
-    const int rs = t % kWaveD;
     if (no_input) {
 #pragma unroll
       for (int j = 0; j < C; j++) cz[j] = T(0);
@@ -419,13 +421,9 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
       long long spins = 0;
       while (!mbar_try_wait_cluster(&rbar_in[rs], (rparity >> rs) & 1u)) {
         if (++spins > kSpinLimit || ld_vol(failed)) {
-          ok = false;
-          break;
+          if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_RING, failed);
+          return false;
         }
-      }
-      if (!ok) {
-        if (lane == 0) wave_fail(a.st, WAVE_TIMEOUT_RING, failed);
-        break;
       }
       rparity ^= 1u << rs;
       lds_row<T, C>(ring_in + (size_t)rs * W + lane * C, cz);
@@ -452,7 +450,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
       const unsigned off = (unsigned)(((size_t)rs * W + lane * C) * sizeof(T));
       st_async_row<T, C>(dst.ring + off, pass, dst.rbar + (unsigned)(rs * sizeof(uint64_t)));
     }
-    // ---- off the chain: output, next step's inputs, bookkeeping ----
+    // ---- off the chain: output and bookkeeping ----
 #pragma unroll
     for (int j = 0; j < C; j++) cy[j] = pass[j];
     T* orow = outp + (size_t)(BWD ? (R - 1 - t) : t) * W + lane * C;
@@ -464,7 +462,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
 #pragma unroll
       for (int j = 0; j < C; j++) orow[j] = vout[j];
     }
-    if ((t & 3) == 3 || t + 1 == R) {  // report consumed ring steps (back-pressure)
+    if ((u & 3) == 3 || t + 1 == R) {  // report consumed ring steps (back-pressure)
       __syncwarp();
       if (lane == 0) st_vol(&sm.prog[warp], t + 1);
     }
@@ -474,16 +472,29 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
       __syncwarp();
       if (lane == 0) st_vol(&sm.misc[2], t + 1);
     }
-    if (t + 1 < R) {
-      if ((t + 1) % kWaveKB == 0 && !enter_block(t + 1)) {
-        ok = false;
-        break;
-      }
-      load_step(t + 1);
-      if (has_dst && !open_dst(t + 1)) {
-        ok = false;
-        break;
-      }
+    return true;
+  };
+  for (int j = 0; j < nblocks && ok; j++) {
+    if (!enter_block(j)) {
+      ok = false;
+      break;
+    }
+    const int t0 = j * kWaveKB;
+    const int n = min(kWaveKB, R - t0);
+    const T* blk = din;
+    if (n == kWaveKB) {
+#pragma unroll
+      for (int u = 0; u < kWaveKB; u++)
+        if (!step(t0 + u, u, blk, kWaveKB)) {
+          ok = false;
+          break;
+        }
+    } else {
+      for (int u = 0; u < n; u++)
+        if (!step(t0 + u, u, blk, n)) {
+          ok = false;
+          break;
+        }
     }
   }
   // every issued TMA block must land before its slot is reused or the CTA exits
