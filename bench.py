@@ -154,16 +154,33 @@ def bytes_per_iteration(nint, S, P):
     return nint * (16 * S + 2 * P + 3)
 
 
-def cpu_baseline(res, steps):
-    """The oracle (FP64 CPU restatement of the reference step, 1 thread) on the
-    first `steps` steps of the same plume: steps/s."""
+def host_cpu():
+    """(logical cores, model name) of this host."""
+    model = None
+    try:
+        for line in open("/proc/cpuinfo"):
+            k = line.split(":")[0].strip().lower()
+            if k in ("model name", "cpu part") and model is None:
+                model = line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return os.cpu_count(), model
+
+
+def cpu_baseline(res, steps, skip=0):
+    """The oracle (FP64 CPU restatement of the reference step, 1 thread, as
+    the reference runs) on steps skip .. skip+steps-1 of the same plume, the
+    first `skip` run untimed (the GPU arms' warm-up window): steps/s."""
     from cfs_plume_gb300 import _abi
     from oracle import oracle
     p = _abi.plume_config(res, precision=_abi.PREC_FP64)
     o = oracle.Oracle(p)
+    for s in range(skip):
+        o.add_source(s)
+        o.step()
     t0 = time.perf_counter()
     iters = []
-    for s in range(steps):
+    for s in range(skip, skip + steps):
         o.add_source(s)
         iters.append(o.step().iterations)
     dt = time.perf_counter() - t0
@@ -179,17 +196,22 @@ def run_reference(args, rank, world):
         return 0
     res = RES
     sample = max(1, min(args.steps, 3))
-    v, iters, dt = cpu_baseline(res, sample)
+    skip = max(0, min(args.warmup, 5))
+    v, iters, dt = cpu_baseline(res, sample, skip)
+    cores, model = host_cpu()
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": world,
-        "steps": sample, "warmup": 0, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+        "steps": sample, "warmup": skip, "ms_per_step": 1000.0 / v, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "plume 128x192x128, closed box, box source +-0.05 seeded noise, "
                                "buoyancy 1, vorticity 2, MIC(0)-PCG rel-residual 1e-6",
                    "res": list(res)},
         "pcg_iters_per_step": statistics.mean(iters),
         "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
-                         "sample": "first %d steps from rest of the same plume (%.1f s)" % (sample, dt)},
+                         "host_cores": cores, "host_cpu": model,
+                         "sample": "steps %d-%d of the same plume after %d untimed warm-up steps, as the GPU "
+                                   "arms' timed window starts (%.1f s, %s PCG iterations); the reference step "
+                                   "is single-threaded" % (skip, skip + sample - 1, skip, dt, iters)},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -667,10 +689,14 @@ def main():
         "clocks": clk,
     }
     if rank == 0 and a.cpu_steps > 0:
-        v, it_cpu, dt = cpu_baseline(res, a.cpu_steps)
+        skip = min(a.warmup, 5)
+        v, it_cpu, dt = cpu_baseline(res, a.cpu_steps, skip)
+        cores, model = host_cpu()
         line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
-                                "sample": "first %d step(s) from rest of the same plume, FP64 "
-                                          "oracle (%.1f s, %s PCG iterations)" % (a.cpu_steps, dt, it_cpu)}
+                                "host_cores": cores, "host_cpu": model,
+                                "sample": "steps %d-%d of the same plume after %d untimed warm-up steps, FP64 "
+                                          "oracle, single-threaded as the reference (%.1f s, %s PCG iterations)"
+                                          % (skip, skip + a.cpu_steps - 1, skip, dt, it_cpu)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
