@@ -139,9 +139,9 @@ def measured_peaks():
 
 
 # DRAM bytes (read + write) of one sweep launch from an ncu capture of this
-# workload (profiles/mic_wave_and_cg_kernels_plume_128x192x128_fp32.md), keyed
-# by grid and field bytes.
-SWEEP_DRAM_BYTES = {((128, 192, 128), 4): 28.529152e6 + 35.84e3}
+# workload (dram__bytes.sum.per_second x gpu__time_duration.sum of one forward
+# and one backward launch), keyed by grid and field bytes.
+SWEEP_DRAM_BYTES = {((128, 192, 128), 4): 28.57e6}
 
 
 def bytes_per_step(nint, iters, S, P):

@@ -111,6 +111,28 @@ inline cudaError_t once_per_device(std::atomic<unsigned long long>& done, F&& se
   return e;
 }
 
+// The same for a vector field, two cells per thread: the 6 doubles of a cell
+// pair are 48 contiguous bytes, written as three 16-byte stores (dst 16-byte
+// aligned); an odd last cell is written by one thread.
+template <typename T>
+__global__ void k_vec_to_host2(const T* a, const T* b, const T* c, long long N, double* dst) {
+  const long long np = N / 2;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < np;
+       p += (long long)gridDim.x * blockDim.x) {
+    const long long c0 = 2 * p;
+    double2* o = reinterpret_cast<double2*>(dst + 6 * p);
+    o[0] = make_double2((double)a[c0], (double)b[c0]);
+    o[1] = make_double2((double)c[c0], (double)a[c0 + 1]);
+    o[2] = make_double2((double)b[c0 + 1], (double)c[c0 + 1]);
+  }
+  if ((N & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const long long l = N - 1;
+    dst[3 * l] = (double)a[l];
+    dst[3 * l + 1] = (double)b[l];
+    dst[3 * l + 2] = (double)c[l];
+  }
+}
+
 template <typename T, int C, bool EXACT>
 cudaError_t launch_wave_c(const WaveArgs<T>& a, int grid, size_t smem, cudaStream_t s) {
   void (*kf)(WaveArgs<T>) = a.backward ? k_mic_wave<T, C, EXACT, true> : k_mic_wave<T, C, EXACT, false>;
@@ -1382,7 +1404,10 @@ class EngineT : public Engine {
   int fetch_vec(const V3<T>& v, double* dst) {
     if (host_direct_) {
       const long long N = g_.N;
-      k_planes_to_host<T><<<grid_for(3 * N), 256, 0, s_>>>(v.x, v.y, v.z, 3, N, dst);
+      if (((uintptr_t)dst & 15) == 0)
+        k_vec_to_host2<T><<<grid_for(N / 2 + 1), 256, 0, s_>>>(v.x, v.y, v.z, N, dst);
+      else
+        k_planes_to_host<T><<<grid_for(3 * N), 256, 0, s_>>>(v.x, v.y, v.z, 3, N, dst);
       PL_CHECK_LAUNCH();
       PL_TRY(cudaStreamSynchronize(s_));
       return PLUME_OK;

@@ -30,7 +30,7 @@ struct CgState {
 };
 
 constexpr int kRedThreads = 256;
-constexpr int kRedBlocks = 608;  // 4 x 152 SMs
+constexpr int kRedBlocks = 912;  // 6 x 152 SMs: every reduction kernel keeps 6 blocks of 8 warps resident
 
 // Off-diagonal coefficient toward a neighbour: -1 unless the neighbour is a wall.
 template <typename T>
