@@ -154,6 +154,26 @@ def bytes_per_iteration(nint, S, P):
     return nint * (16 * S + 2 * P + 3)
 
 
+# Algorithmic bytes per interior cell of each stage outside the solve (the
+# canonical model: each pass reads its operands and writes its results once,
+# stencil neighbours from cache, wall flags one byte): the same figures the
+# fluid3D step log uses.
+STAGE_BYTES = {"forces": lambda S: 4 * S, "vorticity": lambda S: 18 * S + 2, "advection": lambda S: 10 * S,
+               "damping": lambda S: 6 * S, "divergence": lambda S: 5 * S + 1, "gradient": lambda S: 7 * S}
+
+
+def stage_roofline(stages, nint, S, peak):
+    """Achieved GB/s and fraction of the measured HBM rate of each stencil
+    stage from its mean device time."""
+    out = {}
+    for k, f in STAGE_BYTES.items():
+        ms = stages.get(k, 0.0)
+        gbs = f(S) * nint / (ms * 1e6) if ms > 0 else None
+        out[k] = {"ms": ms, "achieved_gbs": gbs, "frac": (gbs / peak) if gbs else None,
+                  "bytes_per_cell": f(S)}
+    return out
+
+
 def host_cpu():
     """(logical cores, model name) of this host."""
     model = None
@@ -444,6 +464,45 @@ def measure_batched(steps, warmup, seed=0, n=64):
                         "MIC(0)-PCG rel-L2 1e-6, one handle and CUDA stream per instance" % n}
 
 
+LARGE_RES = (256, 384, 256)
+
+
+def measure_large(steps, warmup, weights, local, rank):
+    """The large plume of the same family (256x384x256, ~25M cells, the
+    source box scaled the same way), FP32 fields, rel-L2 1e-6: plain MIC-PCG
+    and the learned warm start with the network trained on 64x96x64 plumes
+    (no retraining), `steps` device-timed steps after `warmup`."""
+    from cfs_plume_gb300 import _abi
+    from cfs_plume_gb300.plume import Plume
+    out = {}
+    for arm in ("plain", "learned"):
+        if arm == "learned" and not os.path.exists(weights):
+            continue
+        g = Plume(_abi.plume_config(LARGE_RES, seed=rank, device=local,
+                                    warm_start=_abi.WARM_LEARNED if arm == "learned" else _abi.WARM_ZERO))
+        net = None
+        if arm == "learned":
+            from cfs_plume_gb300.net import PlumeNet
+            net = PlumeNet(device=local, path=weights)
+            net.attach(g)
+        g.run_timed(0, warmup, stats=False)
+        ms, stats = g.run_timed(warmup, steps)
+        g.close()
+        if net is not None:
+            net.close()
+        out[arm] = {"value": 1000.0 * steps / ms, "unit": "steps/s", "ms_per_step": ms / steps,
+                    "pcg_iters_per_step": statistics.mean(s.iterations for s in stats),
+                    "fallbacks": sum(s.fallback for s in stats),
+                    "all_converged": all(s.converged for s in stats)}
+    rec = {"workload": "plume %dx%dx%d (~25M cells), closed box, box source +-0.05 seeded noise, buoyancy 1, "
+                       "vorticity 2, FP32 fields, MIC(0)-PCG rel-residual 1e-6; learned: the warm-start network "
+                       "trained on 64x96x64 plumes, not retrained" % LARGE_RES,
+           "steps": steps, "warmup": warmup, "arms": out}
+    if "learned" in out:
+        rec["learned_over_plain"] = out["learned"]["value"] / out["plain"]["value"]
+    return rec
+
+
 def net_forward_mode(spec, warmup=3, iters=5):
     """--net-forward X,Y,Z: wall time of the warm-start network's forward pass
     (host input in, host output out) on a seeded standard-normal field with
@@ -544,6 +603,8 @@ def main():
     ap.add_argument("--svd-snapshots", type=int, default=48,
                     help="snapshots for the device snapshot-SVD measurement (0: skip)")
     ap.add_argument("--no-reduced", action="store_true", help="skip the reduced-step measurement")
+    ap.add_argument("--large-steps", type=int, default=5,
+                    help="timed steps of the 256x384x256 plume, plain and learned (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=10,
                     help="timed steps of the 64-plume batched configuration (0: skip)")
     ap.add_argument("--net-forward", default=None, metavar="X,Y,Z",
@@ -611,6 +672,7 @@ def main():
     svd = measure_snapshot_svd(res, prec, local, rank, a.svd_snapshots) if a.svd_snapshots > 0 else None
     red = None if a.no_reduced else measure_reduced(a.steps, local, rank)
     bat = measure_batched(a.batch_steps, 3, seed=rank) if a.batch_steps > 0 else None
+    big = measure_large(a.large_steps, 3, weights, local, rank) if a.large_steps > 0 else None
     clk = clocks.stop()
     head = lrn if lrn is not None else plain
     ms_max, value, iters = head["ms"], head["value"], head["iters"]
@@ -676,6 +738,9 @@ def main():
                      "ns_per_hyperplane": (sweep_avg_ms * 1e6 / hyperplanes(res)) if sweep_avg_ms else None,
                      "pass": "second pass of K steps with CUDA events around each sweep launch "
                              "(host-driven CG loop); value is timed with the CG loop as a CUDA graph"},
+        "stage_roofline": dict(stage_roofline(head["stages"], nint, S, peak),
+                               note="per stencil stage of the headline arm: mean CUDA-event time, algorithmic "
+                                    "bytes per interior cell x N_int; grid-stride kernels, HBM-bound"),
         "solve_roofline": {"kernel": "poisson solve (all MIC-PCG kernels)", "achieved": achieved_solve,
                            "unit": "GB/s", "frac": (achieved_solve / peak) if achieved_solve else None,
                            "bytes_model": "N_int*(5S+2P+2 + iters*(16S+2P+3)) per solve"},
@@ -684,6 +749,7 @@ def main():
         "reduced_step": reduced_record(red, peak) if red else None,
         "reduced_products": products_record(red, 2 * 2 * 152 * 2.070e9 / 1e12) if red else None,
         "batched": bat,
+        "large_plume": big,
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": nbox * 8,
                 "d2h_bytes_per_step": 3 * N * 8},
         "clocks": clk,

@@ -15,8 +15,16 @@ STRIDE-th value of those four fields (the same cells for every run):
   oracle_plume_128x192x128_tol1e-06.npz    rel-L2 1e-6 (the benchmark's test)
   oracle_plume_128x192x128_tol1e-10.npz    rel-L2 1e-10 (the converged field)
 
-Usage: python tests/golden/make_golden_plume.py <tol> [steps]
-A run takes 20-40 minutes on one core; the two tolerances can run side by side.
+and, for the large plume of the same family (256x384x256, the box scaled the
+same way), the first 12 steps at rel-L2 1e-6 with samples after steps 6 and
+12, every 1021st value:
+
+  oracle_plume_256x384x256_tol1e-06.npz
+
+Usage: python tests/golden/make_golden_plume.py <tol> [steps] [--res X,Y,Z]
+                                               [--snapshots a,b,..] [--stride n]
+A 128x192x128 run takes 20-60 minutes on one core, the 256x384x256 one about
+an hour; runs can go side by side.
 """
 import os
 import sys
@@ -41,12 +49,21 @@ def fixture_path(tol, res=RES):
 
 
 def main():
-    tol = float(sys.argv[1])
-    steps = int(sys.argv[2]) if len(sys.argv) > 2 else 200
-    p = _abi.plume_config(RES, precision=_abi.PREC_FP64, criterion=_abi.CRIT_REL2, tol=tol)
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("tol", type=float)
+    ap.add_argument("steps", type=int, nargs="?", default=200)
+    ap.add_argument("--res", default=",".join(str(v) for v in RES))
+    ap.add_argument("--snapshots", default=",".join(str(v) for v in SNAPSHOTS))
+    ap.add_argument("--stride", type=int, default=STRIDE)
+    a = ap.parse_args()
+    tol, steps, stride = a.tol, a.steps, a.stride
+    res = tuple(int(v) for v in a.res.split(","))
+    snapshots = tuple(int(v) for v in a.snapshots.split(","))
+    p = _abi.plume_config(res, precision=_abi.PREC_FP64, criterion=_abi.CRIT_REL2, tol=tol)
     o = oracle.Oracle(p)
-    rec = {"res": np.array(RES), "tol": tol, "steps": steps, "stride": STRIDE,
-           "snapshots": np.array([s for s in SNAPSHOTS if s <= steps])}
+    rec = {"res": np.array(res), "tol": tol, "steps": steps, "stride": stride,
+           "snapshots": np.array([s for s in snapshots if s <= steps])}
     iters, rel = [], []
     norms = {f: [] for f in FIELDS}
     sums = {f: [] for f in FIELDS}
@@ -60,8 +77,8 @@ def main():
             a = o.field(f)
             norms[f].append(np.sqrt((a * a).sum()))
             sums[f].append(a.sum())
-            if s + 1 in SNAPSHOTS:
-                rec["sample_%s_%d" % (f, s + 1)] = a[::STRIDE].copy()
+            if s + 1 in snapshots:
+                rec["sample_%s_%d" % (f, s + 1)] = a[::stride].copy()
         print("step %d iters %d rel %.3e  %.0f s" % (s + 1, st.iterations, st.rel_residual,
                                                      time.time() - t0), flush=True)
     rec["iters"] = np.array(iters)
@@ -69,8 +86,8 @@ def main():
     for f in FIELDS:
         rec["l2_" + f] = np.array(norms[f])
         rec["sum_" + f] = np.array(sums[f])
-    np.savez_compressed(fixture_path(tol), **rec)
-    print("wrote", fixture_path(tol))
+    np.savez_compressed(fixture_path(tol, res), **rec)
+    print("wrote", fixture_path(tol, res))
 
 
 if __name__ == "__main__":

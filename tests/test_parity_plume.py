@@ -127,3 +127,52 @@ def test_fp32_plume_200_steps_against_fp64_oracle(arm):
         report[name + " max norm deviation"] = float(dn.max())
         assert dn.max() < NORM_BOUND, (arm, name, dn.max())
     print(arm, {k: ("%.3g" % v) for k, v in report.items()})
+
+
+# ---- the large plume of the same family: 256x384x256 (~25M cells) ----
+LARGE = (256, 384, 256)
+
+
+def large_fixture():
+    path = os.path.join(GOLDEN, "oracle_plume_%dx%dx%d_tol1e-06.npz" % LARGE)
+    if not os.path.exists(path):  # written by make_golden_plume.py --res 256,384,256 (about an hour)
+        pytest.skip("oracle fixture %s not generated" % os.path.basename(path))
+    return np.load(path)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("arm", ["plain", "learned"])
+def test_large_plume_against_fp64_oracle(arm):
+    """256x384x256, FP32 fields, rel-L2 1e-6: the plain solver and the learned
+    warm start (the network trained on 64x96x64 plumes, not retrained) against
+    the FP64 oracle's first 12 steps at the same stop test: velocity and
+    density within 1e-4 relative L2 after steps 6 and 12 (inside the
+    predictability horizon), every solve meeting the stop test without
+    falling back, and the L2 norms within 1e-4 at every step."""
+    from cfs_plume_gb300.plume import Plume
+    f = large_fixture()
+    stride, steps = int(f["stride"]), int(f["steps"])
+    kw = dict(warm_start=_abi.WARM_LEARNED) if arm == "learned" else {}
+    g = Plume(_abi.plume_config(LARGE, **kw))
+    net = None
+    if arm == "learned":
+        from cfs_plume_gb300.net import PlumeNet
+        net = PlumeNet(path=WEIGHTS)
+        net.attach(g)
+    report = {}
+    for s in range(steps):
+        g.add_source(s)
+        st = g.step()
+        assert st.converged == 1 and st.fallback == 0 and st.rel_residual <= 1e-6, (s, st.rel_residual)
+        for name in ("velocity", "density"):
+            a = g.field(name)
+            dn = abs(np.linalg.norm(a) - f["l2_" + name][s]) / f["l2_" + name][s]
+            assert dn < BOUND, (arm, name, s, dn)
+            if s + 1 in tuple(int(v) for v in f["snapshots"]):
+                e = rel(a[::stride], f["sample_%s_%d" % (name, s + 1)])
+                report["%s step %d" % (name, s + 1)] = e
+                assert e < BOUND, (arm, name, s + 1, e)
+    g.close()
+    if net is not None:
+        net.close()
+    print(arm, {k: "%.2e" % v for k, v in report.items()})
