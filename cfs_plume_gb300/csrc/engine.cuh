@@ -950,6 +950,26 @@ class EngineT : public Engine {
 
   // fused direction update + SpMV (skew_kernels.cuh), dispatched on C
   int launch_spmv_dir(const T* z, const T* d_old, T* d_new, T* q) {
+    // 16-byte groups where the cells per lane divide into them
+    constexpr int NV = Vec16<T>::n;
+    if (k_.C % NV == 0) {
+      switch (k_.C) {
+#define PL_SPMV_V_CASE(CC)                                                                              \
+  case CC:                                                                                              \
+    k_cgs_spmv_dir_v<T, (CC % NV == 0 ? CC : NV)><<<kRedBlocks, kRedThreads, 0, s_>>>(g_, k_, z, d_old, \
+                                                                                      d_new, q, st_,  \
+                                                                                      part_);         \
+    PL_CHECK_LAUNCH();                                                                                  \
+    return PLUME_OK;
+        PL_SPMV_V_CASE(2)
+        PL_SPMV_V_CASE(4)
+        PL_SPMV_V_CASE(6)
+        PL_SPMV_V_CASE(8)
+#undef PL_SPMV_V_CASE
+        default:
+          break;
+      }
+    }
     switch (k_.C) {
 #define PL_SPMV_CASE(CC)                                                                         \
   case CC:                                                                                       \

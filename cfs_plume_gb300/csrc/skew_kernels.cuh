@@ -378,6 +378,102 @@ __device__ inline void vset<double>(double2& v, int i, double x) {
   if (i == 0) v.x = x; else v.y = x;
 }
 
+// k_cgs_spmv_dir on 16-byte groups: a thread takes NV consecutive values of
+// one lane's segment of a row (4 FP32 or 2 FP64 cells; C % NV == 0, so a group
+// never straddles two lanes) and loads the group, its y and z neighbour
+// groups as vectors; the x neighbours inside the group come from registers,
+// the two at its ends as scalars (the previous or next lane's cell sits one
+// row up or down in the skewed layout).  Each cell evaluates the same
+// expression as k_cgs_spmv_dir (bit for bit in FP64, which is compiled
+// without multiply-add contraction); the order in which d.q is summed
+// differs.
+template <typename T, int C>
+__global__ void __launch_bounds__(kRedThreads) k_cgs_spmv_dir_v(Grid g, Skew k, const T* z, const T* d_old,
+                                                                T* d_new, T* q, CgState* st, double* part) {
+  if (st->done) return;
+  typedef typename Vec16<T>::type V;
+  constexpr int NV = Vec16<T>::n;
+  constexpr int W = 32 * C, GPR = W / NV;  // groups per row
+  static_assert(C % NV == 0, "a group must lie in one lane's segment");
+  __shared__ double sh[32];
+  const T beta = (T)st->beta;
+  const int plane = (int)k.plane;
+  const int ngroups = k.nz * k.R * GPR;
+  DotAcc<T> dq;
+  PL_GRID_STRIDE(gi, ngroups) {
+    const int row = gi / GPR;
+    const int ix0 = (gi - row * GPR) * NV;
+    const int lane = ix0 / C, jb0 = ix0 - lane * C;
+    const int iz = row / k.R;
+    const int iy = row - iz * k.R - lane;
+    const int e0 = row * W + ix0;
+    V dnv, qv;
+    if (iy >= 0 && iy < k.ny && ix0 < k.nx) {
+      const int y = iy + 1, zz = iz + 1;
+      auto dirv = [&](int e) {  // z + beta d_old at e, as a vector
+        const V a = *reinterpret_cast<const V*>(z + e), b = *reinterpret_cast<const V*>(d_old + e);
+        V r;
+#pragma unroll
+        for (int j = 0; j < NV; j++) vset<T>(r, j, vget<T>(b, j) * beta + vget<T>(a, j));
+        return r;
+      };
+      const V dc = dirv(e0);
+      const V dym = iy > 0 ? dirv(e0 - W) : V{};
+      const V dyp = iy + 1 < k.ny ? dirv(e0 + W) : V{};
+      const V dzm = iz > 0 ? dirv(e0 - plane) : V{};
+      const V dzp = iz + 1 < k.nz ? dirv(e0 + plane) : V{};
+      // x neighbours at the group's ends
+      const int el = jb0 > 0 ? e0 - 1 : e0 - W - 1;
+      const int er = jb0 + NV < C ? e0 + NV : e0 + NV - 1 + W + 1;
+      const T xl = ix0 > 0 ? d_old[el] * beta + z[el] : T(0);
+      const T xr = ix0 + NV < k.nx ? d_old[er] * beta + z[er] : T(0);
+#pragma unroll
+      for (int j = 0; j < NV; j++) {
+        const int ix = ix0 + j, x = ix + 1;
+        T dn = T(0), qq = T(0);
+        if (ix < k.nx) {
+          dn = vget<T>(dc, j);
+          const T vxm = ix > 0 ? (j > 0 ? vget<T>(dc, j - 1) : xl) : T(0);
+          const T vxp = ix + 1 < k.nx ? (j + 1 < NV ? vget<T>(dc, j + 1) : xr) : T(0);
+          const T vym = iy > 0 ? vget<T>(dym, j) : T(0);
+          const T vyp = iy + 1 < k.ny ? vget<T>(dyp, j) : T(0);
+          const T vzm = iz > 0 ? vget<T>(dzm, j) : T(0);
+          const T vzp = iz + 1 < k.nz ? vget<T>(dzp, j) : T(0);
+          qq = adiag<T>(g, x, y, zz) * dn + vxm * coef<T>(wall_xm(g, x)) + vxp * coef<T>(wall_xp(g, x)) +
+               vym * coef<T>(wall_ym(g, y)) + vyp * coef<T>(wall_yp(g, y)) +
+               vzm * coef<T>(wall_zm(g, zz)) + vzp * coef<T>(wall_zp(g, zz));
+          dq.prod(dn, qq);
+        }
+        vset<T>(dnv, j, dn);
+        vset<T>(qv, j, qq);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NV; j++) {
+        vset<T>(dnv, j, T(0));
+        vset<T>(qv, j, T(0));
+      }
+    }
+    *reinterpret_cast<V*>(d_new + e0) = dnv;
+    *reinterpret_cast<V*>(q + e0) = qv;
+  }
+  const double sblk = dq.block(sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = sblk;
+  if (arrive_last(&st->ticket[0])) {
+    const double t = sum_partials(part, sh);
+    if (threadIdx.x == 0) {
+      st->dq = t;
+      if (fabs(t) > 0.0) {
+        st->alpha = st->deltaNew / t;
+      } else {  // "PCG alpha broke down! Bailing." (FLUID_3D_MIC.cpp:962-969)
+        st->done = 1;
+        st->broke = 1;
+      }
+      st->ticket[0] = 0;
+    }
+  }
+}
+
 // Iteration part 2, vectorised: x += alpha d, r -= alpha q, signed max(r), r.r
 template <typename T>
 __global__ void k_cgs_axpy_v(Skew k, const T* d, const T* q, T* x, T* r, CgState* st, double* part) {

@@ -138,6 +138,38 @@ def test_solve_fp64_vs_oracle():
     assert sg.rel_residual <= 1e-8
 
 
+@pytest.mark.parametrize("precision", [_abi.PREC_FP64, _abi.PREC_FP32])
+def test_solve_on_wide_rows_vs_oracle(precision):
+    """A grid 128 cells wide (4 cells per lane): the SpMV/direction kernel
+    takes its 16-byte-group form in both precisions.  FP64 within 1e-9 and one
+    iteration of the oracle's solve; FP32 (rel-L2 1e-6, as the benchmark
+    configuration) within 1e-5 of the FP64 solution and two iterations."""
+    res = (128, 24, 16)
+    po = _abi.plume_config(res, precision=_abi.PREC_FP64, criterion=_abi.CRIT_REL2, tol=1e-8)
+    o = oracle.Oracle(po)
+    for s in range(3):
+        o.add_source(s)
+        o.step()
+    b = o.field("divergence")
+    tol = 1e-8 if precision == _abi.PREC_FP64 else 1e-6
+    p = _abi.plume_config(res, precision=precision, criterion=_abi.CRIT_REL2, tol=tol)
+    xo, so = oracle.solve_poisson(p if precision == _abi.PREC_FP64 else
+                                  _abi.plume_config(res, precision=_abi.PREC_FP64, criterion=_abi.CRIT_REL2,
+                                                    tol=1e-6), b)
+    xg, sg = Plume(p).solve_poisson(b)
+    interior = np.zeros((res[2], res[1], res[0]), dtype=bool)
+    interior[1:-1, 1:-1, 1:-1] = True
+    m = interior.ravel()
+    a, r = xg[m] - xg[m].mean(), xo[m] - xo[m].mean()  # closed box: up to a constant
+    if precision == _abi.PREC_FP64:
+        assert abs(sg.iterations - so.iterations) <= 1
+        assert rel_l2(a, r) < 1e-9
+    else:
+        assert abs(sg.iterations - so.iterations) <= 2
+        assert rel_l2(a, r) < 1e-5
+    assert sg.rel_residual <= tol
+
+
 def test_fp32_plume_against_fp64_oracle():
     """FP32 fields with FP64-class CG reductions at rel-residual 1e-6 against
     the FP64 oracle at the same residual, 48x64x48 plume, 20 steps.  Bound:

@@ -24,9 +24,11 @@ pointwise bound of another run past that horizon.  So the checks are:
  * steps 100 and 200, past it: the distance to the oracle's 1e-6 run no
    larger than twice the oracle's own 1e-6 vs 1e-10 separation, i.e. these
    runs are as close to the oracle as the oracle is to itself;
- * every step: every solve meets the stop test, and the L2 norms of
-   velocity and density, global quantities that the chaos does not
-   scramble, stay within 5 % of the oracle's 1e-6 run.
+ * every step: every solve meets the stop test; the L2 norms of velocity
+   and density, which drift apart more slowly (the oracle's two runs by up to
+   8 % and 5 % over the 200 steps), deviate from the oracle's 1e-6 run by at
+   most twice the oracle's own largest deviation, and by less than 1e-4 up to
+   step 20.
 
 (Relative L2 over the stored cells.)
 """
@@ -43,7 +45,7 @@ WEIGHTS = os.path.join(ROOT, "cfs_plume_gb300", "weights", "unet_warmstart.bin")
 RES = (128, 192, 128)
 BOUND = 1e-4       # pointwise, inside the predictability horizon (step 20)
 SPREAD = 2.0       # past it: at most this times the oracle's own separation
-NORM_BOUND = 0.05  # per-step L2 norms of velocity and density
+HORIZON = 20       # steps inside the predictability horizon
 
 
 def fixture(tol):
@@ -70,7 +72,8 @@ def test_fixtures_show_the_predictability_horizon():
         assert rel(f6["sample_%s_20" % name], f10["sample_%s_20" % name]) < BOUND, name
         assert rel(f6["sample_%s_200" % name], f10["sample_%s_200" % name]) > 1e-2, name
         dn = np.abs(f6["l2_" + name] - f10["l2_" + name]) / f10["l2_" + name]
-        assert dn.max() < NORM_BOUND, (name, dn.max())
+        assert dn[:HORIZON].max() < BOUND, (name, dn[:HORIZON].max())
+        assert 0.01 < dn.max() < 0.2, (name, dn.max())
 
 
 def run_arm(arm):
@@ -122,10 +125,13 @@ def test_fp32_plume_200_steps_against_fp64_oracle(arm):
             e = rel(out["%s_%d" % (name, s)], f6["sample_%s_%d" % (name, s)])
             report["%s step %d vs 1e-6 (oracle spread %.2f)" % (name, s, own)] = e
             assert e < SPREAD * own, (arm, name, s, e, own)
-        # global norms at every step
+        # global norms at every step: within the bound up to the horizon, and
+        # no further from the oracle than the oracle's own runs are apart
         dn = np.abs(np.array(norms[name]) - f6["l2_" + name]) / f6["l2_" + name]
-        report[name + " max norm deviation"] = float(dn.max())
-        assert dn.max() < NORM_BOUND, (arm, name, dn.max())
+        own = np.abs(f6["l2_" + name] - f10["l2_" + name]) / f10["l2_" + name]
+        report[name + " max norm deviation (oracle spread %.3f)" % own.max()] = float(dn.max())
+        assert dn[:HORIZON].max() < BOUND, (arm, name, dn[:HORIZON].max())
+        assert dn.max() < SPREAD * own.max(), (arm, name, dn.max(), own.max())
     print(arm, {k: ("%.3g" % v) for k, v in report.items()})
 
 
