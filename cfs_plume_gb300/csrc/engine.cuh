@@ -593,7 +593,7 @@ class EngineT : public Engine {
       // border 0, as the reference's p = 0 leaves it
       // (a network trained on solve pairs maps b itself: x0 = g c, c = net(b))
       if (!net_) return fail(PLUME_ERR_STATE, "learned warm start without an attached network");
-      const bool corr = net_->kind() == 1;
+      const bool corr = net_->kind() != 0;  // correction and iterate networks map a residual
       k_zero_border<T><<<gF, 256, 0, s_>>>(g_, pres_);
       PL_CHECK_LAUNCH();
       if (corr) {
@@ -1008,6 +1008,13 @@ class EngineT : public Engine {
     a.gate = gate_closed_ ? (const int*)(wave_ctl_ + 3) : nullptr;  // ctl[3]: never written
     a.gate_spins = gate_spins_;
     return a;
+  }
+
+  int partial_solve(int max_iters, void* xv) override {
+    if (max_iters < 1) return fail(PLUME_ERR_INVALID, "partial solve needs at least one iteration");
+    T* x = (T*)xv;
+    PL_TRY(cudaMemsetAsync(x, 0, (size_t)g_.N * sizeof(T), s_));
+    return solve_device(div_, x, max_iters, true);
   }
 
   int set_wait_gate(int closed, long long polls) override {

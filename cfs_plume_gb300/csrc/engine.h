@@ -55,6 +55,11 @@ class Engine {
   // and starts recording, 0 stops; sweep_times returns the summed device ms
   // and the number of timed launches.
   virtual int profile_sweeps(int on) = 0;
+  // The divergence's solve from x = 0 stopped after at most `max_iters`
+  // iterations, the iterate written into `x` (a device plane of N values of
+  // the engine's field type, border 0); the step's own solver state is
+  // overwritten (training pairs of the preconditioner role).
+  virtual int partial_solve(int max_iters, void* x) = 0;
   // Test hook of the sweeps' bounded waits (plume_set_wait_gate).
   virtual int set_wait_gate(int closed, long long polls) = 0;
   virtual int sweep_times(double* ms, int64_t* launches) = 0;

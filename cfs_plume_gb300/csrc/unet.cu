@@ -905,7 +905,7 @@ int plume_dataset_generate(const plume_dataset_spec* spec, plume_dataset** out) 
   if (!spec || !out) return fail(PLUME_ERR_INVALID, "null argument");
   const plume_dataset_spec& sp = *spec;
   if (sp.plumes < 1 || sp.steps < 1 || sp.skip < 0 || sp.skip >= sp.steps || sp.threads < 1 ||
-      sp.kind < 0 || sp.kind > 1)
+      sp.kind < 0 || sp.kind > 2)
     return fail(PLUME_ERR_INVALID, "plumes, steps, skip, threads or kind out of range");
   for (int k = 0; k < 3; k++)
     if (sp.res[k] < 8 || sp.res[k] % 4 != 0) return fail(PLUME_ERR_INVALID, "grid dimensions must be multiples of 4");
@@ -940,15 +940,16 @@ int plume_dataset_generate(const plume_dataset_spec* spec, plume_dataset** out) 
     double* dpart = nullptr;
     float* scale = nullptr;
     const size_t cells_al = al(cells * 4);
-    if (cudaMalloc((void**)&dpart, kMaxBlocks * 8 + 256 + (sp.kind == 1 ? 2 * cells_al : 0)) != cudaSuccess) {
+    if (cudaMalloc((void**)&dpart, kMaxBlocks * 8 + 256 + (sp.kind != 0 ? 2 * cells_al : 0)) != cudaSuccess) {
       rcs[t] = PLUME_ERR_OOM;
       e = "workspace";
       return;
     }
     scale = (float*)((char*)dpart + kMaxBlocks * 8);
-    // correction pairs: the previous pressure and the residual it leaves
-    float* p_prev = sp.kind == 1 ? (float*)((char*)dpart + kMaxBlocks * 8 + 256) : nullptr;
-    float* r0 = sp.kind == 1 ? (float*)((char*)p_prev + cells_al) : nullptr;
+    // correction pairs: the previous pressure and the residual it leaves;
+    // iterate pairs: the k-th PCG iterate in its place
+    float* p_prev = sp.kind != 0 ? (float*)((char*)dpart + kMaxBlocks * 8 + 256) : nullptr;
+    float* r0 = sp.kind != 0 ? (float*)((char*)p_prev + cells_al) : nullptr;
     for (int i = t; i < sp.plumes && rcs[t] == PLUME_OK; i += T) {
       const uint64_t seed = sp.seed + (uint64_t)i;
       plume_params p;
@@ -1006,7 +1007,15 @@ int plume_dataset_generate(const plume_dataset_spec* spec, plume_dataset** out) 
         }
         if (st < sp.skip) continue;
         const size_t slot = (size_t)i * per + (st - sp.skip);
-        if (sp.kind == 1) {  // (r0, p - p_prev) with r0 = b - A p_prev
+        if (sp.kind == 2) {  // x_k: the same solve from 0, stopped after k iterations
+          const int kits = 2 + (int)(mix(seed * 0x9E3779B97F4A7C15ULL + (uint64_t)st) % 32);
+          rc = eng->partial_solve(kits, p_prev);
+          if (rc != PLUME_OK) {
+            e = eng->last_error();
+            break;
+          }
+        }
+        if (sp.kind != 0) {  // (r, p - x) with r = b - A x, x = p_prev or x_k
           k_closed_box_residual<float><<<nb, kThreads, 0, s>>>(ds.d, b, p_prev, r0);
           k_sumsq_interior<float><<<nb, kThreads, 0, s>>>(ds.d, r0, dpart);
           k_rms_scale<<<1, 256, 0, s>>>(dpart, nb, count, scale);

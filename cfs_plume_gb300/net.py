@@ -12,7 +12,7 @@ from .plume import PlumeError, load_library
 
 _signed = False
 LOSS_MSE, LOSS_ENERGY = 0, 1
-PAIRS_SOLVE, PAIRS_CORRECTION = 0, 1
+PAIRS_SOLVE, PAIRS_CORRECTION, PAIRS_ITERATE = 0, 1, 2
 
 
 class PlumeDatasetSpec(C.Structure):

@@ -1,4 +1,5 @@
-"""Train the learned pressure warm start and measure what it saves.
+"""Train the learned pressure warm start (or the preconditioner stage) and
+measure what it saves.
 
     python -m cfs_plume_gb300.train_warmstart --plumes 100 --steps 200 --epochs 4 \
         --out cfs_plume_gb300/weights/unet_warmstart.bin
@@ -9,14 +10,19 @@
    (FP32 fields, rel-L2 1e-6); every solve after `--skip` steps is kept on the
    GPU as (b / rms(b), p / rms(b)), or with `--pairs correction` (the default)
    as (r0 / rms(r0), (p - p_prev) / rms(r0)), r0 = b - A p_prev, p_prev the
-   previous step's pressure.
+   previous step's pressure, or with `--pairs iterate` as (r_k / rms(r_k),
+   (p - x_k) / rms(r_k)), x_k the iterate after k = 2..33 MIC-PCG iterations of
+   the same solve: residuals met mid-solve mapped to their errors, the
+   preconditioner stage's role.
 2. Training: Adam on the network's own BF16 tensor-core forward and backward
    kernels, cosine step size, the last `--val-plumes` plumes held out; the
    loss is the energy norm e^T A e of the error (the norm CG's error bound
    starts from) unless `--loss mse`.
 3. Evaluation: the same plume stepped with the zero and the learned initial
-   guess at each `--eval-res`, reporting PCG iterations per step, steps/s and
-   the relative L2 difference of the final velocity.
+   guess at each `--eval-res` (with `--pairs iterate`: plain MIC-PCG against
+   flexible CG with the network as the preconditioner), reporting PCG
+   iterations per step, steps/s and the relative L2 difference of the final
+   velocity.
 
 Everything runs on the GPU; the script only sequences the C ABI calls.
 """
@@ -29,18 +35,23 @@ import time
 import numpy as np
 
 from . import _abi
-from .net import LOSS_ENERGY, LOSS_MSE, PAIRS_CORRECTION, PAIRS_SOLVE, PairStore, PlumeNet
+from .net import LOSS_ENERGY, LOSS_MSE, PAIRS_CORRECTION, PAIRS_ITERATE, PAIRS_SOLVE, PairStore, PlumeNet
 from .plume import Plume
 
 
-def evaluate(net, res, steps, seed=0):
+def evaluate(net, res, steps, seed=0, precondition=False):
     """(plain, learned) dicts: iterations per step, ms per step, fallbacks,
-    and the final velocity's relative L2 difference."""
+    and the final velocity's relative L2 difference.  `precondition`: the
+    learned arm uses the network as the flexible-CG preconditioner stage
+    (previous-pressure start) instead of as the warm start."""
     out = {}
     vel = {}
     for name, warm in (("plain", _abi.WARM_ZERO), ("learned", _abi.WARM_LEARNED)):
-        h = Plume(_abi.plume_config(res, seed=seed, warm_start=warm))
-        if warm == _abi.WARM_LEARNED:
+        kw = dict(warm_start=warm)
+        if name == "learned" and precondition:
+            kw = dict(warm_start=_abi.WARM_PREVIOUS, preconditioner=_abi.PRECOND_NET)
+        h = Plume(_abi.plume_config(res, seed=seed, **kw))
+        if name == "learned":
             net.attach(h)
         h.run_timed(0, 3)  # warm-up
         ms, stats = h.run_timed(3, steps)
@@ -70,7 +81,7 @@ def main(argv=None):
     ap.add_argument("--lr-final", type=float, default=5e-5)
     ap.add_argument("--loss", default="energy", choices=["energy", "mse"],
                     help="energy: e^T A e of the error (CG's error norm); mse: squared error")
-    ap.add_argument("--pairs", default="correction", choices=["correction", "solve"],
+    ap.add_argument("--pairs", default="correction", choices=["correction", "solve", "iterate"],
                     help="correction: (b - A p_prev) -> p - p_prev; solve: b -> p")
     ap.add_argument("--seed", type=int, default=1000)
     ap.add_argument("--init", default=None, help="start from these weights")
@@ -89,7 +100,7 @@ def main(argv=None):
         summary = {"weights": a.init, "eval": {}}
         return finish(a, net, summary, t0)
     ds = PairStore(res, a.plumes, a.steps, skip=a.skip, threads=a.threads, seed=a.seed,
-                   kind=PAIRS_CORRECTION if a.pairs == "correction" else PAIRS_SOLVE)
+                   kind={"correction": PAIRS_CORRECTION, "solve": PAIRS_SOLVE, "iterate": PAIRS_ITERATE}[a.pairs])
     print("pairs %d from %d plumes in %.1f s (solution rms %.4g)" % (ds.pairs, a.plumes, ds.seconds,
                                                                       ds.target_rms), flush=True)
     net = PlumeNet(seed=a.seed, path=a.init)
@@ -114,7 +125,7 @@ def main(argv=None):
 def finish(a, net, summary, t0):
     for spec in filter(None, a.eval_res.split(";")):
         r = tuple(int(v) for v in spec.split(","))
-        ev = evaluate(net, r, a.eval_steps)
+        ev = evaluate(net, r, a.eval_steps, precondition=a.pairs == "iterate")
         summary["eval"]["x".join(map(str, r))] = ev
         print("eval %s: plain %.1f it/step %.2f steps/s | learned %.1f it/step %.2f steps/s "
               "(fallbacks %d) | velocity rel L2 %.2e" % (

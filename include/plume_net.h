@@ -82,7 +82,7 @@ typedef struct plume_dataset_spec {
   int32_t device;
   uint64_t seed;
   double tol;       /* rel-L2 stop test of the generating solves               */
-  int32_t kind;     /* PLUME_PAIRS_SOLVE or PLUME_PAIRS_CORRECTION             */
+  int32_t kind;     /* PLUME_PAIRS_SOLVE, _CORRECTION or _ITERATE              */
 } plume_dataset_spec;
 
 /* What a pair (and a network trained on such pairs) maps:
@@ -91,8 +91,14 @@ typedef struct plume_dataset_spec {
    CORRECTION: r0 / rms(r0) -> (p - p_prev) / rms(r0), r0 = b - A p_prev with
                p_prev the previous step's pressure (the step uses
                x0 = p_prev + scaled network output on r0).
+   ITERATE:    r_k / rms(r_k) -> (p - x_k) / rms(r_k), r_k = b - A x_k with x_k
+               the iterate after k MIC-PCG iterations of the same solve from
+               p = 0, k drawn per pair from 2..33: the residuals a solve meets
+               mid-way mapped to their errors, the role of a preconditioner
+               stage (PLUME_PRECOND_NET).  A network of this kind used as a
+               warm start is applied like a correction network.
    The kind is stored in the network file. */
-enum { PLUME_PAIRS_SOLVE = 0, PLUME_PAIRS_CORRECTION = 1 };
+enum { PLUME_PAIRS_SOLVE = 0, PLUME_PAIRS_CORRECTION = 1, PLUME_PAIRS_ITERATE = 2 };
 
 /* Simulates `plumes` closed-box plumes with the batched-plume randomisation
    (box source centre uniform in the middle third of the floor, buoyancy

@@ -155,12 +155,13 @@ def test_gradients_are_deterministic(net):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", [0, 1])
+@pytest.mark.parametrize("kind", [0, 1, 2])
 def test_pairs_are_normalised_solves(kind):
     """Generated pairs: the input has unit rms over interior cells and the
-    target solves A x = input to the stop test -- for solve pairs (b, p) and
-    for correction pairs (r0 = b - A p_prev, p - p_prev), since
-    A (p - p_prev) = b - A p_prev."""
+    target solves A x = input to the stop test -- for solve pairs (b, p), for
+    correction pairs (r0 = b - A p_prev, p - p_prev), since
+    A (p - p_prev) = b - A p_prev, and for iterate pairs (r_k = b - A x_k,
+    p - x_k) with x_k a truncated solve's iterate."""
     from cfs_plume_gb300.net import PairStore
     res = (16, 24, 16)
     ds = PairStore(res, plumes=2, steps=4, skip=1, threads=2, seed=11, kind=kind)
