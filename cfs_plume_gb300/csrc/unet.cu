@@ -1000,7 +1000,8 @@ int plume_dataset_generate(const plume_dataset_spec* spec, plume_dataset** out) 
           break;
         }
         rc = plume_add_source(ph, st);
-        if (rc == PLUME_OK) rc = plume_step(ph, nullptr);
+        plume_step_stats sst;
+        if (rc == PLUME_OK) rc = plume_step(ph, sp.kind == 2 ? &sst : nullptr);
         if (rc != PLUME_OK) {
           e = plume_last_error(ph);
           break;
@@ -1008,7 +1009,10 @@ int plume_dataset_generate(const plume_dataset_spec* spec, plume_dataset** out) 
         if (st < sp.skip) continue;
         const size_t slot = (size_t)i * per + (st - sp.skip);
         if (sp.kind == 2) {  // x_k: the same solve from 0, stopped after k iterations
-          const int kits = 2 + (int)(mix(seed * 0x9E3779B97F4A7C15ULL + (uint64_t)st) % 32);
+          // k below half the solve's own count, so that x_k is not yet the
+          // solution (whose residual the target p - x_k would not solve)
+          const int kmax = std::max(1, std::min(32, sst.iterations / 2 - 1));
+          const int kits = 1 + (int)(mix(seed * 0x9E3779B97F4A7C15ULL + (uint64_t)st) % (uint64_t)kmax);
           rc = eng->partial_solve(kits, p_prev);
           if (rc != PLUME_OK) {
             e = eng->last_error();

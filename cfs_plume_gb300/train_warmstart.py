@@ -11,8 +11,9 @@ measure what it saves.
    GPU as (b / rms(b), p / rms(b)), or with `--pairs correction` (the default)
    as (r0 / rms(r0), (p - p_prev) / rms(r0)), r0 = b - A p_prev, p_prev the
    previous step's pressure, or with `--pairs iterate` as (r_k / rms(r_k),
-   (p - x_k) / rms(r_k)), x_k the iterate after k = 2..33 MIC-PCG iterations of
-   the same solve: residuals met mid-solve mapped to their errors, the
+   (p - x_k) / rms(r_k)), x_k the iterate after k (1 to 32, below half the
+   solve's count) MIC-PCG iterations of the same solve: residuals met
+   mid-solve mapped to their errors, the
    preconditioner stage's role.
 2. Training: Adam on the network's own BF16 tensor-core forward and backward
    kernels, cosine step size, the last `--val-plumes` plumes held out; the

@@ -93,7 +93,8 @@ typedef struct plume_dataset_spec {
                x0 = p_prev + scaled network output on r0).
    ITERATE:    r_k / rms(r_k) -> (p - x_k) / rms(r_k), r_k = b - A x_k with x_k
                the iterate after k MIC-PCG iterations of the same solve from
-               p = 0, k drawn per pair from 2..33: the residuals a solve meets
+               p = 0, k drawn per pair from 1 .. min(32, half the solve's
+               iterations - 1): the residuals a solve meets
                mid-way mapped to their errors, the role of a preconditioner
                stage (PLUME_PRECOND_NET).  A network of this kind used as a
                warm start is applied like a correction network.
