@@ -442,26 +442,49 @@ def measure_batched(steps, warmup, seed=0, n=64):
     """The batched-plume configuration: `n` randomised plumes of uneven grids
     (plume_batch_params: 32^3 .. 96x128x96, source position, buoyancy and
     vorticity drawn per instance), FP32 fields, MIC(0)-PCG rel-L2 1e-6,
-    stepped together (plume_batch_run).  Aggregate interior cell-steps/s."""
+    stepped together (plume_batch_run).  Aggregate interior cell-steps/s of
+    the fused engine (one launch per stage over all plumes, each step one
+    CUDA graph launch, tile shapes from the autotuner), with the streams
+    engine (one handle and stream per plume) on the same plumes beside it."""
     import numpy as np
     from cfs_plume_gb300.batch import PlumeBatch, batch_params
     params = [batch_params(seed, i) for i in range(n)]
     cells = np.array([(p.res[0] - 2) * (p.res[1] - 2) * (p.res[2] - 2) for p in params], dtype=np.float64)
-    b = PlumeBatch(params)
-    b.run(0, warmup, stats=False)
-    secs, stats = b.run(warmup, steps, stats=True)
-    b.close()
+    arms = {}
+    for engine in ("fused", "streams"):
+        t0 = time.time()
+        b = PlumeBatch(params, engine=engine)
+        create_s = time.time() - t0
+        b.run(0, warmup, stats=False)
+        secs, stats = b.run(warmup, steps, stats=True)
+        tuning = b.tuning() if engine == "fused" else None
+        b.close()
+        arm = {"value": cells.sum() * steps / secs, "seconds": secs, "create_seconds": create_s,
+               "instance_steps_per_s": n * steps / secs,
+               "pcg_iters_per_step_mean": float(np.mean([[s.iterations for s in st] for st in stats])),
+               "pcg_iters_per_step_max": int(np.max([[s.iterations for s in st] for st in stats])),
+               "all_converged": all(s.converged for st in stats for s in st)}
+        if engine == "fused":
+            # one graph launch per step; the statistics row carries the
+            # kernels its step launched and the device time of the call
+            arm["gpu_launches_per_step"] = float(np.mean([s.launches for s in stats[0]]))
+            arm["device_seconds"] = sum(s.ms_total for s in stats[0]) / 1e3
+            arm["tuning"] = tuning
+        arms[engine] = arm
     grids = {}
     for p in params:
         k = "x".join(str(v) for v in p.res)
         grids[k] = grids.get(k, 0) + 1
-    return {"value": cells.sum() * steps / secs, "unit": "interior cell-steps/s", "instances": n,
-            "steps": steps, "warmup": warmup, "seconds": secs, "instance_steps_per_s": n * steps / secs,
-            "pcg_iters_per_step_mean": float(np.mean([[s.iterations for s in st] for st in stats])),
-            "all_converged": all(s.converged for st in stats for s in st), "grids": grids,
+    f = arms["fused"]
+    return {"value": f["value"], "unit": "interior cell-steps/s", "engine": "fused", "instances": n,
+            "steps": steps, "warmup": warmup, "seconds": f["seconds"],
+            "instance_steps_per_s": f["instance_steps_per_s"],
+            "pcg_iters_per_step_mean": f["pcg_iters_per_step_mean"], "all_converged": f["all_converged"],
+            "fused_over_streams": f["value"] / arms["streams"]["value"], "arms": arms, "grids": grids,
             "interior_cells_total": float(cells.sum()),
             "workload": "%d randomised closed-box plumes of the batched configuration, FP32 fields, "
-                        "MIC(0)-PCG rel-L2 1e-6, one handle and CUDA stream per instance" % n}
+                        "MIC(0)-PCG rel-L2 1e-6, advanced in lockstep: one launch per stage over all "
+                        "plumes, each step one CUDA graph launch" % n}
 
 
 LARGE_RES = (256, 384, 256)

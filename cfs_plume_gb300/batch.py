@@ -1,8 +1,31 @@
-"""Python binding of many independent plumes on one GPU (include/plume_batch.h)."""
+"""Python binding of many independent plumes on one GPU (include/plume_batch.h).
+
+Two engines: "fused" (one launch per stage over every plume, each step one
+CUDA graph launch, tile shapes from the autotuner) and "streams" (one
+plume_handle and CUDA stream per plume, stepped from host threads)."""
 import ctypes as C
+import json
+
+import numpy as np
 
 from . import _abi
 from .plume import PlumeError, PlumeStepStats, load_library
+
+ENGINE_FUSED = 0
+ENGINE_STREAMS = 1
+ENGINES = {"fused": ENGINE_FUSED, "streams": ENGINE_STREAMS}
+
+
+class PlumeBatchOptions(C.Structure):
+    _fields_ = [
+        ("engine", C.c_int32),
+        ("graph", C.c_int32),
+        ("tune", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("tune_cache", C.c_char_p),
+        ("reserved", C.c_int32 * 8),
+    ]
+
 
 _signed = False
 
@@ -14,10 +37,14 @@ def _lib():
         V, P = C.c_void_p, C.POINTER
         sig = {
             "plume_batch_params": (C.c_int, [C.c_uint64, C.c_int32, P(_abi.PlumeParams)]),
+            "plume_batch_default_options": (None, [P(PlumeBatchOptions)]),
             "plume_batch_create": (C.c_int, [P(_abi.PlumeParams), C.c_int32, P(V)]),
+            "plume_batch_create_ex": (C.c_int, [P(_abi.PlumeParams), C.c_int32, P(PlumeBatchOptions), P(V)]),
             "plume_batch_destroy": (None, [V]),
             "plume_batch_size": (C.c_int, [V, P(C.c_int32)]),
             "plume_batch_handle": (C.c_int, [V, C.c_int32, P(V)]),
+            "plume_batch_download": (C.c_int, [V, C.c_int32, C.c_int32, V, C.c_size_t]),
+            "plume_batch_tuning": (C.c_int, [V, C.c_char_p, C.c_size_t, P(C.c_size_t)]),
             "plume_batch_run": (C.c_int, [V, C.c_int32, C.c_int32, C.c_int32, P(C.c_double), V]),
         }
         for name, (res, args) in sig.items():
@@ -40,13 +67,29 @@ def batch_params(seed, index):
     return p
 
 
+def default_options():
+    o = PlumeBatchOptions()
+    _lib().plume_batch_default_options(C.byref(o))
+    return o
+
+
 class PlumeBatch:
-    def __init__(self, params):
+    """n plumes advanced together.  engine: "fused" (default) or "streams";
+    graph / tune / tune_cache: the fused engine's options."""
+
+    def __init__(self, params, engine="fused", graph=True, tune=True, tune_cache=None):
         self.lib = _lib()
         arr = (_abi.PlumeParams * len(params))(*params)
+        o = default_options()
+        o.engine = ENGINES[engine]
+        o.graph = 1 if graph else 0
+        o.tune = 1 if tune else 0
+        self._cache = tune_cache.encode() if tune_cache else None
+        o.tune_cache = self._cache
         self.h = C.c_void_p()
-        _check(self.lib.plume_batch_create(arr, len(params), C.byref(self.h)))
+        _check(self.lib.plume_batch_create_ex(arr, len(params), C.byref(o), C.byref(self.h)))
         self.n = len(params)
+        self.engine = engine
         self.params = list(params)
 
     def run(self, first_step, steps, threads=0, stats=True):
@@ -62,6 +105,23 @@ class PlumeBatch:
         h = C.c_void_p()
         _check(self.lib.plume_batch_handle(self.h, i, C.byref(h)))
         return h
+
+    def field(self, i, name):
+        """Instance i's field as FP64 (vector fields interleaved per cell)."""
+        p = self.params[i]
+        N = p.res[0] * p.res[1] * p.res[2]
+        vec = name in _abi.VECTOR_FIELDS
+        a = np.empty(3 * N if vec else N, dtype=np.float64)
+        _check(self.lib.plume_batch_download(self.h, i, _abi.FIELD_ID[name], a.ctypes.data, a.size))
+        return a
+
+    def tuning(self):
+        """The fused engine's tile shapes (and how they were chosen) as a dict."""
+        need = C.c_size_t()
+        _check(self.lib.plume_batch_tuning(self.h, None, 0, C.byref(need)))
+        buf = C.create_string_buffer(need.value + 1)
+        _check(self.lib.plume_batch_tuning(self.h, buf, len(buf), C.byref(need)))
+        return json.loads(buf.value.decode())
 
     def close(self):
         if self.h:

@@ -83,6 +83,8 @@ def build(verbose=False, ptxas_info=False):
         ("svd.cu", [nvcc] + common_nv),
         ("reduced.cu", [nvcc] + common_nv),
         ("products.cu", [nvcc] + common_nv),
+        ("batched_f32.cu", [nvcc] + common_nv),
+        ("batched_f64.cu", [nvcc] + common_nv + ["-fmad=false"]),
         ("plume_api.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-I" + os.path.join(cuda, "include")]),
         ("snapshot.cpp", ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread"] + zc),
         ("state_read.cpp", ["g++", "-O2", "-std=c++17", "-fPIC"] + zc),

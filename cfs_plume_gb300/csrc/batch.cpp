@@ -1,10 +1,13 @@
 // batch.cpp -- many independent plumes on one GPU (include/plume_batch.h).
 //
-// Host C++ over the C ABI: each instance is a plume_handle with its own CUDA
-// stream; a pool of host threads steps them concurrently.
+// Host C++ over the C ABI.  The fused engine (batched.cuh) advances every
+// plume in lockstep, one launch per stage; the streams engine keeps each
+// instance as a plume_handle with its own CUDA stream, stepped concurrently
+// from a pool of host threads.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstring>
 #include <new>
 #include <string>
 #include <thread>
@@ -13,10 +16,14 @@
 #include "../../include/plume.h"
 #include "../../include/plume_batch.h"
 #include "../../include/plume_solver.h"
+#include "batched.h"
 #include "engine.h"
 
 struct plume_batch {
-  std::vector<plume_handle*> h;
+  int engine = PLUME_BATCH_STREAMS;
+  std::vector<plume_handle*> h;         // streams engine
+  plume::BatchEngine* fused = nullptr;  // fused engine
+  int n = 0;
 };
 
 namespace {
@@ -69,10 +76,43 @@ int plume_batch_params(uint64_t seed, int32_t index, plume_params* p) {
   return PLUME_OK;
 }
 
-int plume_batch_create(const plume_params* params, int32_t n, plume_batch** out) {
+void plume_batch_default_options(plume_batch_options* o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->engine = PLUME_BATCH_FUSED;
+  o->graph = 1;
+  o->tune = 1;
+  o->tune_cache = nullptr;
+}
+
+int plume_batch_create_ex(const plume_params* params, int32_t n, const plume_batch_options* opt,
+                          plume_batch** out) {
   if (!params || !out || n < 1) return fail(PLUME_ERR_INVALID, "bad argument");
+  plume_batch_options o;
+  plume_batch_default_options(&o);
+  if (opt) o = *opt;
+  if (o.engine != PLUME_BATCH_FUSED && o.engine != PLUME_BATCH_STREAMS)
+    return fail(PLUME_ERR_INVALID, "unknown batch engine");
   plume_batch* b = new (std::nothrow) plume_batch();
   if (!b) return fail(PLUME_ERR_OOM, "out of host memory");
+  b->engine = o.engine;
+  b->n = n;
+  if (o.engine == PLUME_BATCH_FUSED) {
+    const bool fp64 = params[0].precision == PLUME_PREC_FP64;
+    if (!fp64 && params[0].precision != PLUME_PREC_FP32) {
+      delete b;
+      return fail(PLUME_ERR_INVALID, "unknown precision");
+    }
+    b->fused = fp64 ? plume::make_batch_engine_f64() : plume::make_batch_engine_f32();
+    const int rc = b->fused ? b->fused->init(params, n, o) : (int)PLUME_ERR_OOM;
+    if (rc != PLUME_OK) {
+      const std::string why = b->fused ? b->fused->last_error() : std::string("out of host memory");
+      plume_batch_destroy(b);
+      return fail(rc, why);
+    }
+    *out = b;
+    return PLUME_OK;
+  }
   for (int i = 0; i < n; i++) {
     plume_handle* h = nullptr;
     const int rc = plume_create(&params[i], &h);
@@ -91,27 +131,61 @@ int plume_batch_create(const plume_params* params, int32_t n, plume_batch** out)
   return PLUME_OK;
 }
 
+int plume_batch_create(const plume_params* params, int32_t n, plume_batch** out) {
+  return plume_batch_create_ex(params, n, nullptr, out);
+}
+
 void plume_batch_destroy(plume_batch* b) {
   if (!b) return;
   for (plume_handle* h : b->h) plume_destroy(h);
+  delete b->fused;
   delete b;
 }
 
 int plume_batch_size(plume_batch* b, int32_t* n) {
   if (!b || !n) return fail(PLUME_ERR_INVALID, "bad argument");
-  *n = (int32_t)b->h.size();
+  *n = (int32_t)b->n;
   return PLUME_OK;
 }
 
 int plume_batch_handle(plume_batch* b, int32_t i, plume_handle** h) {
-  if (!b || !h || i < 0 || i >= (int32_t)b->h.size()) return fail(PLUME_ERR_INVALID, "bad instance");
+  if (!b || !h) return fail(PLUME_ERR_INVALID, "bad argument");
+  if (b->engine == PLUME_BATCH_FUSED)
+    return fail(PLUME_ERR_STATE, "a fused batch has no per-plume handles (plume_batch_download)");
+  if (i < 0 || i >= (int32_t)b->h.size()) return fail(PLUME_ERR_INVALID, "bad instance");
   *h = b->h[i];
+  return PLUME_OK;
+}
+
+int plume_batch_download(plume_batch* b, int32_t i, int32_t field, double* dst, size_t n) {
+  if (!b || i < 0 || i >= b->n) return fail(PLUME_ERR_INVALID, "bad instance");
+  if (b->engine == PLUME_BATCH_FUSED) {
+    const int rc = b->fused->download(i, field, dst, n);
+    return rc == PLUME_OK ? rc : fail(rc, b->fused->last_error());
+  }
+  const int rc = plume_download(b->h[i], field, dst, n);
+  return rc == PLUME_OK ? rc : fail(rc, plume_last_error(b->h[i]));
+}
+
+int plume_batch_tuning(plume_batch* b, char* json, size_t cap, size_t* len) {
+  if (!b) return fail(PLUME_ERR_INVALID, "bad argument");
+  const std::string s = b->engine == PLUME_BATCH_FUSED ? b->fused->tuning_json() : std::string("{}");
+  if (len) *len = s.size();
+  if (json && cap > 0) {
+    const size_t k = std::min(cap - 1, s.size());
+    memcpy(json, s.data(), k);
+    json[k] = 0;
+  }
   return PLUME_OK;
 }
 
 int plume_batch_run(plume_batch* b, int32_t first_step, int32_t steps, int32_t threads, double* seconds,
                     plume_step_stats* stats) {
   if (!b || steps < 0 || threads < 0) return fail(PLUME_ERR_INVALID, "bad argument");
+  if (b->engine == PLUME_BATCH_FUSED) {
+    const int rc = b->fused->run(first_step, steps, seconds, stats);
+    return rc == PLUME_OK ? rc : fail(rc, b->fused->last_error());
+  }
   const int n = (int)b->h.size();
   const int T = threads == 0 ? n : std::min(threads, n);
   std::vector<int> rcs(n, PLUME_OK);

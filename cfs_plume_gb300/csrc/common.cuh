@@ -8,6 +8,18 @@ namespace plume {
 #define PL_GRID_STRIDE(i, n) \
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += blockDim.x * gridDim.x)
 
+// The block a kernel body runs as: its index among the blocks that share one
+// plume's work, and their count.  A launch for one plume passes
+// {blockIdx.x, gridDim.x} (hw_blk); a batched launch over many plumes
+// (batched.cu) gives each plume a contiguous range of the grid, so the same
+// body serves both and visits the same elements per block for the same count.
+struct Blk {
+  int id, n;
+};
+__device__ inline Blk hw_blk() { return Blk{(int)blockIdx.x, (int)gridDim.x}; }
+#define PL_BLK_STRIDE(i, count, blk) \
+  for (int i = (blk).id * (int)blockDim.x + (int)threadIdx.x; i < (count); i += (int)blockDim.x * (blk).n)
+
 // Grid geometry.  Index = x + y*X + z*X*Y (x fastest), the reference layout
 // (src/geometry/FIELD_3D.h:54-57).  `wall` holds the six BC flags in the
 // reference order front(z=0), back(z=Z-1), left(x=0), right(x=X-1),

@@ -65,31 +65,38 @@ __device__ inline double mult_a_skew_d(const Grid& g, const Skew& k, const T* v,
 
 // natural full grid -> skewed interior (padding zero)
 template <typename S, typename T>
-__global__ void k_to_skew(Grid g, Skew k, const S* nat, T* sk) {
-  PL_GRID_STRIDE(e, (int)k.total) {
+__device__ __forceinline__ void to_skew_body(Blk blk_, Grid g, Skew k, const S* nat, T* sk) {
+  PL_BLK_STRIDE(e, (int)k.total, blk_) {
     int ix, iy, iz;
     T v = T(0);
     if (skew_cell(k, e, ix, iy, iz)) v = (T)nat[(ix + 1) + (iy + 1) * g.X + (iz + 1) * g.slab];
     sk[e] = v;
   }
 }
+template <typename S, typename T>
+__global__ void k_to_skew(Grid g, Skew k, const S* nat, T* sk) {
+  to_skew_body<S, T>(hw_blk(), g, k, nat, sk);
+}
 
 // skewed interior -> natural full grid (interior cells only)
 template <typename T>
-__global__ void k_from_skew(Grid g, Skew k, const T* sk, T* nat) {
-  PL_GRID_STRIDE(e, (int)k.total) {
+__device__ __forceinline__ void from_skew_body(Blk blk_, Grid g, Skew k, const T* sk, T* nat) {
+  PL_BLK_STRIDE(e, (int)k.total, blk_) {
     int ix, iy, iz;
     if (skew_cell(k, e, ix, iy, iz)) nat[(ix + 1) + (iy + 1) * g.X + (iz + 1) * g.slab] = sk[e];
   }
 }
+template <typename T>
+__global__ void k_from_skew(Grid g, Skew k, const T* sk, T* nat) {
+  from_skew_body<T>(hw_blk(), g, k, sk, nat);
+}
 
 // set-up part 1: r = b - A x, b.b
 template <typename T>
-__global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState* st, double* part,
-                           double tol, int max_iters, int criterion, int x_zero) {
+__device__ __forceinline__ void cgs_init_body(Blk blk_, Grid g, Skew k, const T* b, const T* x, T* r, CgState* st, double* part, double tol, int max_iters, int criterion, int x_zero) {
   __shared__ double sh[32];
   DotAcc<T> bb;
-  PL_GRID_STRIDE(e, (int)k.total) {
+  PL_BLK_STRIDE(e, (int)k.total, blk_) {
     int ix, iy, iz;
     T v = T(0);
     if (skew_cell(k, e, ix, iy, iz)) {
@@ -109,9 +116,9 @@ __global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState
     r[e] = v;
   }
   const double s = bb.block(sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
-  if (arrive_last(&st->ticket[0])) {
-    const double tot = sum_partials(part, sh);
+  if (threadIdx.x == 0) part[blk_.id] = s;
+  if (arrive_last(&st->ticket[0], blk_.n)) {
+    const double tot = sum_partials(part, sh, blk_.n);
     if (threadIdx.x == 0) {
       st->bb = tot;
       st->tol = tol;
@@ -126,25 +133,30 @@ __global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState
     }
   }
 }
+template <typename T>
+__global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState* st, double* part,
+                           double tol, int max_iters, int criterion, int x_zero) {
+  cgs_init_body<T>(hw_blk(), g, k, b, x, r, st, part, tol, max_iters, criterion, x_zero);
+}
 
 // set-up part 2: d = z, deltaNew = r.z, loop entry test
 template <typename T>
-__global__ void k_cgs_init2(Skew k, const T* r, const T* z, T* d, CgState* st, double* part) {
+__device__ __forceinline__ void cgs_init2_body(Blk blk_, Skew k, const T* r, const T* z, T* d, CgState* st, double* part) {
   __shared__ double sh[32];
   DotAcc<T> rz, rr;
-  PL_GRID_STRIDE(e, (int)k.total) {
+  PL_BLK_STRIDE(e, (int)k.total, blk_) {
     const T zi = z[e], ri = r[e];
     if (d) d[e] = zi;
     rz.prod(ri, zi);
     rr.prod(ri, ri);
   }
   const double s1 = rz.block(sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s1;
+  if (threadIdx.x == 0) part[blk_.id] = s1;
   const double s2 = rr.block(sh);
-  if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
-  if (arrive_last(&st->ticket[0])) {
-    const double trz = sum_partials(part, sh);
-    const double trr = sum_partials(part + kRedBlocks, sh);
+  if (threadIdx.x == 0) part[blk_.n + blk_.id] = s2;
+  if (arrive_last(&st->ticket[0], blk_.n)) {
+    const double trz = sum_partials(part, sh, blk_.n);
+    const double trr = sum_partials(part + blk_.n, sh, blk_.n);
     if (threadIdx.x == 0) {
       st->deltaNew = trz;
       st->rr = trr;
@@ -163,6 +175,10 @@ __global__ void k_cgs_init2(Skew k, const T* r, const T* z, T* d, CgState* st, d
       st->ticket[0] = 0;
     }
   }
+}
+template <typename T>
+__global__ void k_cgs_init2(Skew k, const T* r, const T* z, T* d, CgState* st, double* part) {
+  cgs_init2_body<T>(hw_blk(), k, r, z, d, st, part);
 }
 
 // iteration part 1: q = A d, alpha = deltaNew / d.q
@@ -344,6 +360,69 @@ __global__ void __launch_bounds__(SkewRows<C>::THREADS) k_cgs_spmv_dir(Grid g, S
   }
 }
 
+// The same fused direction update + SpMV with the row width W = 32*C read at
+// run time (the batched launch covers plumes of several widths in one grid):
+// blockDim.x / W rows per block pass (blockDim.x >= W), threads past them
+// idle.  Per cell the expression of k_cgs_spmv_dir.
+template <typename T>
+__device__ __forceinline__ void cgs_spmv_dir_rows_body(Blk blk_, Grid g, Skew k, const T* z, const T* d_old,
+                                                       T* d_new, T* q, CgState* st, double* part) {
+  if (st->done) return;
+  __shared__ double sh[32];
+  const int W = k.W, C = k.C;
+  const int rpb = (int)blockDim.x / W;
+  const int lr = (int)threadIdx.x / W, ix = (int)threadIdx.x - lr * W;
+  const int lb = ix / C, jb = ix - lb * C;
+  const T beta = (T)st->beta;
+  const int plane = (int)k.plane;
+  const int nrows = k.nz * k.R;
+  DotAcc<T> dq;
+  if (lr < rpb) {
+    for (int row = blk_.id * rpb + lr; row < nrows; row += blk_.n * rpb) {
+      const int iz = row / k.R;
+      const int sr = row - iz * k.R;
+      const int iy = sr - lb;
+      const int e = row * W + ix;
+      T dn = T(0), qq = T(0);
+      if (ix < k.nx && iy >= 0 && iy < k.ny) {
+        const int x = ix + 1, y = iy + 1, zz = iz + 1;
+        dn = d_old[e] * beta + z[e];
+        const T vxm = ix > 0 ? (jb > 0 ? d_old[e - 1] * beta + z[e - 1]
+                                       : d_old[e - W - 1] * beta + z[e - W - 1])
+                             : T(0);
+        const T vxp = ix + 1 < k.nx ? (jb < C - 1 ? d_old[e + 1] * beta + z[e + 1]
+                                                  : d_old[e + W + 1] * beta + z[e + W + 1])
+                                    : T(0);
+        const T vym = iy > 0 ? d_old[e - W] * beta + z[e - W] : T(0);
+        const T vyp = iy + 1 < k.ny ? d_old[e + W] * beta + z[e + W] : T(0);
+        const T vzm = iz > 0 ? d_old[e - plane] * beta + z[e - plane] : T(0);
+        const T vzp = iz + 1 < k.nz ? d_old[e + plane] * beta + z[e + plane] : T(0);
+        qq = adiag<T>(g, x, y, zz) * dn + vxm * coef<T>(wall_xm(g, x)) + vxp * coef<T>(wall_xp(g, x)) +
+             vym * coef<T>(wall_ym(g, y)) + vyp * coef<T>(wall_yp(g, y)) +
+             vzm * coef<T>(wall_zm(g, zz)) + vzp * coef<T>(wall_zp(g, zz));
+        dq.prod(dn, qq);
+      }
+      d_new[e] = dn;
+      q[e] = qq;
+    }
+  }
+  const double sblk = dq.block(sh);
+  if (threadIdx.x == 0) part[blk_.id] = sblk;
+  if (arrive_last(&st->ticket[0], blk_.n)) {
+    const double t = sum_partials(part, sh, blk_.n);
+    if (threadIdx.x == 0) {
+      st->dq = t;
+      if (fabs(t) > 0.0) {
+        st->alpha = st->deltaNew / t;
+      } else {  // "PCG alpha broke down! Bailing." (FLUID_3D_MIC.cpp:962-969)
+        st->done = 1;
+        st->broke = 1;
+      }
+      st->ticket[0] = 0;
+    }
+  }
+}
+
 // 16-byte vector type of T
 template <typename T>
 struct Vec16;
@@ -476,7 +555,7 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_spmv_dir_v(Grid g, Skew k, 
 
 // Iteration part 2, vectorised: x += alpha d, r -= alpha q, signed max(r), r.r
 template <typename T>
-__global__ void k_cgs_axpy_v(Skew k, const T* d, const T* q, T* x, T* r, CgState* st, double* part) {
+__device__ __forceinline__ void cgs_axpy_v_body(Blk blk_, Skew k, const T* d, const T* q, T* x, T* r, CgState* st, double* part) {
   if (st->done) return;
   typedef typename Vec16<T>::type V;
   constexpr int NV = Vec16<T>::n;
@@ -489,7 +568,7 @@ __global__ void k_cgs_axpy_v(Skew k, const T* d, const T* q, T* x, T* r, CgState
   const V* qv = reinterpret_cast<const V*>(q);
   V* xv = reinterpret_cast<V*>(x);
   V* rv = reinterpret_cast<V*>(r);
-  PL_GRID_STRIDE(i, nvec) {
+  PL_BLK_STRIDE(i, nvec, blk_) {
     const V dd = dv[i], qq = qv[i];
     V xx = xv[i], ri = rv[i];
 #pragma unroll
@@ -504,12 +583,12 @@ __global__ void k_cgs_axpy_v(Skew k, const T* d, const T* q, T* x, T* r, CgState
     rv[i] = ri;
   }
   const double s1 = block_max_w(mx, sh, -1.0e308);
-  if (threadIdx.x == 0) part[blockIdx.x] = s1;
+  if (threadIdx.x == 0) part[blk_.id] = s1;
   const double s2 = rr.block(sh);
-  if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
-  if (arrive_last(&st->ticket[0])) {
-    const double tm = max_partials(part, sh);
-    const double trr = sum_partials(part + kRedBlocks, sh);
+  if (threadIdx.x == 0) part[blk_.n + blk_.id] = s2;
+  if (arrive_last(&st->ticket[0], blk_.n)) {
+    const double tm = max_partials(part, sh, blk_.n);
+    const double trr = sum_partials(part + blk_.n, sh, blk_.n);
     if (threadIdx.x == 0) {
       st->oldMaxR = st->maxR;
       st->maxR = tm > 0.0 ? tm : 0.0;  // FIELD_3D::max starts at a border cell (0)
@@ -523,10 +602,14 @@ __global__ void k_cgs_axpy_v(Skew k, const T* d, const T* q, T* x, T* r, CgState
     }
   }
 }
+template <typename T>
+__global__ void k_cgs_axpy_v(Skew k, const T* d, const T* q, T* x, T* r, CgState* st, double* part) {
+  cgs_axpy_v_body<T>(hw_blk(), k, d, q, x, r, st, part);
+}
 
 // Iteration part 3, vectorised: deltaNew = r.z, beta, exit tests
 template <typename T>
-__global__ void k_cgs_rz_v(Skew k, const T* r, const T* z, CgState* st, double* part) {
+__device__ __forceinline__ void cgs_rz_v_body(Blk blk_, Skew k, const T* r, const T* z, CgState* st, double* part) {
   if (st->done) return;
   typedef typename Vec16<T>::type V;
   constexpr int NV = Vec16<T>::n;
@@ -535,15 +618,15 @@ __global__ void k_cgs_rz_v(Skew k, const T* r, const T* z, CgState* st, double* 
   const int nvec = (int)(k.total / NV);
   const V* rv = reinterpret_cast<const V*>(r);
   const V* zv = reinterpret_cast<const V*>(z);
-  PL_GRID_STRIDE(i, nvec) {
+  PL_BLK_STRIDE(i, nvec, blk_) {
     const V a = rv[i], b = zv[i];
 #pragma unroll
     for (int c = 0; c < NV; c++) rz.prod(vget<T>(a, c), vget<T>(b, c));
   }
   const double s = rz.block(sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
-  if (arrive_last(&st->ticket[0])) {
-    const double t = sum_partials(part, sh);
+  if (threadIdx.x == 0) part[blk_.id] = s;
+  if (arrive_last(&st->ticket[0], blk_.n)) {
+    const double t = sum_partials(part, sh, blk_.n);
     if (threadIdx.x == 0) {
       st->deltaOld = st->deltaNew;
       st->deltaNew = t;
@@ -559,6 +642,10 @@ __global__ void k_cgs_rz_v(Skew k, const T* r, const T* z, CgState* st, double* 
       st->ticket[0] = 0;
     }
   }
+}
+template <typename T>
+__global__ void k_cgs_rz_v(Skew k, const T* r, const T* z, CgState* st, double* part) {
+  cgs_rz_v_body<T>(hw_blk(), k, r, z, st, part);
 }
 
 // Flexible CG, iteration part 3 (Notay, "Flexible conjugate gradients",

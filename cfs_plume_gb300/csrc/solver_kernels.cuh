@@ -61,32 +61,41 @@ __device__ inline T mult_a_cell(const Grid& g, const T* xf, int i, int x, int y,
 }
 
 // ------------------------------------------------- last-block reductions
-__device__ inline bool arrive_last(unsigned int* ticket) {
+// True in the last of `nblk` blocks to arrive (the blocks sharing one
+// plume's reduction: the whole grid for a single-plume launch).
+__device__ inline bool arrive_last(unsigned int* ticket, int nblk) {
   __shared__ bool last;
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
     const unsigned int t = atomicAdd(ticket, 1u);
-    last = (t == gridDim.x - 1);
+    last = (t == (unsigned)nblk - 1u);
   }
   __syncthreads();
   if (last) __threadfence();
   return last;
 }
+__device__ inline bool arrive_last(unsigned int* ticket) { return arrive_last(ticket, (int)gridDim.x); }
 
-// Sum the gridDim.x partials in a fixed order (valid in thread 0).
-__device__ inline double sum_partials(const double* part, double* sh) {
+// Sum the first `nblk` partials in a fixed order (valid in thread 0).
+__device__ inline double sum_partials(const double* part, double* sh, int nblk) {
   double s = 0.0;
-  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) s += __ldcg(part + k);
+  for (int k = threadIdx.x; k < nblk; k += blockDim.x) s += __ldcg(part + k);
   return block_sum(s, sh);
 }
-__device__ inline double max_partials(const double* part, double* sh) {
+__device__ inline double sum_partials(const double* part, double* sh) {
+  return sum_partials(part, sh, (int)gridDim.x);
+}
+__device__ inline double max_partials(const double* part, double* sh, int nblk) {
   double s = -1.0e308;
-  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+  for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
     const double v = __ldcg(part + k);
     s = v > s ? v : s;
   }
   return block_max(s, sh, -1.0e308);
+}
+__device__ inline double max_partials(const double* part, double* sh) {
+  return max_partials(part, sh, (int)gridDim.x);
 }
 
 // ------------------------------------------------- initial guess from two

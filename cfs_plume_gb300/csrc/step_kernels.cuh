@@ -42,10 +42,9 @@ struct StepConsts {
 // ---------------------------------------------------------------- sources
 // Box source: density = heat = 1 + noise*(2u-1) on [lo, hi).
 template <typename T>
-__global__ void k_source_box(T* dens, T* heat, Grid g, int x0, int y0, int z0, int bx, int by,
-                             int bz, uint64_t seed, int step, double noise) {
+__device__ __forceinline__ void source_box_body(Blk blk_, T* dens, T* heat, Grid g, int x0, int y0, int z0, int bx, int by, int bz, uint64_t seed, int step, double noise) {
   const int n = bx * by * bz;
-  PL_GRID_STRIDE(i, n) {
+  PL_BLK_STRIDE(i, n, blk_) {
     const int x = x0 + i % bx;
     const int t = i / bx;
     const int y = y0 + t % by;
@@ -55,6 +54,11 @@ __global__ void k_source_box(T* dens, T* heat, Grid g, int x0, int y0, int z0, i
     dens[c] = v;
     heat[c] = v;
   }
+}
+template <typename T>
+__global__ void k_source_box(T* dens, T* heat, Grid g, int x0, int y0, int z0, int bx, int by,
+                             int bz, uint64_t seed, int step, double noise) {
+  source_box_body<T>(hw_blk(), dens, heat, g, x0, y0, z0, bx, by, bz, seed, step, noise);
 }
 
 // Box source with host-supplied values (x fastest over the box).
@@ -89,9 +93,8 @@ __global__ void k_source_list(T* dens, T* heat, const int* cells, int n) {
 // setZeroBorder, addBuoyancy (force.y = beta*heat), velocity += force*dt,
 // prevorticity = velocity.
 template <typename T>
-__global__ void k_forces(Grid g, V3<T> vel, T* dens, const T* heat, V3<T> prevort,
-                         StepConsts<T> c, int cache) {
-  PL_GRID_STRIDE(i, g.N) {
+__device__ __forceinline__ void forces_body(Blk blk_, Grid g, V3<T> vel, T* dens, const T* heat, V3<T> prevort, StepConsts<T> c, int cache) {
+  PL_BLK_STRIDE(i, g.N, blk_) {
     const int x = i % g.X;
     const int t = i / g.X;
     const int y = t % g.Y;
@@ -114,6 +117,11 @@ __global__ void k_forces(Grid g, V3<T> vel, T* dens, const T* heat, V3<T> prevor
       prevort.z[i] = vz;
     }
   }
+}
+template <typename T>
+__global__ void k_forces(Grid g, V3<T> vel, T* dens, const T* heat, V3<T> prevort,
+                         StepConsts<T> c, int cache) {
+  forces_body<T>(hw_blk(), g, vel, dens, heat, prevort, c, cache);
 }
 
 // ------------------------------------------------------- vorticity confinement
@@ -141,8 +149,8 @@ __device__ inline VortStencil vort_stencil(const Grid& g, int i, int x, int y, i
 // Pass 1: vorticity = curl(velocity) on the interior (lines 530-547) and
 // |vorticity| on every cell (VECTOR3_FIELD_3D::magnitudeField, 353-361).
 template <typename T>
-__global__ void k_vort1(Grid g, V3<T> v, V3<T> w, T* mag, StepConsts<T> c) {
-  PL_GRID_STRIDE(i, g.N) {
+__device__ __forceinline__ void vort1_body(Blk blk_, Grid g, V3<T> v, V3<T> w, T* mag, StepConsts<T> c) {
+  PL_BLK_STRIDE(i, g.N, blk_) {
     const int x = i % g.X;
     const int t = i / g.X;
     const int y = t % g.Y;
@@ -167,13 +175,16 @@ __global__ void k_vort1(Grid g, V3<T> v, V3<T> w, T* mag, StepConsts<T> c) {
     mag[i] = sqrt_t(wx * wx + wy * wy + wz * wz);
   }
 }
+template <typename T>
+__global__ void k_vort1(Grid g, V3<T> v, V3<T> w, T* mag, StepConsts<T> c) {
+  vort1_body<T>(hw_blk(), g, v, w, mag, c);
+}
 
 // Pass 2: N = grad|w| / |grad|w||, force = eps*dx*(N x w) on the interior
 // (lines 552-589), then velocity += force*dt (line 202).
 template <typename T>
-__global__ void k_vort2(Grid g, V3<T> vel, V3<T> w, const T* mag, V3<T> force,
-                        StepConsts<T> c, int cache) {
-  PL_GRID_STRIDE(i, g.N) {
+__device__ __forceinline__ void vort2_body(Blk blk_, Grid g, V3<T> vel, V3<T> w, const T* mag, V3<T> force, StepConsts<T> c, int cache) {
+  PL_BLK_STRIDE(i, g.N, blk_) {
     const int x = i % g.X;
     const int t = i / g.X;
     const int y = t % g.Y;
@@ -213,6 +224,11 @@ __global__ void k_vort2(Grid g, V3<T> vel, V3<T> w, const T* mag, V3<T> force,
     }
   }
 }
+template <typename T>
+__global__ void k_vort2(Grid g, V3<T> vel, V3<T> w, const T* mag, V3<T> force,
+                        StepConsts<T> c, int cache) {
+  vort2_body<T>(hw_blk(), g, vel, w, mag, force, c, cache);
+}
 
 // ----------------------------------------------------------- face conditions
 // One component per pair of faces: mode 0 zero (setZeroX/Y/Z), 1 copy from one
@@ -222,9 +238,9 @@ __global__ void k_vort2(Grid g, V3<T> vel, V3<T> w, const T* mag, V3<T> force,
 // writes, so all six faces run in one launch.  Threads enumerate the cells of
 // the x faces, then the y faces, then the z faces.
 template <typename T>
-__global__ void k_face_bc(Grid g, V3<T> v, int mode_x, int mode_y, int mode_z) {
+__device__ __forceinline__ void face_bc_body(Blk blk_, Grid g, V3<T> v, int mode_x, int mode_y, int mode_z) {
   const int nxf = 2 * g.Y * g.Z, nyf = 2 * g.X * g.Z, nzf = 2 * g.X * g.Y;
-  PL_GRID_STRIDE(i, nxf + nyf + nzf) {
+  PL_BLK_STRIDE(i, nxf + nyf + nzf, blk_) {
     if (i < nxf) {
       const int side = i & 1, r = i >> 1;
       const int y = r % g.Y, z = r / g.Y;
@@ -250,6 +266,10 @@ __global__ void k_face_bc(Grid g, V3<T> v, int mode_x, int mode_y, int mode_z) {
       v.z[c] = (mode_z == 0) ? T(0) : v.z[side ? c - m : c + m];
     }
   }
+}
+template <typename T>
+__global__ void k_face_bc(Grid g, V3<T> v, int mode_x, int mode_y, int mode_z) {
+  face_bc_body<T>(hw_blk(), g, v, mode_x, mode_y, mode_z);
 }
 
 // ---------------------------------------------------------------- advection
@@ -305,10 +325,8 @@ __device__ inline Trilinear<T> backtrace(const Grid& g, const StepConsts<T>& c, 
 // its interior neighbour's new value, which the border thread recomputes.
 // postadvection (the pre-fix-up velocity) is written when `cache` is set.
 template <typename T>
-__global__ void k_advect(Grid g, StepConsts<T> c, V3<T> vo, const T* dens_o, const T* heat_o,
-                         V3<T> vn, T* dens_n, T* heat_n, V3<T> postadv, int cache,
-                         int open_x, int open_y, int open_z, int vel_out = 1) {
-  PL_GRID_STRIDE(i, g.N) {
+__device__ __forceinline__ void advect_body(Blk blk_, Grid g, StepConsts<T> c, V3<T> vo, const T* dens_o, const T* heat_o, V3<T> vn, T* dens_n, T* heat_n, V3<T> postadv, int cache, int open_x, int open_y, int open_z, int vel_out) {
+  PL_BLK_STRIDE(i, g.N, blk_) {
     const int x = i % g.X;
     const int t = i / g.X;
     const int y = t % g.Y;
@@ -359,6 +377,12 @@ __global__ void k_advect(Grid g, StepConsts<T> c, V3<T> vo, const T* dens_o, con
     }
   }
 }
+template <typename T>
+__global__ void k_advect(Grid g, StepConsts<T> c, V3<T> vo, const T* dens_o, const T* heat_o,
+                         V3<T> vn, T* dens_n, T* heat_n, V3<T> postadv, int cache,
+                         int open_x, int open_y, int open_z, int vel_out = 1) {
+  advect_body<T>(hw_blk(), g, c, vo, dens_o, heat_o, vn, dens_n, heat_n, postadv, cache, open_x, open_y, open_z, vel_out);
+}
 
 // ------------------------------------------------------------------ damping
 // The peeled damping product (buildPeeledDampingMatrixFull, FLUID_3D_MIC.cpp:
@@ -380,9 +404,8 @@ __device__ inline T damp1(const Grid& g, const T* v, int i, int x, int y, int z,
 }
 
 template <typename T>
-__global__ void k_damping(Grid g, StepConsts<T> c, V3<T> vin, V3<T> vout, V3<T> preproj,
-                          int cache) {
-  PL_GRID_STRIDE(i, g.N) {
+__device__ __forceinline__ void damping_body(Blk blk_, Grid g, StepConsts<T> c, V3<T> vin, V3<T> vout, V3<T> preproj, int cache) {
+  PL_BLK_STRIDE(i, g.N, blk_) {
     const int x = i % g.X;
     const int t = i / g.X;
     const int y = t % g.Y;
@@ -407,14 +430,19 @@ __global__ void k_damping(Grid g, StepConsts<T> c, V3<T> vin, V3<T> vout, V3<T> 
     }
   }
 }
+template <typename T>
+__global__ void k_damping(Grid g, StepConsts<T> c, V3<T> vin, V3<T> vout, V3<T> preproj,
+                          int cache) {
+  damping_body<T>(hw_blk(), g, c, vin, vout, preproj, cache);
+}
 
 // --------------------------------------------------------------- projection
 // Divergence of FLUID_3D_MIC::project (lines 337-361) with the reflection at
 // wall neighbours, and p = 0 on the interior unless the previous pressure is
 // kept as the initial guess.
 template <typename T>
-__global__ void k_divergence(Grid g, StepConsts<T> c, V3<T> v, T* div, T* p, int keep_p) {
-  PL_GRID_STRIDE(k, g.nint) {
+__device__ __forceinline__ void divergence_body(Blk blk_, Grid g, StepConsts<T> c, V3<T> v, T* div, T* p, int keep_p) {
+  PL_BLK_STRIDE(k, g.nint, blk_) {
     int x, y, z;
     const int i = interior_cell(g, k, x, y, z);
     T xright = v.x[i + 1], xleft = v.x[i - 1];
@@ -430,14 +458,18 @@ __global__ void k_divergence(Grid g, StepConsts<T> c, V3<T> v, T* div, T* p, int
     if (!keep_p) p[i] = T(0);
   }
 }
+template <typename T>
+__global__ void k_divergence(Grid g, StepConsts<T> c, V3<T> v, T* div, T* p, int keep_p) {
+  divergence_body<T>(hw_blk(), g, c, v, div, p, keep_p);
+}
 
 // FIELD_3D::copyBorderAll (FIELD_3D.cpp:1382-1420): z faces, then y faces, then
 // x faces.  Composed, every border cell takes the value of the cell with each
 // coordinate clamped into the interior.
 template <typename T>
-__global__ void k_copy_border_all(Grid g, T* p) {
+__device__ __forceinline__ void copy_border_all_body(Blk blk_, Grid g, T* p) {
   const int nxf = 2 * g.Y * g.Z, nyf = 2 * g.X * g.Z, nzf = 2 * g.X * g.Y;
-  PL_GRID_STRIDE(i, nxf + nyf + nzf) {
+  PL_BLK_STRIDE(i, nxf + nyf + nzf, blk_) {
     int x, y, z;
     if (i < nxf) {
       const int r = i >> 1;
@@ -461,12 +493,16 @@ __global__ void k_copy_border_all(Grid g, T* p) {
     p[x + y * g.X + z * g.slab] = p[cx + cy * g.X + cz * g.slab];
   }
 }
+template <typename T>
+__global__ void k_copy_border_all(Grid g, T* p) {
+  copy_border_all_body<T>(hw_blk(), g, p);
+}
 
 // Pressure-gradient subtraction (lines 372-398): central differences, one-sided
 // at the first and last interior index of each axis.
 template <typename T>
-__global__ void k_gradient(Grid g, StepConsts<T> c, V3<T> v, const T* p) {
-  PL_GRID_STRIDE(k, g.nint) {
+__device__ __forceinline__ void gradient_body(Blk blk_, Grid g, StepConsts<T> c, V3<T> v, const T* p) {
+  PL_BLK_STRIDE(k, g.nint, blk_) {
     int x, y, z;
     const int i = interior_cell(g, k, x, y, z);
     const T inv = c.oneOverDx;
@@ -493,6 +529,10 @@ __global__ void k_gradient(Grid g, StepConsts<T> c, V3<T> v, const T* p) {
     v.y[i] = v.y[i] - gy;
     v.z[i] = v.z[i] - gz;
   }
+}
+template <typename T>
+__global__ void k_gradient(Grid g, StepConsts<T> c, V3<T> v, const T* p) {
+  gradient_body<T>(hw_blk(), g, c, v, p);
 }
 
 

@@ -44,7 +44,7 @@ __host__ __device__ inline long long skew_index(const Skew& k, int ix, int iy, i
 }
 
 constexpr int kWaveKB = 8;     // rows per TMA block (contiguous in the skewed layout)
-constexpr int kWavePF = 3;     // TMA ring depth (blocks)
+constexpr int kWavePF = 3;     // TMA ring depth (blocks) of a single plume's sweep
 constexpr int kWaveD = 8;      // inter-warp ring depth (steps)
 static_assert(kWaveD == kWaveKB, "sweep_plane maps step u of a TMA block to ring slot u");
 constexpr long long kSpinLimit = 1ll << 24;     // shared-memory polls (~0.3 s)
@@ -71,6 +71,8 @@ struct WaveArgs {
   unsigned* ctl;    // [0] slab ticket, [1] exited CTAs
   int* progress;    // [nz] steps completed, for planes read by another slab
   CgState* st;      // skip when st->done; wave_err recorded here
+  int pf = kWavePF; // TMA ring depth in blocks (2 or 3): 2 needs a third less
+                    // shared memory, so more CTAs share an SM
   // Test hook for the bounded waits: when `gate` is set, one thread per CTA
   // first polls *gate (a device word that nothing sets) at most gate_spins
   // times, before any copy is issued; on expiry the CTA records
@@ -224,9 +226,9 @@ struct WaveSmem {
 __host__ __device__ inline size_t wave_al(size_t b) { return (b + 127) & ~(size_t)127; }
 
 template <typename T>
-__host__ __device__ inline size_t wave_smem_bytes(int BZ, int W) {
-  size_t b = wave_al((size_t)BZ * kWavePF * 2 * kWaveKB * W * sizeof(T));
-  b += wave_al((size_t)BZ * kWavePF * sizeof(uint64_t));
+__host__ __device__ inline size_t wave_smem_bytes(int BZ, int W, int pf = kWavePF) {
+  size_t b = wave_al((size_t)BZ * pf * 2 * kWaveKB * W * sizeof(T));
+  b += wave_al((size_t)BZ * pf * sizeof(uint64_t));
   b += wave_al((size_t)BZ * kWaveD * W * sizeof(T));
   b += wave_al((size_t)BZ * kWaveD * sizeof(uint64_t));
   b += wave_al((size_t)(BZ + 1 + 4) * sizeof(int));
@@ -234,12 +236,12 @@ __host__ __device__ inline size_t wave_smem_bytes(int BZ, int W) {
 }
 
 template <typename T>
-__device__ inline WaveSmem<T> wave_carve(char* base, int BZ, int W) {
+__device__ inline WaveSmem<T> wave_carve(char* base, int BZ, int W, int pf) {
   WaveSmem<T> s;
   s.tma = (T*)base;
-  base += wave_al((size_t)BZ * kWavePF * 2 * kWaveKB * W * sizeof(T));
+  base += wave_al((size_t)BZ * pf * 2 * kWaveKB * W * sizeof(T));
   s.bar = (uint64_t*)base;
-  base += wave_al((size_t)BZ * kWavePF * sizeof(uint64_t));
+  base += wave_al((size_t)BZ * pf * sizeof(uint64_t));
   s.ring = (T*)base;
   base += wave_al((size_t)BZ * kWaveD * W * sizeof(T));
   s.rbar = (uint64_t*)base;
@@ -336,8 +338,9 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
   const T* inp = a.in + (long long)z * a.k.plane;
   const T* Pp = a.P + (long long)z * a.k.plane;
   T* outp = a.out + (long long)z * a.k.plane;
-  T* tma = sm.tma + (size_t)warp * kWavePF * 2 * kWaveKB * W;
-  uint64_t* bar = sm.bar + warp * kWavePF;
+  const int PF = a.pf;
+  T* tma = sm.tma + (size_t)warp * PF * 2 * kWaveKB * W;
+  uint64_t* bar = sm.bar + warp * PF;
   const T* ring_in = sm.ring + (size_t)warp * kWaveD * W;
   uint64_t* rbar_in = sm.rbar + warp * kWaveD;
   // block j = steps [j*KB, j*KB+KB); its rows are contiguous, so one bulk
@@ -346,25 +349,25 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
     const int t0 = j * kWaveKB;
     const int n = min(kWaveKB, R - t0);
     const int row0 = BWD ? (R - t0 - n) : t0;
-    uint64_t* bb = &bar[j % kWavePF];
-    T* d = tma + (size_t)(j % kWavePF) * 2 * kWaveKB * W;
+    uint64_t* bb = &bar[j % PF];
+    T* d = tma + (size_t)(j % PF) * 2 * kWaveKB * W;
     mbar_expect_tx(bb, 2u * (unsigned)n * rowb);
     tma_row(d, inp + (size_t)row0 * W, (unsigned)n * rowb, bb);
     tma_row(d + (size_t)kWaveKB * W, Pp + (size_t)row0 * W, (unsigned)n * rowb, bb);
   };
-  int issued = min(kWavePF - 1, nblocks), consumed = 0;
+  int issued = min(PF - 1, nblocks), consumed = 0;
   if (lane == 0)
     for (int j = 0; j < issued; j++) issue(j);
   bool ok = true;
   const T* din = tma;
-  // make block j current (issue the block kWavePF - 1 ahead, wait for j's
+  // make block j current (issue the block PF - 1 ahead, wait for j's
   // copies); false on timeout
   auto enter_block = [&](int j) -> bool {
-    if (j + kWavePF - 1 < nblocks) {
-      if (lane == 0) issue(j + kWavePF - 1);
-      issued = j + kWavePF;
+    if (j + PF - 1 < nblocks) {
+      if (lane == 0) issue(j + PF - 1);
+      issued = j + PF;
     }
-    const int slot = j % kWavePF;
+    const int slot = j % PF;
     long long spins = 0;
     while (!mbar_try_wait(&bar[slot], (tparity >> slot) & 1u)) {
       if (++spins > kSpinLimitSlow) {
@@ -499,7 +502,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
   }
   // every issued TMA block must land before its slot is reused or the CTA exits
   for (int j = consumed; j < issued; j++) {
-    const int k = j % kWavePF;
+    const int k = j % PF;
     long long spins = 0;
     while (!mbar_try_wait(&bar[k], (tparity >> k) & 1u)) {
       if (++spins > kSpinLimitSlow) {
@@ -519,11 +522,11 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
 // compute warp of a slab st.async-writes its per-step values into ring 0 of
 // the next slab's CTA over distributed shared memory.  No global flags.
 template <typename T, int C, bool EXACT, bool BWD>
-__global__ void __launch_bounds__(32 * 16) k_mic_wave_cl(WaveArgs<T> a) {
+__device__ __forceinline__ void mic_wave_cl_body(const WaveArgs<T>& a) {
   if (a.st->done) return;
   extern __shared__ __align__(128) char smem_raw[];
   const int BZ = a.BZ, W = a.k.W;
-  WaveSmem<T> sm = wave_carve<T>(smem_raw, BZ, W);
+  WaveSmem<T> sm = wave_carve<T>(smem_raw, BZ, W, a.pf);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned rank = cluster_rank();
   const int z0 = (int)rank * BZ;
@@ -534,7 +537,7 @@ __global__ void __launch_bounds__(32 * 16) k_mic_wave_cl(WaveArgs<T> a) {
   const unsigned down_rank = BWD ? rank - 1 : rank + 1;
   int* failed = &sm.misc[1];
   if (lane == 0 && warp < BZ) {
-    for (int k = 0; k < kWavePF; k++) mbar_init(&sm.bar[warp * kWavePF + k], 1);
+    for (int k = 0; k < a.pf; k++) mbar_init(&sm.bar[warp * a.pf + k], 1);
     for (int k = 0; k < kWaveD; k++) mbar_init(&sm.rbar[warp * kWaveD + k], 1);
   }
   if (threadIdx.x == 0) {
@@ -568,6 +571,10 @@ __global__ void __launch_bounds__(32 * 16) k_mic_wave_cl(WaveArgs<T> a) {
   __syncthreads();
   cluster_sync_all();  // no CTA leaves while a neighbour may still write into it
 }
+template <typename T, int C, bool EXACT, bool BWD>
+__global__ void __launch_bounds__(32 * 16) k_mic_wave_cl(WaveArgs<T> a) {
+  mic_wave_cl_body<T, C, EXACT, BWD>(a);
+}
 
 // ------------------------------------------------------------ courier path
 // For plumes too tall for one cluster: slabs are handed to CTAs in sweep
@@ -580,12 +587,12 @@ __global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
   if (a.st->done) return;
   extern __shared__ __align__(128) char smem_raw[];
   const int BZ = a.BZ, W = a.k.W, R = a.k.R;
-  WaveSmem<T> sm = wave_carve<T>(smem_raw, BZ, W);
+  WaveSmem<T> sm = wave_carve<T>(smem_raw, BZ, W, a.pf);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int* failed = &sm.misc[1];
   const unsigned rowb = (unsigned)(W * sizeof(T));
   if (lane == 0 && warp < BZ) {
-    for (int k = 0; k < kWavePF; k++) mbar_init(&sm.bar[warp * kWavePF + k], 1);
+    for (int k = 0; k < a.pf; k++) mbar_init(&sm.bar[warp * a.pf + k], 1);
     for (int k = 0; k < kWaveD; k++) mbar_init(&sm.rbar[warp * kWaveD + k], 1);
   }
   if (threadIdx.x == 0) sm.misc[1] = 0;
