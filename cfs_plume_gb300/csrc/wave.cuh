@@ -176,21 +176,44 @@ __device__ inline void st_async2(unsigned addr, double a, double b, unsigned bar
                "d"(a), "d"(b), "r"(bar)
                : "memory");
 }
-// lane's C values -> ring slot at shared::cluster address `dst` (16 B aligned)
+__device__ inline void st_async2f(unsigned addr, float a, float b, unsigned bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(addr),
+               "f"(a), "f"(b), "r"(bar)
+               : "memory");
+}
+
+// Values a lane keeps per ring row: C rounded up so that the lane's hand-off
+// is whole vector stores (16 bytes, or 8 for a pair of floats, or one value),
+// which is what the consumer's slot barrier counts per step; the padding is
+// written as zero and never read.  The ring is internal to the sweep: the
+// global vectors keep their W = 32*C rows.
+__host__ __device__ constexpr int ring_cp(int C, int tsize) {
+  return C == 1 ? 1 : (tsize == 4 ? (C == 2 ? 2 : ((C + 3) / 4) * 4) : ((C + 1) / 2) * 2);
+}
+
+// lane's C values -> its padded ring slice at shared::cluster address `dst`
+// (aligned to the slice size)
 template <typename T, int C>
-__device__ inline void st_async_row(unsigned dst, const T (&v)[C], unsigned bar) {
-  if (sizeof(T) == 4 && C % 4 == 0) {
+__device__ inline void st_async_ring(unsigned dst, const T (&v)[C], unsigned bar) {
+  constexpr int CP = ring_cp(C, sizeof(T));
+  T w[CP];
 #pragma unroll
-    for (int j = 0; j < C; j += 4)
-      st_async4(dst + j * 4, (float)v[j], (float)v[j + 1], (float)v[j + 2], (float)v[j + 3], bar);
-  } else if (sizeof(T) == 8 && C % 2 == 0) {
+  for (int j = 0; j < CP; j++) w[j] = j < C ? v[j] : T(0);
+  if (sizeof(T) == 4 && CP % 4 == 0) {
 #pragma unroll
-    for (int j = 0; j < C; j += 2) st_async2(dst + j * 8, (double)v[j], (double)v[j + 1], bar);
+    for (int j = 0; j < CP; j += 4)
+      st_async4(dst + j * 4, (float)w[j], (float)w[j + 1], (float)w[j + 2], (float)w[j + 3], bar);
+  } else if (sizeof(T) == 4 && CP == 2) {
+    st_async2f(dst, (float)w[0], (float)w[1], bar);
+  } else if (sizeof(T) == 8 && CP % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < CP; j += 2) st_async2(dst + j * 8, (double)w[j], (double)w[j + 1], bar);
   } else {
 #pragma unroll
-    for (int j = 0; j < C; j++) st_async(dst + j * sizeof(T), v[j], bar);
+    for (int j = 0; j < CP; j++) st_async(dst + j * sizeof(T), w[j], bar);
   }
 }
+
 __device__ inline unsigned cluster_rank() {
   unsigned r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -215,7 +238,7 @@ template <typename T>
 struct WaveSmem {
   T* tma;          // [BZ][PF][2][KB][W]  KB input rows, then KB diagonal rows
   uint64_t* bar;   // [BZ][PF]        TMA slot barriers
-  T* ring;         // [BZ][D][W]      ring r is read by compute warp r
+  T* ring;         // [BZ][D][32*CP]  ring r is read by compute warp r (CP = ring_cp)
   uint64_t* rbar;  // [BZ][D]         ring slot barriers (armed by the reader)
   int* prog;       // [BZ + 1]        steps consumed per compute warp; [BZ] courier fetch count
   int* misc;       // [4]             slab, failed
@@ -229,7 +252,7 @@ template <typename T>
 __host__ __device__ inline size_t wave_smem_bytes(int BZ, int W, int pf = kWavePF) {
   size_t b = wave_al((size_t)BZ * pf * 2 * kWaveKB * W * sizeof(T));
   b += wave_al((size_t)BZ * pf * sizeof(uint64_t));
-  b += wave_al((size_t)BZ * kWaveD * W * sizeof(T));
+  b += wave_al((size_t)BZ * kWaveD * 32 * ring_cp(W / 32, (int)sizeof(T)) * sizeof(T));
   b += wave_al((size_t)BZ * kWaveD * sizeof(uint64_t));
   b += wave_al((size_t)(BZ + 1 + 4) * sizeof(int));
   return b;
@@ -243,7 +266,7 @@ __device__ inline WaveSmem<T> wave_carve(char* base, int BZ, int W, int pf) {
   s.bar = (uint64_t*)base;
   base += wave_al((size_t)BZ * pf * sizeof(uint64_t));
   s.ring = (T*)base;
-  base += wave_al((size_t)BZ * kWaveD * W * sizeof(T));
+  base += wave_al((size_t)BZ * kWaveD * 32 * ring_cp(W / 32, (int)sizeof(T)) * sizeof(T));
   s.rbar = (uint64_t*)base;
   base += wave_al((size_t)BZ * kWaveD * sizeof(uint64_t));
   s.prog = (int*)base;
@@ -280,6 +303,22 @@ __device__ inline void lds_row(const T* src, T (&v)[C]) {
 #pragma unroll
     for (int j = 0; j < C; j++) v[j] = src[j];
   }
+}
+
+// A lane's C values from its padded ring slice (ring_cp values, vector loads).
+template <typename T, int C>
+__device__ inline void lds_ring(const T* src, T (&v)[C]) {
+  constexpr int CP = ring_cp(C, sizeof(T));
+  T w[CP];
+  if (sizeof(T) == 4 && CP == 2) {
+    const float2 f = *reinterpret_cast<const float2*>(src);
+    w[0] = (T)f.x;
+    w[1] = (T)f.y;
+  } else {
+    lds_row<T, CP>(src, w);
+  }
+#pragma unroll
+  for (int j = 0; j < C; j++) v[j] = w[j];
 }
 
 // Explicitly typed multiply-add: the generic overload set must never pick the
@@ -334,6 +373,8 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
                             unsigned& tparity, unsigned& rparity, int feed_K, bool feed_fence) {
   const int W = a.k.W, R = a.k.R;
   const unsigned rowb = (unsigned)(W * sizeof(T));
+  constexpr int CP = ring_cp(C, sizeof(T));
+  constexpr unsigned ringb = 32u * CP * sizeof(T);  // bytes of one ring row
   const int nblocks = (R + kWaveKB - 1) / kWaveKB;
   const T* inp = a.in + (long long)z * a.k.plane;
   const T* Pp = a.P + (long long)z * a.k.plane;
@@ -341,7 +382,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
   const int PF = a.pf;
   T* tma = sm.tma + (size_t)warp * PF * 2 * kWaveKB * W;
   uint64_t* bar = sm.bar + warp * PF;
-  const T* ring_in = sm.ring + (size_t)warp * kWaveD * W;
+  const T* ring_in = sm.ring + (size_t)warp * kWaveD * 32 * CP;
   uint64_t* rbar_in = sm.rbar + warp * kWaveD;
   // block j = steps [j*KB, j*KB+KB); its rows are contiguous, so one bulk
   // copy per array per block (rows stored ascending in the slot).
@@ -408,7 +449,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
           }
         }
       }
-      if (lane == 0) mbar_arm_remote(dst.rbar + (unsigned)(rs * sizeof(uint64_t)), rowb);
+      if (lane == 0) mbar_arm_remote(dst.rbar + (unsigned)(rs * sizeof(uint64_t)), ringb);
     }
     // this step's inputs from the block's TMA slot
     const int rib = BWD ? (n_blk - 1 - u) : u;
@@ -429,7 +470,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
         }
       }
       rparity ^= 1u << rs;
-      lds_row<T, C>(ring_in + (size_t)rs * W + lane * C, cz);
+      lds_ring<T, C>(ring_in + (size_t)(rs * 32 + lane) * CP, cz);
     }
     T cx = BWD ? __shfl_down_sync(0xffffffffu, edge, 1) : __shfl_up_sync(0xffffffffu, edge, 1);
     if (BWD ? (lane == 31) : (lane == 0)) cx = T(0);
@@ -450,8 +491,8 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
       edge = pass[0];
     }
     if (has_dst) {
-      const unsigned off = (unsigned)(((size_t)rs * W + lane * C) * sizeof(T));
-      st_async_row<T, C>(dst.ring + off, pass, dst.rbar + (unsigned)(rs * sizeof(uint64_t)));
+      const unsigned off = (unsigned)((size_t)(rs * 32 + lane) * CP * sizeof(T));
+      st_async_ring<T, C>(dst.ring + off, pass, dst.rbar + (unsigned)(rs * sizeof(uint64_t)));
     }
     // ---- off the chain: output and bookkeeping ----
 #pragma unroll
@@ -553,7 +594,7 @@ __device__ __forceinline__ void mic_wave_cl_body(const WaveArgs<T>& a) {
     RingDst d{0u, 0u, 0u, false};
     bool has_dst = false;
     if (warp + 1 < nw) {
-      d.ring = smem_u32(sm.ring + (size_t)(warp + 1) * kWaveD * W);
+      d.ring = smem_u32(sm.ring + (size_t)(warp + 1) * kWaveD * 32 * ring_cp(C, sizeof(T)));
       d.rbar = smem_u32(sm.rbar + (warp + 1) * kWaveD);
       d.prog = smem_u32(&sm.prog[warp + 1]);
       has_dst = true;
@@ -590,7 +631,6 @@ __global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
   WaveSmem<T> sm = wave_carve<T>(smem_raw, BZ, W, a.pf);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int* failed = &sm.misc[1];
-  const unsigned rowb = (unsigned)(W * sizeof(T));
   if (lane == 0 && warp < BZ) {
     for (int k = 0; k < a.pf; k++) mbar_init(&sm.bar[warp * a.pf + k], 1);
     for (int k = 0; k < kWaveD; k++) mbar_init(&sm.rbar[warp * kWaveD + k], 1);
@@ -659,9 +699,10 @@ __global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
               T v[C];
 #pragma unroll
               for (int j = 0; j < C; j++) v[j] = BWD ? o[i][j] : pv[i][j] * o[i][j];
-              if (lane == 0) mbar_arm_remote(rbar0 + (unsigned)(rs * sizeof(uint64_t)), rowb);
-              st_async_row<T, C>(ring0 + (unsigned)(((size_t)rs * W + lane * C) * sizeof(T)), v,
-                                 rbar0 + (unsigned)(rs * sizeof(uint64_t)));
+              constexpr int CP = ring_cp(C, sizeof(T));
+              if (lane == 0) mbar_arm_remote(rbar0 + (unsigned)(rs * sizeof(uint64_t)), 32u * CP * sizeof(T));
+              st_async_ring<T, C>(ring0 + (unsigned)((size_t)(rs * 32 + lane) * CP * sizeof(T)), v,
+                                  rbar0 + (unsigned)(rs * sizeof(uint64_t)));
             }
           }
           in_next += n;
@@ -691,7 +732,7 @@ __global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
       RingDst d{0u, 0u, 0u, false};
       const bool has_dst = warp + 1 < nw;
       if (has_dst) {
-        d.ring = smem_u32(sm.ring + (size_t)(warp + 1) * kWaveD * W);
+        d.ring = smem_u32(sm.ring + (size_t)(warp + 1) * kWaveD * 32 * ring_cp(C, sizeof(T)));
         d.rbar = smem_u32(sm.rbar + (warp + 1) * kWaveD);
         d.prog = smem_u32(&sm.prog[warp + 1]);
       }
@@ -699,7 +740,6 @@ __global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
       sweep_plane<T, C, EXACT, BWD>(a, sm, warp, lane, z, warp == 0 && !has_up, d, has_dst, failed,
                                     tpar, rpar, a.K, boundary);
     }
-    (void)rowb;
     __syncthreads();
     if (ld_vol(failed)) break;
   }
