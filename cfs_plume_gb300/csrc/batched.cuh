@@ -208,12 +208,13 @@ __global__ void kb_cgs_init2(const BPlume<T>* P, DomMap m) {
   cgs_init2_body<T>(b, p.k, p.sr, p.sz, (T*)nullptr, p.st, p.part);
 }
 
-// CG iteration j: direction d[j+1 mod 2] = z + beta d[j mod 2], q = A d
+// CG iteration j: direction d[j+1 mod 2] = z + beta d[j mod 2], q = A d,
+// marching tiles of zc planes
 template <typename T>
-__global__ void __launch_bounds__(256) kb_spmv_dir(const BPlume<T>* P, DomMap m, int flip) {
+__global__ void __launch_bounds__(256, 4) kb_spmv_dir(const BPlume<T>* P, DomMap m, int flip, int zc) {
   Blk b;
   const BPlume<T>& p = locate(P, m, b);
-  cgs_spmv_dir_rows_body<T>(b, p.g, p.k, p.sz, p.sd[flip], p.sd[flip ^ 1], p.sq, p.st, p.part);
+  cgs_spmv_dir_march_body<T>(b, p.g, p.k, p.sz, p.sd[flip], p.sd[flip ^ 1], p.sq, p.st, p.part, zc);
 }
 
 template <typename T>
@@ -344,21 +345,21 @@ cudaError_t launch_bwave(int C, const WaveArgs<T>* tab, int nplumes, int nslabs,
 
 // ------------------------------------------------------------------ tuning
 // Tile shapes of a batch.  cells_epb: elements per thread of the stencil and
-// layout kernels; vec_epb / rows_epb: elements (16-byte groups) / rows per
-// thread of the CG reductions; per sweep class, bz: planes per CTA (slab
+// layout kernels; vec_epb: 16-byte groups per thread of the CG vector
+// reductions; spmv_zc: planes per tile of the marching SpMV; per sweep class, bz: planes per CTA (slab
 // height) and pf: TMA ring depth in 8-row blocks (2 takes a third less shared
 // memory than 3, so more CTAs of the batch's clusters share an SM).
 struct BatchTuning {
   int cells_epb = 2;
   int vec_epb = 4;
-  int rows_epb = 2;
+  int spmv_zc = 32;
   std::vector<int> bz, pf;
   bool from_cache = false;
   bool timed = false;
 };
 
 // The tuning cache: one JSON object whose keys are batch signatures and whose
-// values are {"cells_epb": a, "vec_epb": b, "rows_epb": c, "bz": [..],
+// values are {"cells_epb": a, "vec_epb": b, "spmv_zc": c, "bz": [..],
 // "pf": [..]}.  The
 // reader accepts exactly what the writer produces.
 inline std::string tune_cache_path(const char* given) {
@@ -441,7 +442,7 @@ inline bool json_int_list(const std::string& obj, const char* key, std::vector<i
 
 inline std::string tuning_value_json(const BatchTuning& t) {
   std::string s = "{\"cells_epb\": " + std::to_string(t.cells_epb) + ", \"vec_epb\": " +
-                  std::to_string(t.vec_epb) + ", \"rows_epb\": " + std::to_string(t.rows_epb) + ", \"bz\": [";
+                  std::to_string(t.vec_epb) + ", \"spmv_zc\": " + std::to_string(t.spmv_zc) + ", \"bz\": [";
   for (size_t i = 0; i < t.bz.size(); i++) s += (i ? ", " : "") + std::to_string(t.bz[i]);
   s += "], \"pf\": [";
   for (size_t i = 0; i < t.pf.size(); i++) s += (i ? ", " : "") + std::to_string(t.pf[i]);
@@ -656,8 +657,8 @@ class BatchEngineT : public BatchEngine {
 
   std::string tuning_json() const override {
     std::string s = "{\"signature\": \"" + signature() + "\", \"cells_epb\": " + std::to_string(tune_.cells_epb) +
-                    ", \"vec_epb\": " + std::to_string(tune_.vec_epb) + ", \"rows_epb\": " +
-                    std::to_string(tune_.rows_epb) + ", \"classes\": [";
+                    ", \"vec_epb\": " + std::to_string(tune_.vec_epb) + ", \"spmv_zc\": " +
+                    std::to_string(tune_.spmv_zc) + ", \"classes\": [";
     for (size_t c = 0; c < cls_.size(); c++) {
       const Class& k = cls_[c];
       s += (c ? ", " : "");
@@ -999,7 +1000,7 @@ class BatchEngineT : public BatchEngine {
   // heights and argument tables.
   int apply_tuning(const BatchTuning& t) {
     if (t.bz.size() != cls_.size() || t.pf.size() != cls_.size() || t.cells_epb < 1 || t.vec_epb < 1 ||
-        t.rows_epb < 1)
+        t.spmv_zc < 1)
       return fail(PLUME_ERR_INVALID, "tuning does not match the batch");
     for (size_t ci = 0; ci < cls_.size(); ci++) {
       const auto& sh = cls_[ci].shapes;
@@ -1029,9 +1030,9 @@ class BatchEngineT : public BatchEngine {
           case D_SKEW: c = cdiv(k.total, (long long)kThreads * t.cells_epb); break;
           case D_RED: c = std::min<long long>(kRedBlocks, cdiv(k.total, (long long)kThreads * NV * t.vec_epb)); break;
           case D_VEC: c = std::min<long long>(kRedBlocks, cdiv(k.total / NV, (long long)kThreads * t.vec_epb)); break;
-          case D_ROWS: {
+          case D_ROWS: {  // marching tiles: rows of the plane layout x zc planes
             const int rpb = kThreads / k.W;
-            c = std::min<long long>(kRedBlocks, cdiv((long long)k.nz * k.R, (long long)rpb * t.rows_epb));
+            c = std::min<long long>(kRedBlocks, (long long)cdiv(k.R, rpb) * cdiv(k.nz, t.spmv_zc));
             break;
           }
         }
@@ -1177,7 +1178,7 @@ class BatchEngineT : public BatchEngine {
   // CG iteration j (directions alternate between the two buffers)
   int enqueue_iter(cudaStream_t s, int j, int set) {
     const int flip = j & 1;
-    int rc = launch(D_ROWS, kb_spmv_dir<T>, s, flip);
+    int rc = launch(D_ROWS, kb_spmv_dir<T>, s, flip, tune_.spmv_zc);
     if (rc == PLUME_OK) rc = launch(D_VEC, kb_axpy<T>, s, flip);
     if (rc == PLUME_OK) rc = sweeps(s, 0, set);
     if (rc == PLUME_OK) rc = sweeps(s, 1, set);
@@ -1299,7 +1300,7 @@ class BatchEngineT : public BatchEngine {
       if (e.first != sig) continue;
       BatchTuning c;
       if (!json_int(e.second, "cells_epb", c.cells_epb) || !json_int(e.second, "vec_epb", c.vec_epb) ||
-          !json_int(e.second, "rows_epb", c.rows_epb) || !json_int_list(e.second, "bz", c.bz) ||
+          !json_int(e.second, "spmv_zc", c.spmv_zc) || !json_int_list(e.second, "bz", c.bz) ||
           !json_int_list(e.second, "pf", c.pf))
         return false;
       c.from_cache = true;
@@ -1398,23 +1399,23 @@ class BatchEngineT : public BatchEngine {
       t.vec_epb = best_v;
     }
     {
-      int best_v = t.rows_epb;
+      int best_v = t.spmv_zc;
       float best = 1e30f;
-      for (int v : {1, 2, 4, 8}) {
+      for (int v : {8, 16, 32, 64}) {
         BatchTuning c = t;
-        c.rows_epb = v;
+        c.spmv_zc = v;
         int rc = apply_tuning(c);
         if (rc != PLUME_OK) return rc;
         float ms = 0.f;
-        rc = time_min([&] { return launch(D_ROWS, kb_spmv_dir<T>, s_, 0); }, reps, &ms);
+        rc = time_min([&] { return launch(D_ROWS, kb_spmv_dir<T>, s_, 0, v); }, reps, &ms);
         if (rc != PLUME_OK) return rc;
-        note("rows_epb", v, ms);
+        note("spmv_zc", v, ms);
         if (ms < best) {
           best = ms;
           best_v = v;
         }
       }
-      t.rows_epb = best_v;
+      t.spmv_zc = best_v;
     }
     // each sweep class's shape, the class timed alone
     for (size_t ci = 0; ci < cls_.size(); ci++) {

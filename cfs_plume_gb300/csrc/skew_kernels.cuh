@@ -423,6 +423,101 @@ __device__ __forceinline__ void cgs_spmv_dir_rows_body(Blk blk_, Grid g, Skew k,
   }
 }
 
+// The fused direction update + SpMV marching along z.  A tile is `rpb` rows
+// (blockDim.x / W of them) of the plane layout times `zc` planes; each thread
+// owns one (row, column) position of the tile and walks it down the planes,
+// keeping the direction values of the planes below, at and above in
+// registers, so a cell's z neighbours cost nothing and its wall coefficients,
+// x-neighbour offsets and validity are worked out once per tile instead of
+// once per cell.  Per cell the expression of k_cgs_spmv_dir (same order).
+// Tiles are handed to the plume's blocks round-robin.
+template <typename T>
+__device__ __forceinline__ void cgs_spmv_dir_march_body(Blk blk_, Grid g, Skew k, const T* z, const T* d_old,
+                                                        T* d_new, T* q, CgState* st, double* part, int zc) {
+  if (st->done) return;
+  __shared__ double sh[32];
+  const int W = k.W, C = k.C;
+  const int rpb = (int)blockDim.x / W;
+  const int lr = (int)threadIdx.x / W, ix = (int)threadIdx.x - lr * W;
+  const int lb = ix / C, jb = ix - lb * C;
+  const T beta = (T)st->beta;
+  const int plane = (int)k.plane;
+  const int nrg = (k.R + rpb - 1) / rpb, nzc = (k.nz + zc - 1) / zc;
+  const int ntiles = nrg * nzc;
+  // per-thread constants of the x direction
+  const int x = ix + 1;
+  const bool hxm = ix > 0, hxp = ix + 1 < k.nx;
+  const int oxm = jb > 0 ? -1 : -W - 1, oxp = jb < C - 1 ? 1 : W + 1;
+  const T cxm = coef<T>(wall_xm(g, x)), cxp = coef<T>(wall_xp(g, x));
+  DotAcc<T> dq;
+  if (lr < rpb) {
+    for (int tile = blk_.id; tile < ntiles; tile += blk_.n) {
+      const int rg = tile % nrg, zi = tile / nrg;
+      const int s = rg * rpb + lr;
+      if (s >= k.R) continue;
+      const int z0 = zi * zc, z1 = min(z0 + zc, k.nz);
+      const int iy = s - lb;
+      const bool valid = ix < k.nx && iy >= 0 && iy < k.ny;
+      int e = z0 * plane + s * W + ix;
+      if (!valid) {  // padding stays zero
+        for (int iz = z0; iz < z1; iz++, e += plane) {
+          d_new[e] = T(0);
+          q[e] = T(0);
+        }
+        continue;
+      }
+      const int y = iy + 1;
+      const bool hym = iy > 0, hyp = iy + 1 < k.ny;
+      const T cym = coef<T>(wall_ym(g, y)), cyp = coef<T>(wall_yp(g, y));
+      // the diagonal's x and y part (counts of open neighbours: exact in T,
+      // so the sum equals adiag's whatever the order)
+      const T axy = T((wall_xp(g, x) ? 0 : 1) + (wall_xm(g, x) ? 0 : 1) + (wall_yp(g, y) ? 0 : 1) +
+                      (wall_ym(g, y) ? 0 : 1));
+      auto dn = [&](int i) { return d_old[i] * beta + z[i]; };
+      T dprev = z0 > 0 ? dn(e - plane) : T(0);
+      T dcur = dn(e);
+      for (int iz = z0; iz < z1; iz++, e += plane) {
+        const int zz = iz + 1;
+        const T dnext = iz + 1 < k.nz ? dn(e + plane) : T(0);
+        const T vxm = hxm ? dn(e + oxm) : T(0);
+        const T vxp = hxp ? dn(e + oxp) : T(0);
+        const T vym = hym ? dn(e - W) : T(0);
+        const T vyp = hyp ? dn(e + W) : T(0);
+        const T vzm = iz > 0 ? dprev : T(0);
+        const bool wzm = wall_zm(g, zz), wzp = wall_zp(g, zz);
+        const T diag = axy + T((wzp ? 0 : 1) + (wzm ? 0 : 1));
+        const T qq = diag * dcur + vxm * cxm + vxp * cxp + vym * cym + vyp * cyp + vzm * coef<T>(wzm) +
+                     dnext * coef<T>(wzp);
+        dq.prod(dcur, qq);
+        d_new[e] = dcur;
+        q[e] = qq;
+        dprev = dcur;
+        dcur = dnext;
+      }
+    }
+  }
+  const double sblk = dq.block(sh);
+  if (threadIdx.x == 0) part[blk_.id] = sblk;
+  if (arrive_last(&st->ticket[0], blk_.n)) {
+    const double t = sum_partials(part, sh, blk_.n);
+    if (threadIdx.x == 0) {
+      st->dq = t;
+      if (fabs(t) > 0.0) {
+        st->alpha = st->deltaNew / t;
+      } else {  // "PCG alpha broke down! Bailing." (FLUID_3D_MIC.cpp:962-969)
+        st->done = 1;
+        st->broke = 1;
+      }
+      st->ticket[0] = 0;
+    }
+  }
+}
+template <typename T>
+__global__ void __launch_bounds__(256, 4) k_cgs_spmv_dir_march(Grid g, Skew k, const T* z, const T* d_old, T* d_new,
+                                                            T* q, CgState* st, double* part, int zc) {
+  cgs_spmv_dir_march_body<T>(hw_blk(), g, k, z, d_old, d_new, q, st, part, zc);
+}
+
 // 16-byte vector type of T
 template <typename T>
 struct Vec16;
