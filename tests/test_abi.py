@@ -52,9 +52,11 @@ def test_struct_sizes_match_header(tmp_path):
     """The ctypes mirrors in _abi.py against sizeof/offsetof of the C header
     structs, compiled with gcc."""
     import subprocess
+    from cfs_plume_gb300.batch import PlumeBatchOptions
     checks = [("plume_params", _abi.PlumeParams, "plume.h"),
               ("plume_step_stats", _abi.PlumeStepStats, "plume.h"),
-              ("plume_products_info", _abi.PlumeProductsInfo, "plume_reduced.h")]
+              ("plume_products_info", _abi.PlumeProductsInfo, "plume_reduced.h"),
+              ("plume_batch_options", PlumeBatchOptions, "plume_batch.h")]
     lines = ['#include <stdio.h>', '#include <stddef.h>']
     lines += ['#include "%s"' % h for h in sorted({c[2] for c in checks})]
     lines.append("int main(void) {")
