@@ -126,20 +126,21 @@ __global__ void kb_forces(const BPlume<T>* P, DomMap m, const BCtl* ctl) {
   forces_body<T>(b, p.g, p.vel, p.dens[par], p.heat[par], V3<T>{}, p.c, 0);
 }
 
+// the neighbour stencils: 2.5D tiles of zc planes (tile_kernels.cuh)
 template <typename T>
-__global__ void kb_vort1(const BPlume<T>* P, DomMap m) {
+__global__ void __launch_bounds__(kTileThreads) kb_vort1(const BPlume<T>* P, DomMap m, int zc) {
   Blk b;
   const BPlume<T>& p = locate(P, m, b);
   if (!p.c.has_vort) return;  // addVorticity returns early when eps <= 0
-  vort1_body<T>(b, p.g, p.vel, p.vort, p.mag, p.c);
+  vort1_tile_body<T>(b, p.g, p.vel, p.vort, p.mag, p.c, zc);
 }
 
 template <typename T>
-__global__ void kb_vort2(const BPlume<T>* P, DomMap m) {
+__global__ void __launch_bounds__(kTileThreads) kb_vort2(const BPlume<T>* P, DomMap m, int zc) {
   Blk b;
   const BPlume<T>& p = locate(P, m, b);
   if (!p.c.has_vort) return;
-  vort2_body<T>(b, p.g, p.vel, p.vort, p.mag, V3<T>{}, p.c, 0);
+  vort2_tile_body<T>(b, p.g, p.vel, p.vort, p.mag, V3<T>{}, p.c, 0, zc);
 }
 
 // mode 1 before advection (copyBorder on open axes), 2 before projection
@@ -164,17 +165,17 @@ __global__ void kb_advect(const BPlume<T>* P, DomMap m, const BCtl* ctl) {
 
 // damping from tmp back into the velocity planes
 template <typename T>
-__global__ void kb_damping(const BPlume<T>* P, DomMap m) {
+__global__ void __launch_bounds__(kTileThreads) kb_damping(const BPlume<T>* P, DomMap m, int zc) {
   Blk b;
   const BPlume<T>& p = locate(P, m, b);
-  damping_body<T>(b, p.g, p.c, p.tmp, p.vel, V3<T>{}, 0);
+  damping_tile_body<T>(b, p.g, p.c, p.tmp, p.vel, V3<T>{}, 0, zc);
 }
 
 template <typename T>
-__global__ void kb_divergence(const BPlume<T>* P, DomMap m) {
+__global__ void __launch_bounds__(kTileThreads) kb_divergence(const BPlume<T>* P, DomMap m, int zc) {
   Blk b;
   const BPlume<T>& p = locate(P, m, b);
-  divergence_body<T>(b, p.g, p.c, p.vel, p.div, p.pres, p.keep_p);
+  divergence_tile_body<T>(b, p.g, p.c, p.vel, p.div, p.pres, p.keep_p, zc);
 }
 
 template <typename T>
@@ -239,10 +240,10 @@ __global__ void kb_from_skew(const BPlume<T>* P, DomMap m) {
 }
 
 template <typename T>
-__global__ void kb_gradient(const BPlume<T>* P, DomMap m) {
+__global__ void __launch_bounds__(kTileThreads) kb_gradient(const BPlume<T>* P, DomMap m, int zc) {
   Blk b;
   const BPlume<T>& p = locate(P, m, b);
-  gradient_body<T>(b, p.g, p.c, p.vel, p.pres);
+  gradient_tile_body<T>(b, p.g, p.c, p.vel, p.pres, zc);
 }
 
 // MIC sweep of one shape class: cluster c (nslabs CTAs) sweeps plume
@@ -346,20 +347,22 @@ cudaError_t launch_bwave(int C, const WaveArgs<T>* tab, int nplumes, int nslabs,
 // ------------------------------------------------------------------ tuning
 // Tile shapes of a batch.  cells_epb: elements per thread of the stencil and
 // layout kernels; vec_epb: 16-byte groups per thread of the CG vector
-// reductions; spmv_zc: planes per tile of the marching SpMV; per sweep class, bz: planes per CTA (slab
+// reductions; spmv_zc: planes per tile of the marching SpMV; tile_zc: planes
+// per tile of the 2.5D neighbour stencils; per sweep class, bz: planes per CTA (slab
 // height) and pf: TMA ring depth in 8-row blocks (2 takes a third less shared
 // memory than 3, so more CTAs of the batch's clusters share an SM).
 struct BatchTuning {
   int cells_epb = 2;
   int vec_epb = 4;
   int spmv_zc = 32;
+  int tile_zc = 16;
   std::vector<int> bz, pf;
   bool from_cache = false;
   bool timed = false;
 };
 
 // The tuning cache: one JSON object whose keys are batch signatures and whose
-// values are {"cells_epb": a, "vec_epb": b, "spmv_zc": c, "bz": [..],
+// values are {"cells_epb": a, "vec_epb": b, "spmv_zc": c, "tile_zc": d, "bz": [..],
 // "pf": [..]}.  The
 // reader accepts exactly what the writer produces.
 inline std::string tune_cache_path(const char* given) {
@@ -442,7 +445,8 @@ inline bool json_int_list(const std::string& obj, const char* key, std::vector<i
 
 inline std::string tuning_value_json(const BatchTuning& t) {
   std::string s = "{\"cells_epb\": " + std::to_string(t.cells_epb) + ", \"vec_epb\": " +
-                  std::to_string(t.vec_epb) + ", \"spmv_zc\": " + std::to_string(t.spmv_zc) + ", \"bz\": [";
+                  std::to_string(t.vec_epb) + ", \"spmv_zc\": " + std::to_string(t.spmv_zc) +
+                  ", \"tile_zc\": " + std::to_string(t.tile_zc) + ", \"bz\": [";
   for (size_t i = 0; i < t.bz.size(); i++) s += (i ? ", " : "") + std::to_string(t.bz[i]);
   s += "], \"pf\": [";
   for (size_t i = 0; i < t.pf.size(); i++) s += (i ? ", " : "") + std::to_string(t.pf[i]);
@@ -658,7 +662,8 @@ class BatchEngineT : public BatchEngine {
   std::string tuning_json() const override {
     std::string s = "{\"signature\": \"" + signature() + "\", \"cells_epb\": " + std::to_string(tune_.cells_epb) +
                     ", \"vec_epb\": " + std::to_string(tune_.vec_epb) + ", \"spmv_zc\": " +
-                    std::to_string(tune_.spmv_zc) + ", \"classes\": [";
+                    std::to_string(tune_.spmv_zc) + ", \"tile_zc\": " + std::to_string(tune_.tile_zc) +
+                    ", \"classes\": [";
     for (size_t c = 0; c < cls_.size(); c++) {
       const Class& k = cls_[c];
       s += (c ? ", " : "");
@@ -683,7 +688,7 @@ class BatchEngineT : public BatchEngine {
   }
 
  private:
-  enum { D_CELLS, D_FACES, D_INT, D_SRC, D_SKEW, D_RED, D_VEC, D_ROWS, D_COUNT };
+  enum { D_CELLS, D_FACES, D_SRC, D_SKEW, D_RED, D_VEC, D_ROWS, D_TILES, D_COUNT };
   static constexpr int kThreads = 256;
   static constexpr int kBody = 16;  // CG iterations per graph-loop body (even: directions swap back)
   static constexpr int kKinds = 9;  // skewed vectors per plume
@@ -1000,7 +1005,7 @@ class BatchEngineT : public BatchEngine {
   // heights and argument tables.
   int apply_tuning(const BatchTuning& t) {
     if (t.bz.size() != cls_.size() || t.pf.size() != cls_.size() || t.cells_epb < 1 || t.vec_epb < 1 ||
-        t.spmv_zc < 1)
+        t.spmv_zc < 1 || t.tile_zc < 1)
       return fail(PLUME_ERR_INVALID, "tuning does not match the batch");
     for (size_t ci = 0; ci < cls_.size(); ci++) {
       const auto& sh = cls_[ci].shapes;
@@ -1020,7 +1025,6 @@ class BatchEngineT : public BatchEngine {
         switch (d) {
           case D_CELLS: c = cdiv(g.N, (long long)kThreads * t.cells_epb); break;
           case D_FACES: c = cdiv(2ll * (g.Y * g.Z + g.X * g.Z + g.X * g.Y), kThreads); break;
-          case D_INT: c = cdiv(g.nint, (long long)kThreads * t.cells_epb); break;
           case D_SRC: {
             const BPlume<T>& p = plumes_[i];
             const long long nb = (long long)p.src_n[0] * p.src_n[1] * p.src_n[2];
@@ -1030,6 +1034,7 @@ class BatchEngineT : public BatchEngine {
           case D_SKEW: c = cdiv(k.total, (long long)kThreads * t.cells_epb); break;
           case D_RED: c = std::min<long long>(kRedBlocks, cdiv(k.total, (long long)kThreads * NV * t.vec_epb)); break;
           case D_VEC: c = std::min<long long>(kRedBlocks, cdiv(k.total / NV, (long long)kThreads * t.vec_epb)); break;
+          case D_TILES: c = tile_grid(g, t.tile_zc).count(); break;
           case D_ROWS: {  // marching tiles: rows of the plane layout x zc planes
             const int rpb = kThreads / k.W;
             c = std::min<long long>(kRedBlocks, (long long)cdiv(k.R, rpb) * cdiv(k.nz, t.spmv_zc));
@@ -1156,13 +1161,14 @@ class BatchEngineT : public BatchEngine {
     if (rc == PLUME_OK) rc = launch(D_CELLS, kb_forces<T>, s, (const BCtl*)ctl_);
     bool any_vort = false;
     for (const Host& h : hp_) any_vort = any_vort || h.c.has_vort;
-    if (rc == PLUME_OK && any_vort) rc = launch(D_CELLS, kb_vort1<T>, s);
-    if (rc == PLUME_OK && any_vort) rc = launch(D_CELLS, kb_vort2<T>, s);
+    const int zt = tune_.tile_zc;
+    if (rc == PLUME_OK && any_vort) rc = launch(D_TILES, kb_vort1<T>, s, zt);
+    if (rc == PLUME_OK && any_vort) rc = launch(D_TILES, kb_vort2<T>, s, zt);
     if (rc == PLUME_OK) rc = launch(D_FACES, kb_face_bc<T>, s, 1);
     if (rc == PLUME_OK) rc = launch(D_CELLS, kb_advect<T>, s, (const BCtl*)ctl_);
-    if (rc == PLUME_OK) rc = launch(D_CELLS, kb_damping<T>, s);
+    if (rc == PLUME_OK) rc = launch(D_TILES, kb_damping<T>, s, zt);
     if (rc == PLUME_OK) rc = launch(D_FACES, kb_face_bc<T>, s, 2);
-    if (rc == PLUME_OK) rc = launch(D_INT, kb_divergence<T>, s);
+    if (rc == PLUME_OK) rc = launch(D_TILES, kb_divergence<T>, s, zt);
     if (rc == PLUME_OK) rc = launch(D_FACES, kb_copy_border<T>, s);
     if (rc == PLUME_OK) rc = launch(D_SKEW, kb_to_skew<T>, s);
     if (rc == PLUME_OK) rc = launch(D_RED, kb_cgs_init<T>, s);
@@ -1188,7 +1194,7 @@ class BatchEngineT : public BatchEngine {
 
   int enqueue_suffix(cudaStream_t s) {
     int rc = launch(D_SKEW, kb_from_skew<T>, s);
-    if (rc == PLUME_OK) rc = launch(D_INT, kb_gradient<T>, s);
+    if (rc == PLUME_OK) rc = launch(D_TILES, kb_gradient<T>, s, tune_.tile_zc);
     if (rc != PLUME_OK) return rc;
     kb_end_step<<<1, 256, 0, s>>>(st_, ctl_);
     PL_TRY(cudaGetLastError());
@@ -1300,7 +1306,8 @@ class BatchEngineT : public BatchEngine {
       if (e.first != sig) continue;
       BatchTuning c;
       if (!json_int(e.second, "cells_epb", c.cells_epb) || !json_int(e.second, "vec_epb", c.vec_epb) ||
-          !json_int(e.second, "spmv_zc", c.spmv_zc) || !json_int_list(e.second, "bz", c.bz) ||
+          !json_int(e.second, "spmv_zc", c.spmv_zc) || !json_int(e.second, "tile_zc", c.tile_zc) ||
+          !json_int_list(e.second, "bz", c.bz) ||
           !json_int_list(e.second, "pf", c.pf))
         return false;
       c.from_cache = true;
@@ -1354,11 +1361,7 @@ class BatchEngineT : public BatchEngine {
         rc = time_min(
             [&] {
               int r = launch(D_CELLS, kb_forces<T>, s_, (const BCtl*)ctl_);
-              if (r == PLUME_OK) r = launch(D_CELLS, kb_vort1<T>, s_);
-              if (r == PLUME_OK) r = launch(D_CELLS, kb_vort2<T>, s_);
               if (r == PLUME_OK) r = launch(D_CELLS, kb_advect<T>, s_, (const BCtl*)ctl_);
-              if (r == PLUME_OK) r = launch(D_CELLS, kb_damping<T>, s_);
-              if (r == PLUME_OK) r = launch(D_INT, kb_divergence<T>, s_);
               if (r == PLUME_OK) r = launch(D_SKEW, kb_to_skew<T>, s_);
               return r;
             },
@@ -1371,6 +1374,35 @@ class BatchEngineT : public BatchEngine {
         }
       }
       t.cells_epb = best_v;
+    }
+    // neighbour stencils: planes per tile
+    {
+      int best_v = t.tile_zc;
+      float best = 1e30f;
+      for (int v : {2, 4, 8, 16}) {
+        BatchTuning c = t;
+        c.tile_zc = v;
+        int rc = apply_tuning(c);
+        if (rc != PLUME_OK) return rc;
+        float ms = 0.f;
+        rc = time_min(
+            [&] {
+              int r = launch(D_TILES, kb_vort1<T>, s_, v);
+              if (r == PLUME_OK) r = launch(D_TILES, kb_vort2<T>, s_, v);
+              if (r == PLUME_OK) r = launch(D_TILES, kb_damping<T>, s_, v);
+              if (r == PLUME_OK) r = launch(D_TILES, kb_divergence<T>, s_, v);
+              if (r == PLUME_OK) r = launch(D_TILES, kb_gradient<T>, s_, v);
+              return r;
+            },
+            reps, &ms);
+        if (rc != PLUME_OK) return rc;
+        note("tile_zc", v, ms);
+        if (ms < best) {
+          best = ms;
+          best_v = v;
+        }
+      }
+      t.tile_zc = best_v;
     }
     // CG vector kernels
     {

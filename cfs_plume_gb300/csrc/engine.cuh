@@ -24,6 +24,7 @@
 #include "unet.h"
 #include "solver_kernels.cuh"
 #include "step_kernels.cuh"
+#include "tile_kernels.cuh"
 #include "wave.cuh"
 
 namespace plume {
@@ -475,10 +476,11 @@ class EngineT : public Engine {
     PL_TRY(cudaEventRecord(ev_[0], s_));
     k_forces<T><<<gN, 256, 0, s_>>>(g_, vel_, nullptr, heat_, prevort_, c_, 0);
     PL_CHECK_LAUNCH();
+    const int gT = tile_blocks(g_);
     if (c_.has_vort) {
-      k_vort1<T><<<gN, 256, 0, s_>>>(g_, vel_, vort_, mag_, c_);
+      k_vort1_t<T><<<gT, kTileThreads, 0, s_>>>(g_, vel_, vort_, mag_, c_);
       PL_CHECK_LAUNCH();
-      k_vort2<T><<<gN, 256, 0, s_>>>(g_, vel_, vort_, mag_, force_, c_, 0);
+      k_vort2_t<T><<<gT, kTileThreads, 0, s_>>>(g_, vel_, vort_, mag_, force_, c_, 0);
       PL_CHECK_LAUNCH();
     }
     const int ox = p_.bc[2] == 0, oy = p_.bc[4] == 0, oz = p_.bc[0] == 0;
@@ -516,6 +518,7 @@ class EngineT : public Engine {
     const int gI = grid_for(g_.nint);
     const int nfaces = 2 * (g_.Y * g_.Z + g_.X * g_.Z + g_.X * g_.Y);
     const int gF = grid_for(nfaces);
+    const int gT = tile_blocks(g_);  // 2.5D stencil tiles (tile_kernels.cuh)
     launches_ = 0;
     NvtxRange step_range(box ? "stepWithMovingObstacle" : "step");
     PL_TRY(cudaEventRecord(ev_[0], s_));
@@ -530,9 +533,9 @@ class EngineT : public Engine {
     PL_TRY(cudaEventRecord(evs_[0], s_));
     if (c_.has_vort) {  // addVorticity returns early when eps <= 0 (line 527)
       NvtxRange r("addVorticity");
-      k_vort1<T><<<gN, 256, 0, s_>>>(g_, vel_, vort_, mag_, c_);
+      k_vort1_t<T><<<gT, kTileThreads, 0, s_>>>(g_, vel_, vort_, mag_, c_);
       PL_CHECK_LAUNCH();
-      k_vort2<T><<<gN, 256, 0, s_>>>(g_, vel_, vort_, mag_, force_, c_, cache);
+      k_vort2_t<T><<<gT, kTileThreads, 0, s_>>>(g_, vel_, vort_, mag_, force_, c_, cache);
       PL_CHECK_LAUNCH();
     }
     PL_TRY(cudaEventRecord(evs_[1], s_));
@@ -553,7 +556,7 @@ class EngineT : public Engine {
     // damping (lines 209-212); the input buffer becomes `prediffusion`
     {
       NvtxRange r("buildPeeledDampingMatrixFull");
-      k_damping<T><<<gN, 256, 0, s_>>>(g_, c_, vel_, spare_, preproj_, cache);
+      k_damping_t<T><<<gT, kTileThreads, 0, s_>>>(g_, c_, vel_, spare_, preproj_, cache);
       PL_CHECK_LAUNCH();
     }
     std::swap(vel_, spare_);
@@ -577,7 +580,7 @@ class EngineT : public Engine {
     const bool learned = p_.warm_start == PLUME_WARM_LEARNED;
     // the learned start also uses the previous step's pressure
     const int keep_p = (p_.warm_start == PLUME_WARM_PREVIOUS || learned) ? 1 : 0;
-    k_divergence<T><<<gI, 256, 0, s_>>>(g_, c_, vel_, div_, pres_, keep_p);
+    k_divergence_t<T><<<gT, kTileThreads, 0, s_>>>(g_, c_, vel_, div_, pres_, keep_p);
     PL_CHECK_LAUNCH();
     if (!learned) {
       k_copy_border_all<T><<<gF, 256, 0, s_>>>(g_, pres_);
@@ -637,7 +640,7 @@ class EngineT : public Engine {
     }
     last_iters_ = st_host_->iter;
     PL_TRY(cudaEventRecord(ev_[2], s_));
-    k_gradient<T><<<gI, 256, 0, s_>>>(g_, c_, vel_, pres_);
+    k_gradient_t<T><<<gT, kTileThreads, 0, s_>>>(g_, c_, vel_, pres_);
     PL_CHECK_LAUNCH();
     PL_TRY(cudaEventRecord(ev_[3], s_));
     stages_valid_ = true;

@@ -476,6 +476,7 @@ __device__ __forceinline__ void cgs_spmv_dir_march_body(Blk blk_, Grid g, Skew k
       auto dn = [&](int i) { return d_old[i] * beta + z[i]; };
       T dprev = z0 > 0 ? dn(e - plane) : T(0);
       T dcur = dn(e);
+#pragma unroll 2
       for (int iz = z0; iz < z1; iz++, e += plane) {
         const int zz = iz + 1;
         const T dnext = iz + 1 < k.nz ? dn(e + plane) : T(0);
