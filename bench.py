@@ -451,20 +451,23 @@ def measure_batched(steps, warmup, seed=0, n=64):
     params = [batch_params(seed, i) for i in range(n)]
     cells = np.array([(p.res[0] - 2) * (p.res[1] - 2) * (p.res[2] - 2) for p in params], dtype=np.float64)
     arms = {}
-    for engine in ("fused", "streams"):
+    for engine in ("fused", "fused_one_group", "streams"):
         t0 = time.time()
-        b = PlumeBatch(params, engine=engine)
+        if engine == "fused_one_group":  # the same lockstep CG without the group overlap
+            b = PlumeBatch(params, engine="fused", groups=1)
+        else:
+            b = PlumeBatch(params, engine=engine)
         create_s = time.time() - t0
         b.run(0, warmup, stats=False)
         secs, stats = b.run(warmup, steps, stats=True)
-        tuning = b.tuning() if engine == "fused" else None
+        tuning = b.tuning() if engine != "streams" else None
         b.close()
         arm = {"value": cells.sum() * steps / secs, "seconds": secs, "create_seconds": create_s,
                "instance_steps_per_s": n * steps / secs,
                "pcg_iters_per_step_mean": float(np.mean([[s.iterations for s in st] for st in stats])),
                "pcg_iters_per_step_max": int(np.max([[s.iterations for s in st] for st in stats])),
                "all_converged": all(s.converged for st in stats for s in st)}
-        if engine == "fused":
+        if engine != "streams":
             # one graph launch per step; the statistics row carries the
             # kernels its step launched and the device time of the call
             arm["gpu_launches_per_step"] = float(np.mean([s.launches for s in stats[0]]))

@@ -21,7 +21,7 @@ class PlumeBatchOptions(C.Structure):
         ("engine", C.c_int32),
         ("graph", C.c_int32),
         ("tune", C.c_int32),
-        ("reserved0", C.c_int32),
+        ("groups", C.c_int32),
         ("tune_cache", C.c_char_p),
         ("reserved", C.c_int32 * 8),
     ]
@@ -75,15 +75,16 @@ def default_options():
 
 class PlumeBatch:
     """n plumes advanced together.  engine: "fused" (default) or "streams";
-    graph / tune / tune_cache: the fused engine's options."""
+    graph / tune / tune_cache / groups: the fused engine's options."""
 
-    def __init__(self, params, engine="fused", graph=True, tune=True, tune_cache=None):
+    def __init__(self, params, engine="fused", graph=True, tune=True, tune_cache=None, groups=0):
         self.lib = _lib()
         arr = (_abi.PlumeParams * len(params))(*params)
         o = default_options()
         o.engine = ENGINES[engine]
         o.graph = 1 if graph else 0
         o.tune = 1 if tune else 0
+        o.groups = groups
         self._cache = tune_cache.encode() if tune_cache else None
         o.tune_cache = self._cache
         self.h = C.c_void_p()

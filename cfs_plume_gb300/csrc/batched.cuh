@@ -81,15 +81,18 @@ struct BStat {
   double rr, bb, maxR;
 };
 
+constexpr int kMaxGroups = 2;  // CG groups: independent lockstep loops, parallel graph branches
+
 // Batch-wide control word (device memory).
 struct BCtl {
-  int parity;      // which density/heat buffer is current
-  int step_index;  // noise key of the next step's source
-  int step_local;  // statistics row of the next step
-  int bodies;      // CG-loop bodies run in this step
-  int max_iters;   // largest per-plume iteration cap (loop bound)
+  int parity;                 // which density/heat buffer is current
+  int step_index;             // noise key of the next step's source
+  int step_local;             // statistics row of the next step
+  int bodies[kMaxGroups];     // CG-loop bodies each group ran in this step
+  int max_iters;              // largest per-plume iteration cap (loop bound)
   int n;
-  BStat* stats;    // [rows][n]
+  BStat* stats;               // [rows][n]
+  const int* group_of;        // [n] each plume's CG group
 };
 
 // A stage's block table: block b of the launch belongs to plume inst[b] and
@@ -253,18 +256,20 @@ __global__ void __launch_bounds__(32 * 16) kb_wave(const WaveArgs<T>* tab, int n
   mic_wave_cl_body<T, C, EXACT, BWD>(tab[blockIdx.x / nslabs]);
 }
 
-// Last node of the CG-loop body: loop again while any plume is not done.  The
-// body count bounds the loop on the device as in the single-plume graph.
-static __global__ void kb_continue(cudaGraphConditionalHandle h, const CgState* st, BCtl* ctl, int body) {
+// Last node of a CG group's loop body: loop again while any of the group's
+// plumes (`members`, `nm` of them) is not done.  The body count bounds the
+// loop on the device as in the single-plume graph.
+static __global__ void kb_continue(cudaGraphConditionalHandle h, const CgState* st, const int* members, int nm,
+                                   BCtl* ctl, int group, int body) {
   __shared__ int any;
   if (threadIdx.x == 0) any = 0;
   __syncthreads();
-  for (int i = threadIdx.x; i < ctl->n; i += blockDim.x)
-    if (!st[i].done) any = 1;
+  for (int k = threadIdx.x; k < nm; k += blockDim.x)
+    if (!st[members[k]].done) any = 1;
   __syncthreads();
   if (threadIdx.x == 0) {
-    ctl->bodies += 1;
-    const bool more = any && ctl->bodies * body <= ctl->max_iters + 64;
+    ctl->bodies[group] += 1;
+    const bool more = any && ctl->bodies[group] * body <= ctl->max_iters + 64;
     cudaGraphSetConditional(h, more ? 1u : 0u);
   }
 }
@@ -282,7 +287,7 @@ static __global__ void kb_end_step(const CgState* st, BCtl* ctl) {
     o.done = s.done;
     o.broke = s.broke;
     o.wave_err = s.wave_err;
-    o.bodies = ctl->bodies;
+    o.bodies = ctl->bodies[ctl->group_of[i]];
     o.rr = s.rr;
     o.bb = s.bb;
     o.maxR = s.maxR;
@@ -293,7 +298,7 @@ static __global__ void kb_end_step(const CgState* st, BCtl* ctl) {
     ctl->parity ^= 1;
     ctl->step_index += 1;
     ctl->step_local += 1;
-    ctl->bodies = 0;
+    for (int g = 0; g < kMaxGroups; g++) ctl->bodies[g] = 0;
   }
 }
 
@@ -510,8 +515,15 @@ class BatchEngineT : public BatchEngine {
     }
     PL_TRY(cudaSetDevice(dev_));
     PL_TRY(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev_));
+    ngroups_ = opt_.groups > 0 ? std::min(opt_.groups, kMaxGroups) : (n >= 8 ? 2 : 1);
+    ngroups_ = std::max(1, std::min(ngroups_, n));
     PL_TRY(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
-    PL_TRY(cudaStreamCreateWithFlags(&sbody_, cudaStreamNonBlocking));
+    for (int g = 0; g < kMaxGroups; g++) {
+      PL_TRY(cudaStreamCreateWithFlags(&sg_[g], cudaStreamNonBlocking));
+      PL_TRY(cudaStreamCreateWithFlags(&sbody_[g], cudaStreamNonBlocking));
+      PL_TRY(cudaEventCreateWithFlags(&gjoin_[g], cudaEventDisableTiming));
+    }
+    PL_TRY(cudaEventCreateWithFlags(&gfork_, cudaEventDisableTiming));
     for (auto* e : {&ev_[0], &ev_[1]}) PL_TRY(cudaEventCreate(e));
     int rc = allocate();
     if (rc == PLUME_OK) rc = build_diagonals();
@@ -569,10 +581,11 @@ class BatchEngineT : public BatchEngine {
     c.parity = parity_;
     c.step_index = first_step;
     c.step_local = 0;
-    c.bodies = 0;
+    for (int g = 0; g < kMaxGroups; g++) c.bodies[g] = 0;
     c.max_iters = max_iters_all_;
     c.n = n_;
     c.stats = stats_dev_;
+    c.group_of = group_of_dev_;
     *ctl_host_ = c;
     PL_TRY(cudaMemcpyAsync(ctl_, ctl_host_, sizeof(BCtl), cudaMemcpyHostToDevice, s_));
     PL_TRY(cudaEventRecord(ev_[0], s_));
@@ -599,7 +612,15 @@ class BatchEngineT : public BatchEngine {
     total_steps_ += steps;
     last_ms_ = ms;
     int rc = PLUME_OK;
-    for (int k = 0; k < steps; k++)
+    for (int k = 0; k < steps; k++) {
+      int launched = host_launches.empty() ? 0 : host_launches[k];
+      if (graph_ok_) {  // the stencils, each group's set-up and loop bodies, the tail
+        launched = prefix_launches_ + suffix_launches_;
+        for (int g = 0; g < ngroups_; g++) {
+          const int bodies = rows[(size_t)k * n_ + gmembers_[g][0]].bodies;
+          launched += setup_launches_[g] + bodies * (kBody * iter_launches_[g] + 1);
+        }
+      }
       for (int i = 0; i < n_; i++) {
         const BStat& r = rows[(size_t)k * n_ + i];
         if (stats) {
@@ -608,8 +629,7 @@ class BatchEngineT : public BatchEngine {
           o.iterations = r.iter;
           o.converged = r.converged;
           o.fallback = 0;
-          o.launches = graph_ok_ ? prefix_launches_ + r.bodies * (kBody * iter_launches_ + 1) + suffix_launches_
-                                 : host_launches[k];
+          o.launches = launched;
           o.max_residual = r.maxR;
           o.rel_residual = r.bb > 0.0 ? sqrt(r.rr) / sqrt(r.bb) : 0.0;
           o.rhs_norm = sqrt(r.bb);
@@ -622,6 +642,7 @@ class BatchEngineT : public BatchEngine {
           rc = fail(PLUME_ERR_TIMEOUT, buf);
         }
       }
+    }
     return rc;
   }
 
@@ -667,7 +688,8 @@ class BatchEngineT : public BatchEngine {
     for (size_t c = 0; c < cls_.size(); c++) {
       const Class& k = cls_[c];
       s += (c ? ", " : "");
-      s += "{\"cells_per_lane\": " + std::to_string(k.C) + ", \"nz\": " + std::to_string(k.nz) +
+      s += "{\"group\": " + std::to_string(k.group) + ", \"cells_per_lane\": " + std::to_string(k.C) +
+           ", \"nz\": " + std::to_string(k.nz) +
            ", \"plumes\": " + std::to_string(k.members.size()) + ", \"bz\": " + std::to_string(k.BZ) +
            ", \"pf\": " + std::to_string(k.PF) + ", \"slabs\": " + std::to_string(k.nslabs) +
            ", \"smem\": " + std::to_string(k.smem) + ", \"shape_candidates\": [";
@@ -679,9 +701,10 @@ class BatchEngineT : public BatchEngine {
     s += "], \"from_cache\": " + std::string(tune_.from_cache ? "true" : "false") +
          ", \"timed\": " + std::string(tune_.timed ? "true" : "false") +
          ", \"cache_written\": " + std::string(cache_written_ ? "true" : "false") +
-         ", \"graph\": " + std::string(graph_ok_ ? "true" : "false") + ", \"launches_per_step\": {\"prefix\": " +
-         std::to_string(prefix_launches_) + ", \"per_cg_iteration\": " + std::to_string(iter_launches_) +
-         ", \"suffix\": " + std::to_string(suffix_launches_) + "}";
+         ", \"graph\": " + std::string(graph_ok_ ? "true" : "false") + ", \"groups\": " + std::to_string(ngroups_) +
+         ", \"launches_per_step\": {\"stencils\": " + std::to_string(prefix_launches_) + ", \"per_cg_iteration\": [";
+    for (int g = 0; g < ngroups_; g++) s += (g ? ", " : "") + std::to_string(iter_launches_[g]);
+    s += "], \"suffix\": " + std::to_string(suffix_launches_) + "}";
     if (!graph_note_.empty()) s += ", \"graph_note\": \"" + sanitize(graph_note_) + "\"";
     if (!tune_log_.empty()) s += ", \"timings\": {" + tune_log_ + "}";
     return s + "}";
@@ -700,8 +723,10 @@ class BatchEngineT : public BatchEngine {
     Skew k;
     StepConsts<T> c;
     int cls = 0;
+    int group = 0;  // CG group
   };
   struct Class {
+    int group = 0;
     int C = 1, nz = 1, W = 32;
     std::vector<int> members;
     // (slab height, ring depth) pairs that fit: nslabs <= 16, shared memory,
@@ -922,23 +947,52 @@ class BatchEngineT : public BatchEngine {
     return rc;
   }
 
-  // Shape classes of the sweeps: plumes with the same cells per lane and depth.
+  // CG groups and the shape classes of the sweeps.  The plumes of each shape
+  // (cells per lane, depth) are dealt to the groups in turn, so every group
+  // holds a like share of every shape; a class is the plumes of one shape in
+  // one group.
   int plan_classes() {
-    std::map<std::pair<int, int>, int> idx;
+    std::map<std::pair<int, int>, int> dealt;
+    for (int i = 0; i < n_; i++) hp_[i].group = dealt[std::make_pair(hp_[i].k.C, hp_[i].g.nz)]++ % ngroups_;
+    std::map<std::array<int, 3>, int> idx;
     for (int i = 0; i < n_; i++) {
-      const std::pair<int, int> key(hp_[i].k.C, hp_[i].g.nz);
+      const std::array<int, 3> key = {hp_[i].group, hp_[i].k.C, hp_[i].g.nz};
       auto it = idx.find(key);
       if (it == idx.end()) {
         it = idx.emplace(key, (int)cls_.size()).first;
         Class c;
-        c.C = key.first;
-        c.nz = key.second;
+        c.group = key[0];
+        c.C = key[1];
+        c.nz = key[2];
         c.W = 32 * c.C;
         cls_.push_back(c);
       }
       hp_[i].cls = it->second;
       cls_[it->second].members.push_back(i);
     }
+    std::vector<int> group_of(n_), members;
+    for (int g = 0; g < ngroups_; g++) {
+      gmembers_[g].clear();
+      gcls_[g].clear();
+      gmem_off_[g] = (int)members.size();
+      for (int i = 0; i < n_; i++)
+        if (hp_[i].group == g) {
+          gmembers_[g].push_back(i);
+          members.push_back(i);
+        }
+      for (size_t ci = 0; ci < cls_.size(); ci++)
+        if (cls_[ci].group == g) gcls_[g].push_back((int)ci);
+    }
+    for (int i = 0; i < n_; i++) group_of[i] = hp_[i].group;
+    cudaError_t ea = cudaMalloc(&gidx_dev_, 2 * (size_t)n_ * sizeof(int));
+    if (ea != cudaSuccess) {
+      (void)cudaGetLastError();
+      return fail(PLUME_ERR_OOM, "device allocation of the group tables failed");
+    }
+    group_of_dev_ = gidx_dev_;
+    gmem_dev_ = gidx_dev_ + n_;
+    PL_TRY(cudaMemcpyAsync(group_of_dev_, group_of.data(), (size_t)n_ * sizeof(int), cudaMemcpyHostToDevice, s_));
+    PL_TRY(cudaMemcpyAsync(gmem_dev_, members.data(), (size_t)n_ * sizeof(int), cudaMemcpyHostToDevice, s_));
     constexpr bool exact = std::is_same<T, double>::value;
     for (size_t ci = 0; ci < cls_.size(); ci++) {
       Class& c = cls_[ci];
@@ -979,7 +1033,8 @@ class BatchEngineT : public BatchEngine {
         PL_TRY(cudaStreamCreateWithFlags(&st.s, cudaStreamNonBlocking));
         PL_TRY(cudaEventCreateWithFlags(&st.join, cudaEventDisableTiming));
       }
-    for (auto& e : fork_) PL_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto& set : fork_)
+      for (auto& e : set) PL_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return PLUME_OK;
   }
 
@@ -1015,6 +1070,8 @@ class BatchEngineT : public BatchEngine {
     constexpr int NV = Vec16<T>::n;
     auto cdiv = [](long long a, long long b) { return (int)((a + b - 1) / b); };
     std::vector<int> host;
+    // table gi = 0 covers every plume, gi = 1 + g the plumes of CG group g
+    for (int gi = 0; gi <= ngroups_; gi++)
     for (int d = 0; d < D_COUNT; d++) {
       std::vector<int> cnt(n_), first(n_);
       int tot = 0;
@@ -1022,6 +1079,11 @@ class BatchEngineT : public BatchEngine {
         const Grid& g = hp_[i].g;
         const Skew& k = hp_[i].k;
         long long c = 0;
+        if (gi > 0 && hp_[i].group != gi - 1) {  // not in this table's group
+          cnt[i] = 0;
+          first[i] = tot;
+          continue;
+        }
         switch (d) {
           case D_CELLS: c = cdiv(g.N, (long long)kThreads * t.cells_epb); break;
           case D_FACES: c = cdiv(2ll * (g.Y * g.Z + g.X * g.Z + g.X * g.Y), kThreads); break;
@@ -1046,13 +1108,13 @@ class BatchEngineT : public BatchEngine {
         first[i] = tot;
         tot += (int)c;
       }
-      dom_total_[d] = tot;
-      dom_off_[d][0] = (int)host.size();
+      dom_total_[gi][d] = tot;
+      dom_off_[gi][d][0] = (int)host.size();
       for (int i = 0; i < n_; i++)
         for (int b = 0; b < cnt[i]; b++) host.push_back(i);
-      dom_off_[d][1] = (int)host.size();
+      dom_off_[gi][d][1] = (int)host.size();
       host.insert(host.end(), first.begin(), first.end());
-      dom_off_[d][2] = (int)host.size();
+      dom_off_[gi][d][2] = (int)host.size();
       host.insert(host.end(), cnt.begin(), cnt.end());
     }
     if (dom_buf_) cudaFree(dom_buf_);
@@ -1099,64 +1161,73 @@ class BatchEngineT : public BatchEngine {
     return PLUME_OK;
   }
 
-  DomMap dom(int d) const {
+  DomMap dom(int d, int gi = 0) const {
     DomMap m;
-    m.inst = dom_buf_ + dom_off_[d][0];
-    m.first = dom_buf_ + dom_off_[d][1];
-    m.count = dom_buf_ + dom_off_[d][2];
+    m.inst = dom_buf_ + dom_off_[gi][d][0];
+    m.first = dom_buf_ + dom_off_[gi][d][1];
+    m.count = dom_buf_ + dom_off_[gi][d][2];
     return m;
   }
 
   void count_launches() {
     bool any_vort = false;
     for (const Host& h : hp_) any_vort = any_vort || h.c.has_vort;
-    const int ncls = (int)cls_.size();
-    // source, forces, vorticity (two passes), then face conditions,
-    // advection, damping, face conditions, divergence, border copy, layout,
-    // CG set-up (8), the two sweeps per class and the second set-up kernel
-    prefix_launches_ = (dom_total_[D_SRC] > 0 ? 1 : 0) + 1 + (any_vort ? 2 : 0) + 8 + 2 * ncls + 1;
-    iter_launches_ = 3 + 2 * ncls;
+    // source, forces, vorticity (two passes), face conditions, advection,
+    // damping, face conditions, divergence, border copy, layout change
+    prefix_launches_ = (dom_total_[0][D_SRC] > 0 ? 1 : 0) + 1 + (any_vort ? 2 : 0) + 7;
+    for (int g = 0; g < ngroups_; g++) {
+      const int ncls = (int)gcls_[g].size();
+      setup_launches_[g] = 2 + 2 * ncls;  // two set-up kernels, the first sweeps
+      iter_launches_[g] = 3 + 2 * ncls;
+    }
     suffix_launches_ = 3;
   }
 
   // --------------------------------------------------------- launch helpers
+  // one launch of `kern` over the plumes of table gi (0: all, 1 + g: group g)
   template <typename... K, typename... A>
-  int launch(int d, void (*kern)(const BPlume<T>*, DomMap, K...), cudaStream_t s, A... args) {
-    if (dom_total_[d] == 0) return PLUME_OK;
-    kern<<<dom_total_[d], kThreads, 0, s>>>(P_dev_, dom(d), args...);
+  int launch_in(int gi, int d, void (*kern)(const BPlume<T>*, DomMap, K...), cudaStream_t s, A... args) {
+    if (dom_total_[gi][d] == 0) return PLUME_OK;
+    kern<<<dom_total_[gi][d], kThreads, 0, s>>>(P_dev_, dom(d, gi), args...);
     PL_TRY(cudaGetLastError());
     return PLUME_OK;
   }
+  template <typename... K, typename... A>
+  int launch(int d, void (*kern)(const BPlume<T>*, DomMap, K...), cudaStream_t s, A... args) {
+    return launch_in(0, d, kern, s, args...);
+  }
 
-  // One sweep direction for every class: class 0 on stream s, the others on
-  // their own streams forked from s and joined back (parallel branches when
-  // captured).  `set` picks the side streams (0: the step, 1: the CG body).
-  int sweeps(cudaStream_t s, int bwd, int set, int only = -1) {
+  // One sweep direction for the classes `cls`: the first on stream s, the
+  // others on their own streams forked from s and joined back (parallel
+  // branches when captured).  `set` picks the side streams and fork event
+  // (0: the step and timing, 1: the CG loop body), `slot` the group.
+  int sweeps(cudaStream_t s, int bwd, int set, const std::vector<int>& cls, int slot) {
     constexpr bool exact = std::is_same<T, double>::value;
-    const int ncls = (int)cls_.size();
-    const bool fork = only < 0 && ncls > 1;
-    if (fork) PL_TRY(cudaEventRecord(fork_[set], s));
-    for (int ci = 0; ci < ncls; ci++) {
-      if (only >= 0 && ci != only) continue;
+    const int ncls = (int)cls.size();
+    const bool fork = ncls > 1;
+    if (fork) PL_TRY(cudaEventRecord(fork_[set][slot], s));
+    for (int j = 0; j < ncls; j++) {
+      const int ci = cls[j];
       const Class& c = cls_[ci];
       cudaStream_t cs = s;
-      if (fork && ci > 0) {
+      if (fork && j > 0) {
         cs = side_[ci][set].s;
-        PL_TRY(cudaStreamWaitEvent(cs, fork_[set], 0));
+        PL_TRY(cudaStreamWaitEvent(cs, fork_[set][slot], 0));
       }
       const WaveArgs<T>* tab = c.tab + (bwd ? c.members.size() : 0);
       cudaError_t e = bwd ? launch_bwave<T, exact, true>(c.C, tab, (int)c.members.size(), c.nslabs, c.BZ, c.smem, cs)
                           : launch_bwave<T, exact, false>(c.C, tab, (int)c.members.size(), c.nslabs, c.BZ, c.smem, cs);
       PL_TRY(e);
-      if (fork && ci > 0) PL_TRY(cudaEventRecord(side_[ci][set].join, cs));
+      if (fork && j > 0) PL_TRY(cudaEventRecord(side_[ci][set].join, cs));
     }
     if (fork)
-      for (int ci = 1; ci < ncls; ci++) PL_TRY(cudaStreamWaitEvent(s, side_[ci][set].join, 0));
+      for (int j = 1; j < ncls; j++) PL_TRY(cudaStreamWaitEvent(s, side_[cls[j]][set].join, 0));
     return PLUME_OK;
   }
+  int sweep_class(cudaStream_t s, int bwd, int ci) { return sweeps(s, bwd, 0, std::vector<int>{ci}, 0); }
 
-  // source .. projection set-up .. first preconditioner application
-  int enqueue_prefix(cudaStream_t s) {
+  // source .. projection's right side in the solver layout, every plume
+  int enqueue_stencils(cudaStream_t s) {
     int rc = launch(D_SRC, kb_source<T>, s, (const BCtl*)ctl_);
     if (rc == PLUME_OK) rc = launch(D_CELLS, kb_forces<T>, s, (const BCtl*)ctl_);
     bool any_vort = false;
@@ -1171,24 +1242,29 @@ class BatchEngineT : public BatchEngine {
     if (rc == PLUME_OK) rc = launch(D_TILES, kb_divergence<T>, s, zt);
     if (rc == PLUME_OK) rc = launch(D_FACES, kb_copy_border<T>, s);
     if (rc == PLUME_OK) rc = launch(D_SKEW, kb_to_skew<T>, s);
-    if (rc == PLUME_OK) rc = launch(D_RED, kb_cgs_init<T>, s);
-    if (rc == PLUME_OK) rc = sweeps(s, 0, 0);
-    if (rc == PLUME_OK) rc = sweeps(s, 1, 0);
-    if (rc == PLUME_OK) rc = launch(D_RED, kb_cgs_init2<T>, s);
     if (rc != PLUME_OK) return rc;
     // the first direction is z itself: d_old = 0 with beta = 0
     PL_TRY(cudaMemsetAsync(plumes_[0].sd[0], 0, kind_bytes_, s));
     return PLUME_OK;
   }
 
-  // CG iteration j (directions alternate between the two buffers)
-  int enqueue_iter(cudaStream_t s, int j, int set) {
-    const int flip = j & 1;
-    int rc = launch(D_ROWS, kb_spmv_dir<T>, s, flip, tune_.spmv_zc);
-    if (rc == PLUME_OK) rc = launch(D_VEC, kb_axpy<T>, s, flip);
-    if (rc == PLUME_OK) rc = sweeps(s, 0, set);
-    if (rc == PLUME_OK) rc = sweeps(s, 1, set);
-    if (rc == PLUME_OK) rc = launch(D_VEC, kb_rz<T>, s);
+  // CG set-up of group g: r = b - A x, the first preconditioner application, r.z
+  int enqueue_setup(cudaStream_t s, int g) {
+    int rc = launch_in(1 + g, D_RED, kb_cgs_init<T>, s);
+    if (rc == PLUME_OK) rc = sweeps(s, 0, 0, gcls_[g], g);
+    if (rc == PLUME_OK) rc = sweeps(s, 1, 0, gcls_[g], g);
+    if (rc == PLUME_OK) rc = launch_in(1 + g, D_RED, kb_cgs_init2<T>, s);
+    return rc;
+  }
+
+  // CG iteration j of group g (directions alternate between the two buffers)
+  int enqueue_iter(cudaStream_t s, int j, int set, int g) {
+    const int flip = j & 1, gi = 1 + g;
+    int rc = launch_in(gi, D_ROWS, kb_spmv_dir<T>, s, flip, tune_.spmv_zc);
+    if (rc == PLUME_OK) rc = launch_in(gi, D_VEC, kb_axpy<T>, s, flip);
+    if (rc == PLUME_OK) rc = sweeps(s, 0, set, gcls_[g], g);
+    if (rc == PLUME_OK) rc = sweeps(s, 1, set, gcls_[g], g);
+    if (rc == PLUME_OK) rc = launch_in(gi, D_VEC, kb_rz<T>, s);
     return rc;
   }
 
@@ -1201,30 +1277,76 @@ class BatchEngineT : public BatchEngine {
     return PLUME_OK;
   }
 
-  // One step with the CG loop driven from the host (no graph).
+  // One step with the CG loops driven from the host (no graph): the groups
+  // one after another on the main stream.  Each plume's arithmetic does not
+  // depend on its group or on when its loop stops, so the results equal the
+  // graph's bit for bit.
   int host_step(int* launched) {
-    int rc = enqueue_prefix(s_);
+    int rc = enqueue_stencils(s_);
     if (rc != PLUME_OK) return rc;
-    int j = 0, chunk = 4;
+    *launched = prefix_launches_ + suffix_launches_;
     std::vector<CgState> hs(n_);
-    for (;;) {
-      for (int kk = 0; kk < chunk; kk++, j++) {
-        rc = enqueue_iter(s_, j, 0);
-        if (rc != PLUME_OK) return rc;
+    for (int g = 0; g < ngroups_; g++) {
+      rc = enqueue_setup(s_, g);
+      if (rc != PLUME_OK) return rc;
+      int j = 0, chunk = 4;
+      for (;;) {
+        for (int kk = 0; kk < chunk; kk++, j++) {
+          rc = enqueue_iter(s_, j, 0, g);
+          if (rc != PLUME_OK) return rc;
+        }
+        PL_TRY(cudaMemcpyAsync(hs.data(), st_, (size_t)n_ * sizeof(CgState), cudaMemcpyDeviceToHost, s_));
+        PL_TRY(cudaStreamSynchronize(s_));
+        bool all = true;
+        for (int i : gmembers_[g]) all = all && hs[i].done;
+        if (all || j > max_iters_all_ + 64) break;
+        if (chunk < 16) chunk *= 2;
       }
-      PL_TRY(cudaMemcpyAsync(hs.data(), st_, (size_t)n_ * sizeof(CgState), cudaMemcpyDeviceToHost, s_));
-      PL_TRY(cudaStreamSynchronize(s_));
-      bool all = true;
-      for (const CgState& c : hs) all = all && c.done;
-      if (all || j > max_iters_all_ + 64) break;
-      if (chunk < 16) chunk *= 2;
+      *launched += setup_launches_[g] + j * iter_launches_[g];
     }
-    *launched = prefix_launches_ + j * iter_launches_ + suffix_launches_;
     return enqueue_suffix(s_);
   }
 
-  // The whole step as one graph: prefix, a conditional-while node whose body
-  // is kBody CG iterations and kb_continue, suffix.
+  // Group g's CG set-up and loop on stream s (captured): the set-up kernels,
+  // then a conditional-while node whose body -- kBody iterations and
+  // kb_continue -- is captured on the group's body stream.
+  cudaError_t capture_group(cudaStream_t s, int g, int* rc) {
+    *rc = enqueue_setup(s, g);
+    if (*rc != PLUME_OK) return cudaSuccess;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    cudaGraphConditionalHandle h = 0;
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, cg, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &cp);
+    if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamBeginCaptureToGraph(sbody_[g], cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return e;
+    for (int j = 0; j < kBody && *rc == PLUME_OK; j++) *rc = enqueue_iter(sbody_[g], j, 1, g);
+    if (*rc == PLUME_OK) {
+      kb_continue<<<1, 256, 0, sbody_[g]>>>(h, st_, gmem_dev_ + gmem_off_[g], (int)gmembers_[g].size(), ctl_, g,
+                                            kBody);
+      e = cudaGetLastError();
+    }
+    cudaGraph_t body = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(sbody_[g], &body);
+    return e == cudaSuccess ? e2 : e;
+  }
+
+  // The whole step as one graph: the stencils over every plume, the CG groups
+  // as parallel branches (each its set-up and its own conditional-while
+  // loop, so one group's latency-bound sweeps can run beside the other's
+  // bandwidth-bound vector kernels), then the tail over every plume.
   bool build_graph() {
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(s_, cudaStreamCaptureModeRelaxed);
@@ -1232,38 +1354,17 @@ class BatchEngineT : public BatchEngine {
       fail_cuda(e, "graph capture", __FILE__, __LINE__);
       return false;
     }
-    int rc = enqueue_prefix(s_);
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    cudaGraph_t cg = nullptr;
-    const cudaGraphNode_t* deps = nullptr;
-    size_t nd = 0;
-    if (rc == PLUME_OK) e = cudaStreamGetCaptureInfo(s_, &cs, nullptr, &cg, &deps, nullptr, &nd);
-    cudaGraphConditionalHandle h = 0;
-    if (rc == PLUME_OK && e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, cg, 1, cudaGraphCondAssignDefault);
-    cudaGraphNodeParams cp = {};
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = h;
-    cp.conditional.type = cudaGraphCondTypeWhile;
-    cp.conditional.size = 1;
-    cudaGraphNode_t node = nullptr;
-    if (rc == PLUME_OK && e == cudaSuccess) e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &cp);
-    if (rc == PLUME_OK && e == cudaSuccess)
-      e = cudaStreamUpdateCaptureDependencies(s_, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
-    bool body_capturing = false;
-    if (rc == PLUME_OK && e == cudaSuccess) {
-      e = cudaStreamBeginCaptureToGraph(sbody_, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                        cudaStreamCaptureModeRelaxed);
-      body_capturing = e == cudaSuccess;
-    }
-    for (int j = 0; j < kBody && rc == PLUME_OK && e == cudaSuccess; j++) rc = enqueue_iter(sbody_, j, 1);
-    if (rc == PLUME_OK && e == cudaSuccess) {
-      kb_continue<<<1, 256, 0, sbody_>>>(h, st_, ctl_, kBody);
-      e = cudaGetLastError();
-    }
-    if (body_capturing) {
-      cudaGraph_t body = nullptr;
-      const cudaError_t e2 = cudaStreamEndCapture(sbody_, &body);
-      if (e == cudaSuccess) e = e2;
+    int rc = enqueue_stencils(s_);
+    if (rc == PLUME_OK && ngroups_ == 1) {
+      e = capture_group(s_, 0, &rc);
+    } else if (rc == PLUME_OK) {
+      e = cudaEventRecord(gfork_, s_);
+      for (int g = 0; g < ngroups_ && e == cudaSuccess && rc == PLUME_OK; g++) {
+        e = cudaStreamWaitEvent(sg_[g], gfork_, 0);
+        if (e == cudaSuccess) e = capture_group(sg_[g], g, &rc);
+        if (e == cudaSuccess && rc == PLUME_OK) e = cudaEventRecord(gjoin_[g], sg_[g]);
+      }
+      for (int g = 0; g < ngroups_ && e == cudaSuccess && rc == PLUME_OK; g++) e = cudaStreamWaitEvent(s_, gjoin_[g], 0);
     }
     if (rc == PLUME_OK && e == cudaSuccess) rc = enqueue_suffix(s_);
     const cudaError_t e3 = cudaStreamEndCapture(s_, &graph);
@@ -1289,7 +1390,7 @@ class BatchEngineT : public BatchEngine {
     for (const Host& h : hp_)
       grids[std::to_string(h.g.X) + "x" + std::to_string(h.g.Y) + "x" + std::to_string(h.g.Z)] += 1;
     std::string s = sanitize(name) + "|sm" + std::to_string(num_sms_) + "|" +
-                    (std::is_same<T, double>::value ? "fp64" : "fp32") + "|";
+                    (std::is_same<T, double>::value ? "fp64" : "fp32") + "|g" + std::to_string(ngroups_) + "|";
     bool first = true;
     for (const auto& g : grids) {
       s += (first ? "" : ",") + g.first + "*" + std::to_string(g.second);
@@ -1462,8 +1563,8 @@ class BatchEngineT : public BatchEngine {
         float ms = 0.f;
         rc = time_min(
             [&] {
-              int r = sweeps(s_, 0, 0, (int)ci);
-              if (r == PLUME_OK) r = sweeps(s_, 1, 0, (int)ci);
+              int r = sweep_class(s_, 0, (int)ci);
+              if (r == PLUME_OK) r = sweep_class(s_, 1, (int)ci);
               return r;
             },
             reps, &ms);
@@ -1499,8 +1600,9 @@ class BatchEngineT : public BatchEngine {
         if (st.s) cudaStreamDestroy(st.s);
         if (st.join) cudaEventDestroy(st.join);
       }
-    for (auto& e : fork_)
-      if (e) cudaEventDestroy(e);
+    for (auto& set : fork_)
+      for (auto& e : set)
+        if (e) cudaEventDestroy(e);
     for (auto& e : ev_)
       if (e) cudaEventDestroy(e);
     if (dom_buf_) cudaFree(dom_buf_);
@@ -1508,7 +1610,17 @@ class BatchEngineT : public BatchEngine {
     if (P_dev_) cudaFree(P_dev_);
     if (pool_) cudaFree(pool_);
     if (ctl_host_) cudaFreeHost(ctl_host_);
-    if (sbody_) cudaStreamDestroy(sbody_);
+    for (int g = 0; g < kMaxGroups; g++) {
+      if (sbody_[g]) cudaStreamDestroy(sbody_[g]);
+      if (sg_[g]) cudaStreamDestroy(sg_[g]);
+      if (gjoin_[g]) cudaEventDestroy(gjoin_[g]);
+      sbody_[g] = sg_[g] = nullptr;
+      gjoin_[g] = nullptr;
+    }
+    if (gfork_) cudaEventDestroy(gfork_);
+    gfork_ = nullptr;
+    if (gidx_dev_) cudaFree(gidx_dev_);
+    gidx_dev_ = nullptr;
     if (s_) cudaStreamDestroy(s_);
     exec_ = nullptr;
     cls_.clear();
@@ -1518,7 +1630,7 @@ class BatchEngineT : public BatchEngine {
     P_dev_ = nullptr;
     pool_ = nullptr;
     ctl_host_ = nullptr;
-    sbody_ = s_ = nullptr;
+    s_ = nullptr;
   }
 
   struct Side {
@@ -1536,9 +1648,18 @@ class BatchEngineT : public BatchEngine {
   std::vector<BPlume<T>> plumes_;
   std::vector<Class> cls_;
   std::vector<std::array<Side, 2>> side_;
-  cudaEvent_t fork_[2] = {nullptr, nullptr};
+  cudaEvent_t fork_[2][kMaxGroups] = {};
   cudaEvent_t ev_[2] = {nullptr, nullptr};
-  cudaStream_t s_ = nullptr, sbody_ = nullptr;
+  cudaStream_t s_ = nullptr;
+  // CG groups: the plumes and classes of each, their branch and body streams
+  int ngroups_ = 1;
+  std::vector<int> gmembers_[kMaxGroups], gcls_[kMaxGroups];
+  int gmem_off_[kMaxGroups] = {};
+  int* gidx_dev_ = nullptr;      // [2n]: each plume's group, then the groups' member lists
+  int* group_of_dev_ = nullptr;
+  int* gmem_dev_ = nullptr;
+  cudaStream_t sg_[kMaxGroups] = {}, sbody_[kMaxGroups] = {};
+  cudaEvent_t gfork_ = nullptr, gjoin_[kMaxGroups] = {};
   char* pool_ = nullptr;
   char* kind_base_ = nullptr;
   size_t kind_bytes_ = 0;
@@ -1549,8 +1670,8 @@ class BatchEngineT : public BatchEngine {
   BPlume<T>* P_dev_ = nullptr;
   int* dom_buf_ = nullptr;
   std::vector<int> dom_host_;
-  int dom_off_[D_COUNT][3] = {};
-  int dom_total_[D_COUNT] = {};
+  int dom_off_[kMaxGroups + 1][D_COUNT][3] = {};
+  int dom_total_[kMaxGroups + 1][D_COUNT] = {};
   BStat* stats_dev_ = nullptr;
   int stats_cap_ = 0;
   cudaGraphExec_t exec_ = nullptr;
@@ -1560,7 +1681,8 @@ class BatchEngineT : public BatchEngine {
   std::string tune_log_;
   std::string cache_path_;
   bool cache_written_ = false;
-  int prefix_launches_ = 0, iter_launches_ = 0, suffix_launches_ = 0;
+  int prefix_launches_ = 0, suffix_launches_ = 0;
+  int setup_launches_[kMaxGroups] = {}, iter_launches_[kMaxGroups] = {};
   std::string err_;
 };
 

@@ -58,14 +58,16 @@ typedef struct plume_batch_options {
                              same launches driven from the host                   */
   int32_t tune;           /* fused: 1 = tile shapes from the tuning cache, timed
                              on this GPU when the cache has none; 0 = defaults    */
-  int32_t reserved0;
+  int32_t groups;         /* fused: CG groups advanced as parallel graph branches,
+                             each its own lockstep loop (1 or 2; 0 = 2 for a batch
+                             of 8 or more plumes, else 1)                         */
   const char* tune_cache; /* fused: JSON file of tuned shapes; NULL = the file
                              named by $PLUME_TUNE_CACHE, else
                              $HOME/.cache/cfs_plume_gb300/tune.json               */
   int32_t reserved[8];
 } plume_batch_options;
 
-/* engine = FUSED, graph = 1, tune = 1, tune_cache = NULL. */
+/* engine = FUSED, graph = 1, tune = 1, groups = 0, tune_cache = NULL. */
 void plume_batch_default_options(plume_batch_options* o);
 
 /* n instances, params[i] each.  The fused engine needs every instance on the

@@ -172,6 +172,30 @@ def test_fused_graph_and_host_loop_are_identical():
 
 
 @pytest.mark.gpu
+def test_cg_groups_change_no_bit():
+    """Ten plumes of the configuration (every grid size) as one CG group and as
+    two groups advanced in parallel graph branches: each plume's arithmetic
+    does not depend on its group, so the fields are identical bit for bit;
+    and the two-group graph equals its host-driven loop."""
+    params = [batch_params(5, i) for i in range(10)]
+    one = PlumeBatch(params, groups=1, tune=False)
+    two = PlumeBatch(params, groups=2, tune=False)
+    two_host = PlumeBatch(params, groups=2, tune=False, graph=False)
+    assert one.tuning()["groups"] == 1 and two.tuning()["groups"] == 2
+    assert {c["group"] for c in two.tuning()["classes"]} == {0, 1}
+    runs = [b.run(0, 3)[1] for b in (one, two, two_host)]
+    for i in range(len(params)):
+        its = [[s.iterations for s in r[i]] for r in runs]
+        assert its[0] == its[1] == its[2], (i, its)
+        for name in ("velocity", "density", "pressure"):
+            a = one.field(i, name)
+            assert np.array_equal(a, two.field(i, name)), (i, name)
+            assert np.array_equal(a, two_host.field(i, name)), (i, name)
+    for b in (one, two, two_host):
+        b.close()
+
+
+@pytest.mark.gpu
 def test_autotuner_writes_and_reads_its_cache(tmp_path):
     cache = str(tmp_path / "tune" / "cache.json")
     params = [batch_params(9, i) for i in range(6)]
