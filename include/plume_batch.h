@@ -59,8 +59,8 @@ typedef struct plume_batch_options {
   int32_t tune;           /* fused: 1 = tile shapes from the tuning cache, timed
                              on this GPU when the cache has none; 0 = defaults    */
   int32_t groups;         /* fused: CG groups advanced as parallel graph branches,
-                             each its own lockstep loop (1 or 2; 0 = 2 for a batch
-                             of 8 or more plumes, else 1)                         */
+                             each its own lockstep loop (1 to 4; 0 = 4 for a batch
+                             of 32 or more plumes, 2 for 8 or more, else 1)       */
   const char* tune_cache; /* fused: JSON file of tuned shapes; NULL = the file
                              named by $PLUME_TUNE_CACHE, else
                              $HOME/.cache/cfs_plume_gb300/tune.json               */
