@@ -23,7 +23,8 @@ class PlumeBatchOptions(C.Structure):
         ("tune", C.c_int32),
         ("groups", C.c_int32),
         ("tune_cache", C.c_char_p),
-        ("reserved", C.c_int32 * 8),
+        ("persistent", C.c_int32),
+        ("reserved", C.c_int32 * 7),
     ]
 
 
@@ -75,9 +76,10 @@ def default_options():
 
 class PlumeBatch:
     """n plumes advanced together.  engine: "fused" (default) or "streams";
-    graph / tune / tune_cache / groups: the fused engine's options."""
+    graph / tune / tune_cache / groups / persistent: the fused engine's options."""
 
-    def __init__(self, params, engine="fused", graph=True, tune=True, tune_cache=None, groups=0):
+    def __init__(self, params, engine="fused", graph=True, tune=True, tune_cache=None, groups=0,
+                 persistent=False):
         self.lib = _lib()
         arr = (_abi.PlumeParams * len(params))(*params)
         o = default_options()
@@ -85,6 +87,7 @@ class PlumeBatch:
         o.graph = 1 if graph else 0
         o.tune = 1 if tune else 0
         o.groups = groups
+        o.persistent = 1 if persistent else 0
         self._cache = tune_cache.encode() if tune_cache else None
         o.tune_cache = self._cache
         self.h = C.c_void_p()

@@ -64,7 +64,10 @@ typedef struct plume_batch_options {
   const char* tune_cache; /* fused: JSON file of tuned shapes; NULL = the file
                              named by $PLUME_TUNE_CACHE, else
                              $HOME/.cache/cfs_plume_gb300/tune.json               */
-  int32_t reserved[8];
+  int32_t persistent;     /* fused: 1 = every stage a persistent launch (grid =
+                             resident blocks walking the stage's block table);
+                             0 = one block per table entry (measured faster)     */
+  int32_t reserved[7];
 } plume_batch_options;
 
 /* engine = FUSED, graph = 1, tune = 1, groups = 0, tune_cache = NULL. */

@@ -174,12 +174,13 @@ def test_fused_graph_and_host_loop_are_identical():
 @pytest.mark.gpu
 def test_cg_groups_change_no_bit():
     """Ten plumes of the configuration (every grid size) as one CG group and as
-    two groups advanced in parallel graph branches: each plume's arithmetic
-    does not depend on its group, so the fields are identical bit for bit;
+    two groups advanced in parallel graph branches with persistent stage
+    launches: each plume's arithmetic depends neither on its group nor on the
+    grid walking its virtual blocks, so the fields are identical bit for bit;
     and the two-group graph equals its host-driven loop."""
     params = [batch_params(5, i) for i in range(10)]
     one = PlumeBatch(params, groups=1, tune=False)
-    two = PlumeBatch(params, groups=2, tune=False)
+    two = PlumeBatch(params, groups=2, tune=False, persistent=True)
     two_host = PlumeBatch(params, groups=2, tune=False, graph=False)
     assert one.tuning()["groups"] == 1 and two.tuning()["groups"] == 2
     assert {c["group"] for c in two.tuning()["classes"]} == {0, 1}
