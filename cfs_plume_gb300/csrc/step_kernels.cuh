@@ -124,112 +124,6 @@ __global__ void k_forces(Grid g, V3<T> vel, T* dens, const T* heat, V3<T> prevor
   forces_body<T>(hw_blk(), g, vel, dens, heat, prevort, c, cache);
 }
 
-// ------------------------------------------------------- vorticity confinement
-// Neighbour choice of FLUID_3D_MIC::addVorticity (lines 533-545): one-sided at
-// the first and last interior index of each axis (the obstacle test there is
-// true exactly on those cells, since only wall slabs are obstacles).
-struct VortStencil {
-  int up, down, out, in, right, left;
-  bool oy, oz, ox;  // one-sided along y, z, x
-};
-__device__ inline VortStencil vort_stencil(const Grid& g, int i, int x, int y, int z) {
-  VortStencil s;
-  s.up = (y == g.Y - 2) ? i : i + g.X;
-  s.down = (y == 1) ? i : i - g.X;
-  s.out = (z == g.Z - 2) ? i : i + g.slab;
-  s.in = (z == 1) ? i : i - g.slab;
-  s.right = (x == g.X - 2) ? i : i + 1;
-  s.left = (x == 1) ? i : i - 1;
-  s.oy = (s.up == i || s.down == i);
-  s.oz = (s.out == i || s.in == i);
-  s.ox = (s.left == i || s.right == i);
-  return s;
-}
-
-// Pass 1: vorticity = curl(velocity) on the interior (lines 530-547) and
-// |vorticity| on every cell (VECTOR3_FIELD_3D::magnitudeField, 353-361).
-template <typename T>
-__device__ __forceinline__ void vort1_body(Blk blk_, Grid g, V3<T> v, V3<T> w, T* mag, StepConsts<T> c) {
-  PL_BLK_STRIDE(i, g.N, blk_) {
-    const int x = i % g.X;
-    const int t = i / g.X;
-    const int y = t % g.Y;
-    const int z = t / g.Y;
-    T wx, wy, wz;
-    if (!on_border(g, x, y, z)) {
-      const VortStencil s = vort_stencil(g, i, x, y, z);
-      const T dy = s.oy ? c.oneOverDx : c.gridSize;
-      const T dz = s.oz ? c.oneOverDx : c.gridSize;
-      const T dx = s.ox ? c.oneOverDx : c.gridSize;
-      wx = (v.z[s.up] - v.z[s.down]) * dy + (-v.y[s.out] + v.y[s.in]) * dz;
-      wy = (v.x[s.out] - v.x[s.in]) * dz + (-v.z[s.right] + v.z[s.left]) * dx;
-      wz = (v.y[s.right] - v.y[s.left]) * dx + (-v.x[s.up] + v.x[s.down]) * dy;
-      w.x[i] = wx;
-      w.y[i] = wy;
-      w.z[i] = wz;
-    } else {
-      wx = w.x[i];
-      wy = w.y[i];
-      wz = w.z[i];
-    }
-    mag[i] = sqrt_t(wx * wx + wy * wy + wz * wz);
-  }
-}
-template <typename T>
-__global__ void k_vort1(Grid g, V3<T> v, V3<T> w, T* mag, StepConsts<T> c) {
-  vort1_body<T>(hw_blk(), g, v, w, mag, c);
-}
-
-// Pass 2: N = grad|w| / |grad|w||, force = eps*dx*(N x w) on the interior
-// (lines 552-589), then velocity += force*dt (line 202).
-template <typename T>
-__device__ __forceinline__ void vort2_body(Blk blk_, Grid g, V3<T> vel, V3<T> w, const T* mag, V3<T> force, StepConsts<T> c, int cache) {
-  PL_BLK_STRIDE(i, g.N, blk_) {
-    const int x = i % g.X;
-    const int t = i / g.X;
-    const int y = t % g.Y;
-    const int z = t / g.Y;
-    T fx = T(0), fy = T(0), fz = T(0);
-    bool has_f = false;
-    if (!on_border(g, x, y, z)) {
-      const VortStencil s = vort_stencil(g, i, x, y, z);
-      const T dy = s.oy ? c.oneOverDx : c.gridSize;
-      const T dz = s.oz ? c.oneOverDx : c.gridSize;
-      const T dx = s.ox ? c.oneOverDx : c.gridSize;
-      T N0 = (mag[s.right] - mag[s.left]) * dx;
-      T N1 = (mag[s.up] - mag[s.down]) * dy;
-      T N2 = (mag[s.out] - mag[s.in]) * dz;
-      T m = sqrt_t(N0 * N0 + N1 * N1 + N2 * N2);
-      if (m > T(0)) {
-        m = T(1) / m;
-        N0 *= m;
-        N1 *= m;
-        N2 *= m;
-        const T wx = w.x[i], wy = w.y[i], wz = w.z[i];
-        fx = (N1 * wz - N2 * wy) * c.dx * c.eps;
-        fy = -((N0 * wz - N2 * wx) * c.dx * c.eps);
-        fz = (N0 * wy - N1 * wx) * c.dx * c.eps;
-        has_f = true;
-      }
-    }
-    if (has_f) {
-      vel.x[i] = vel.x[i] + fx * c.dt;
-      vel.y[i] = vel.y[i] + fy * c.dt;
-      vel.z[i] = vel.z[i] + fz * c.dt;
-    }
-    if (cache) {
-      force.x[i] = fx;
-      force.y[i] = fy;
-      force.z[i] = fz;
-    }
-  }
-}
-template <typename T>
-__global__ void k_vort2(Grid g, V3<T> vel, V3<T> w, const T* mag, V3<T> force,
-                        StepConsts<T> c, int cache) {
-  vort2_body<T>(hw_blk(), g, vel, w, mag, force, c, cache);
-}
-
 // ----------------------------------------------------------- face conditions
 // One component per pair of faces: mode 0 zero (setZeroX/Y/Z), 1 copy from one
 // cell in (copyBorderX/Y/Z), 2 copy from two cells in (setNeumannX/Y/Z)
@@ -384,85 +278,7 @@ __global__ void k_advect(Grid g, StepConsts<T> c, V3<T> vo, const T* dens_o, con
   advect_body<T>(hw_blk(), g, c, vo, dens_o, heat_o, vn, dens_n, heat_n, postadv, cache, open_x, open_y, open_z, vel_out);
 }
 
-// ------------------------------------------------------------------ damping
-// The peeled damping product (buildPeeledDampingMatrixFull, FLUID_3D_MIC.cpp:
-// 1251-1306, applied through SPARSE_MATRIX operator*, SPARSE_MATRIX.cpp:83-105):
-// out = (1-w) v + (w/6) * (existing peeled neighbours), summed in the map's
-// column order z-1, y-1, x-1, self, x+1, y+1, z+1.  Border cells pass through.
-// Out of place; `preproj` receives a copy of the result when caching.
-template <typename T>
-__device__ inline T damp1(const Grid& g, const T* v, int i, int x, int y, int z, T wm, T s6) {
-  T acc = T(0);
-  if (z != 1) acc += v[i - g.slab] * s6;
-  if (y != 1) acc += v[i - g.X] * s6;
-  if (x != 1) acc += v[i - 1] * s6;
-  acc += v[i] * wm;
-  if (x != g.X - 2) acc += v[i + 1] * s6;
-  if (y != g.Y - 2) acc += v[i + g.X] * s6;
-  if (z != g.Z - 2) acc += v[i + g.slab] * s6;
-  return acc;
-}
-
-template <typename T>
-__device__ __forceinline__ void damping_body(Blk blk_, Grid g, StepConsts<T> c, V3<T> vin, V3<T> vout, V3<T> preproj, int cache) {
-  PL_BLK_STRIDE(i, g.N, blk_) {
-    const int x = i % g.X;
-    const int t = i / g.X;
-    const int y = t % g.Y;
-    const int z = t / g.Y;
-    T ox, oy, oz;
-    if (on_border(g, x, y, z)) {
-      ox = vin.x[i];
-      oy = vin.y[i];
-      oz = vin.z[i];
-    } else {
-      ox = damp1(g, vin.x, i, x, y, z, c.wMinus, c.sixth);
-      oy = damp1(g, vin.y, i, x, y, z, c.wMinus, c.sixth);
-      oz = damp1(g, vin.z, i, x, y, z, c.wMinus, c.sixth);
-    }
-    vout.x[i] = ox;
-    vout.y[i] = oy;
-    vout.z[i] = oz;
-    if (cache) {
-      preproj.x[i] = ox;
-      preproj.y[i] = oy;
-      preproj.z[i] = oz;
-    }
-  }
-}
-template <typename T>
-__global__ void k_damping(Grid g, StepConsts<T> c, V3<T> vin, V3<T> vout, V3<T> preproj,
-                          int cache) {
-  damping_body<T>(hw_blk(), g, c, vin, vout, preproj, cache);
-}
-
 // --------------------------------------------------------------- projection
-// Divergence of FLUID_3D_MIC::project (lines 337-361) with the reflection at
-// wall neighbours, and p = 0 on the interior unless the previous pressure is
-// kept as the initial guess.
-template <typename T>
-__device__ __forceinline__ void divergence_body(Blk blk_, Grid g, StepConsts<T> c, V3<T> v, T* div, T* p, int keep_p) {
-  PL_BLK_STRIDE(k, g.nint, blk_) {
-    int x, y, z;
-    const int i = interior_cell(g, k, x, y, z);
-    T xright = v.x[i + 1], xleft = v.x[i - 1];
-    T yup = v.y[i + g.X], ydown = v.y[i - g.X];
-    T ztop = v.z[i + g.slab], zbottom = v.z[i - g.slab];
-    if (wall_xp(g, x)) xright = -v.x[i];
-    if (wall_xm(g, x)) xleft = -v.x[i];
-    if (wall_yp(g, y)) yup = -v.y[i];
-    if (wall_ym(g, y)) ydown = -v.y[i];
-    if (wall_zp(g, z)) ztop = -v.z[i];
-    if (wall_zm(g, z)) zbottom = -v.z[i];
-    div[i] = c.divc * (xright - xleft + yup - ydown + ztop - zbottom);
-    if (!keep_p) p[i] = T(0);
-  }
-}
-template <typename T>
-__global__ void k_divergence(Grid g, StepConsts<T> c, V3<T> v, T* div, T* p, int keep_p) {
-  divergence_body<T>(hw_blk(), g, c, v, div, p, keep_p);
-}
-
 // FIELD_3D::copyBorderAll (FIELD_3D.cpp:1382-1420): z faces, then y faces, then
 // x faces.  Composed, every border cell takes the value of the cell with each
 // coordinate clamped into the interior.
@@ -497,44 +313,6 @@ template <typename T>
 __global__ void k_copy_border_all(Grid g, T* p) {
   copy_border_all_body<T>(hw_blk(), g, p);
 }
-
-// Pressure-gradient subtraction (lines 372-398): central differences, one-sided
-// at the first and last interior index of each axis.
-template <typename T>
-__device__ __forceinline__ void gradient_body(Blk blk_, Grid g, StepConsts<T> c, V3<T> v, const T* p) {
-  PL_BLK_STRIDE(k, g.nint, blk_) {
-    int x, y, z;
-    const int i = interior_cell(g, k, x, y, z);
-    const T inv = c.oneOverDx;
-    T gx, gy, gz;
-    if (x == 1)
-      gx = (p[i + 1] - p[i]) * inv;
-    else if (x == g.X - 2)
-      gx = (p[i] - p[i - 1]) * inv;
-    else
-      gx = T(0.5) * (p[i + 1] - p[i - 1]) * inv;
-    if (y == 1)
-      gy = (p[i + g.X] - p[i]) * inv;
-    else if (y == g.Y - 2)
-      gy = (p[i] - p[i - g.X]) * inv;
-    else
-      gy = T(0.5) * (p[i + g.X] - p[i - g.X]) * inv;
-    if (z == 1)
-      gz = (p[i + g.slab] - p[i]) * inv;
-    else if (z == g.Z - 2)
-      gz = (p[i] - p[i - g.slab]) * inv;
-    else
-      gz = T(0.5) * (p[i + g.slab] - p[i - g.slab]) * inv;
-    v.x[i] = v.x[i] - gx;
-    v.y[i] = v.y[i] - gy;
-    v.z[i] = v.z[i] - gz;
-  }
-}
-template <typename T>
-__global__ void k_gradient(Grid g, StepConsts<T> c, V3<T> v, const T* p) {
-  gradient_body<T>(hw_blk(), g, c, v, p);
-}
-
 
 // ------------------------------------------------------------ moving box
 // The box of FLUID_3D_MIC::stepWithMovingObstacle as the stomp kernel sees

@@ -10,10 +10,10 @@
 // global memory a second time.  Every plane of every field is read from global
 // memory once by its owning thread, in coalesced rows.
 //
-// Each cell evaluates exactly the expression of the grid-stride kernel it
-// replaces in step_kernels.cuh (FLUID_3D_MIC.cpp lines cited there), in the
-// same order, so the FP64 results are bit-identical; only where the
-// neighbour values come from changes.  Tiles are handed to a plume's blocks
+// Each cell evaluates the reference's expression in the reference's order
+// (the FLUID_3D_MIC.cpp lines are cited per kernel), so the FP64 results are
+// bit-identical to the reference's serial loops; only where the neighbour
+// values come from differs.  Tiles are handed to a plume's blocks
 // round-robin through a Blk (common.cuh), so the same bodies serve one plume
 // and the batch.
 #pragma once
@@ -98,8 +98,12 @@ struct ZCol {
   const int col = x + y * (g).X
 
 // ---------------------------------------------------------------- vorticity
-// Pass 1 of addVorticity (k_vort1): curl on the interior with the one-sided
-// differences of vort_stencil, |w| on every cell.
+// Pass 1 of FLUID_3D_MIC::addVorticity: vorticity = curl(velocity) on the
+// interior (lines 530-547) and |vorticity| on every cell
+// (VECTOR3_FIELD_3D::magnitudeField, 353-361).  The neighbours are those of
+// lines 533-545: one-sided at the first and last interior index of each axis
+// (the obstacle test there is true exactly on those cells, since only the wall
+// slabs are obstacles).
 template <typename T>
 __device__ __forceinline__ void vort1_tile_body(Blk blk_, Grid g, V3<T> v, V3<T> w, T* mag, StepConsts<T> c,
                                                 int zc) {
@@ -153,8 +157,8 @@ __device__ __forceinline__ void vort1_tile_body(Blk blk_, Grid g, V3<T> v, V3<T>
   }
 }
 
-// Pass 2 (k_vort2): N = grad|w| / |grad|w||, force = eps*dx*(N x w), velocity
-// += force*dt.
+// Pass 2: N = grad|w| / |grad|w||, force = eps*dx*(N x w) on the interior
+// (lines 552-589), then velocity += force*dt (line 202).
 template <typename T>
 __device__ __forceinline__ void vort2_tile_body(Blk blk_, Grid g, V3<T> vel, V3<T> w, const T* mag, V3<T> force,
                                                 StepConsts<T> c, int cache, int zc) {
@@ -214,8 +218,11 @@ __device__ __forceinline__ void vort2_tile_body(Blk blk_, Grid g, V3<T> vel, V3<
 }
 
 // ------------------------------------------------------------------ damping
-// k_damping: out = (1-w) v + (w/6) * (existing peeled neighbours) in the
-// column order z-1, y-1, x-1, self, x+1, y+1, z+1; border cells pass through.
+// The peeled damping product (buildPeeledDampingMatrixFull, FLUID_3D_MIC.cpp:
+// 1251-1306, applied through SPARSE_MATRIX operator*, SPARSE_MATRIX.cpp:83-105):
+// out = (1-w) v + (w/6) * (existing peeled neighbours), summed in the map's
+// column order z-1, y-1, x-1, self, x+1, y+1, z+1.  Border cells pass through.
+// Out of place; `preproj` receives a copy of the result when caching.
 template <typename T>
 __device__ __forceinline__ T damp1_tile(const Grid& g, int x, int y, int z, T zm, T ym, T xm, T ctr, T xp, T yp, T zp,
                                         T wm, T s6) {
@@ -269,8 +276,9 @@ __device__ __forceinline__ void damping_tile_body(Blk blk_, Grid g, StepConsts<T
 }
 
 // --------------------------------------------------------------- projection
-// k_divergence: the divergence with wall reflections on the interior, p = 0
-// there unless the previous pressure is kept.
+// Divergence of FLUID_3D_MIC::project (lines 337-361) with the reflection at
+// wall neighbours, and p = 0 on the interior unless the previous pressure is
+// kept as the initial guess.
 template <typename T>
 __device__ __forceinline__ void divergence_tile_body(Blk blk_, Grid g, StepConsts<T> c, V3<T> v, T* div, T* p,
                                                      int keep_p, int zc) {
@@ -305,8 +313,8 @@ __device__ __forceinline__ void divergence_tile_body(Blk blk_, Grid g, StepConst
   }
 }
 
-// k_gradient: central differences of p on the interior, one-sided at the
-// first and last interior index of each axis.
+// Pressure-gradient subtraction (lines 372-398): central differences,
+// one-sided at the first and last interior index of each axis.
 template <typename T>
 __device__ __forceinline__ void gradient_tile_body(Blk blk_, Grid g, StepConsts<T> c, V3<T> v, const T* p, int zc) {
   __shared__ HaloTile<T> sp;
