@@ -156,6 +156,53 @@ def test_fused_batch_fp32_configuration_plumes_match_single_plumes():
 
 
 @pytest.mark.gpu
+def test_fused_batch_fp32_configuration_plumes_against_fp64_oracle():
+    """Plumes of the batched configuration itself (seed 5's 32^3 and 48x64x48
+    instances), FP32 fields with FP64-class reductions at rel-L2 1e-6, 20
+    steps in one fused batch: each within 1e-4 relative L2 of the FP64 oracle
+    of its own configuration (FLUID_3D_MIC::step at the same stop test),
+    inside the plume's predictability horizon."""
+    from oracle import oracle
+    cand = [batch_params(5, i) for i in range(16)]
+    params = [p for p in cand if tuple(p.res) == (32, 32, 32)][:2] + \
+             [p for p in cand if tuple(p.res) == (48, 64, 48)][:2]
+    assert len(params) == 4
+    b = PlumeBatch(params)
+    steps = 20
+    _, stats = b.run(0, steps)
+    for i, p in enumerate(params):
+        q = _abi.PlumeParams.from_buffer_copy(bytes(p))
+        q.precision = _abi.PREC_FP64
+        o = oracle.Oracle(q)
+        for s in range(steps):
+            o.add_source(s)
+            o.step()
+        assert all(st.converged == 1 and st.rel_residual <= 1e-6 for st in stats[i]), i
+        for name in ("velocity", "density"):
+            e = rel_l2(b.field(i, name), o.field(name))
+            assert e < 1e-4, (i, tuple(p.res), name, e)
+        o.close()
+    b.close()
+
+
+@pytest.mark.gpu
+def test_batched_configuration_runs_its_100_steps():
+    """The batched configuration as specified: 64 plumes of uneven grids, 100
+    steps each in one fused batch; every solve meets its stop test and every
+    field stays finite."""
+    params = [batch_params(11, i) for i in range(64)]
+    b = PlumeBatch(params)
+    _, stats = b.run(0, 100)
+    bad = [(i, k) for i in range(64) for k, st in enumerate(stats[i])
+           if not (st.converged == 1 and st.rel_residual <= 1e-6)]
+    assert not bad, bad[:5]
+    for i in (0, 21, 42, 63):
+        for name in ("velocity", "density", "pressure"):
+            assert np.isfinite(b.field(i, name)).all(), (i, name)
+    b.close()
+
+
+@pytest.mark.gpu
 def test_fused_graph_and_host_loop_are_identical():
     params = uneven(_abi.PREC_FP32, tol=1e-6)
     a = PlumeBatch(params, graph=True, tune=False)
