@@ -134,18 +134,13 @@ __device__ inline void st_vol(int* p, int v) { *((volatile int*)p) = v; }
 
 // Extra PTX for the ring hand-off: st.async writes a value into (possibly
 // another CTA's) shared memory and signals that CTA's mbarrier with the bytes
-// written (complete_tx); the consumer arms its slot barrier with the expected
-// byte count and waits on the phase.  No fence is needed on the producer side,
-// so a step never waits for its own global stores to drain.
+// written (complete_tx).  The consumer arms each of its slot barriers itself
+// -- one arrival with the expected byte count, at start and again right after
+// each use of the slot -- and waits on the phase; a phase completes once the
+// arrival and the bytes are both in, in either order.  So the producer's
+// step sends nothing but the data, and no fence sits on its side either (a
+// step never waits for its own global stores to drain).
 __device__ inline void mbar_arm(uint64_t* bar, unsigned bytes) { mbar_expect_tx(bar, bytes); }
-// One arrival plus the expected byte count on a slot barrier at a
-// shared::cluster address (this CTA or another), relaxed: it orders nothing,
-// it only opens the phase that the following st.async bytes complete.
-__device__ inline void mbar_arm_remote(unsigned bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.relaxed.cluster.shared::cluster.b64 _, [%0], %1;" ::"r"(bar),
-               "r"(bytes)
-               : "memory");
-}
 __device__ inline bool mbar_try_wait_cluster(uint64_t* bar, unsigned parity) {
   unsigned ok;
   asm volatile(
@@ -449,7 +444,6 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
           }
         }
       }
-      if (lane == 0) mbar_arm_remote(dst.rbar + (unsigned)(rs * sizeof(uint64_t)), ringb);
     }
     // this step's inputs from the block's TMA slot
     const int rib = BWD ? (n_blk - 1 - u) : u;
@@ -471,6 +465,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
       }
       rparity ^= 1u << rs;
       lds_ring<T, C>(ring_in + (size_t)(rs * 32 + lane) * CP, cz);
+      if (lane == 0) mbar_arm(&rbar_in[rs], ringb);  // the slot's next use
     }
     T cx = BWD ? __shfl_down_sync(0xffffffffu, edge, 1) : __shfl_up_sync(0xffffffffu, edge, 1);
     if (BWD ? (lane == 31) : (lane == 0)) cx = T(0);
@@ -580,6 +575,9 @@ __device__ __forceinline__ void mic_wave_cl_body(const WaveArgs<T>& a) {
   if (lane == 0 && warp < BZ) {
     for (int k = 0; k < a.pf; k++) mbar_init(&sm.bar[warp * a.pf + k], 1);
     for (int k = 0; k < kWaveD; k++) mbar_init(&sm.rbar[warp * kWaveD + k], 1);
+    // every ring slot armed for its first use (the consumer re-arms after each)
+    for (int k = 0; k < kWaveD; k++)
+      mbar_arm(&sm.rbar[warp * kWaveD + k], 32u * ring_cp(C, sizeof(T)) * sizeof(T));
   }
   if (threadIdx.x == 0) {
     sm.misc[1] = 0;
@@ -634,6 +632,9 @@ __global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
   if (lane == 0 && warp < BZ) {
     for (int k = 0; k < a.pf; k++) mbar_init(&sm.bar[warp * a.pf + k], 1);
     for (int k = 0; k < kWaveD; k++) mbar_init(&sm.rbar[warp * kWaveD + k], 1);
+    // every ring slot armed for its first use (the consumer re-arms after each)
+    for (int k = 0; k < kWaveD; k++)
+      mbar_arm(&sm.rbar[warp * kWaveD + k], 32u * ring_cp(C, sizeof(T)) * sizeof(T));
   }
   if (threadIdx.x == 0) sm.misc[1] = 0;
   fence_mbar_init();
@@ -700,7 +701,6 @@ __global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
 #pragma unroll
               for (int j = 0; j < C; j++) v[j] = BWD ? o[i][j] : pv[i][j] * o[i][j];
               constexpr int CP = ring_cp(C, sizeof(T));
-              if (lane == 0) mbar_arm_remote(rbar0 + (unsigned)(rs * sizeof(uint64_t)), 32u * CP * sizeof(T));
               st_async_ring<T, C>(ring0 + (unsigned)((size_t)(rs * 32 + lane) * CP * sizeof(T)), v,
                                   rbar0 + (unsigned)(rs * sizeof(uint64_t)));
             }
