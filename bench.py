@@ -490,6 +490,65 @@ def measure_batched(steps, warmup, seed=0, n=64):
                         "plumes, each step one CUDA graph launch" % n}
 
 
+def measure_with_output(local, rank, cfg1_steps=20, big_steps=2):
+    """The step with its output on: the state file (writeGz layout, gzip level
+    1, deflated in parallel on the host) and the six stream rows written each
+    step by the handle's asynchronous writer, as fluid3D writes them
+    (fluid3D.cpp:357-398).  Two workloads: config 1 (48x64x48 FP64, rel-L2
+    1e-10, output every step) and the 128x192x128 FP32 plume.  Wall-clock
+    steps/s with and without the output, the bytes written per step; the files
+    go to a temporary directory that is removed afterwards."""
+    import shutil
+    from cfs_plume_gb300 import _abi
+    from cfs_plume_gb300.plume import Plume
+    out = {}
+    for name, res, prec, tol, steps in (
+            ("config1_48x64x48_fp64", (48, 64, 48), _abi.PREC_FP64, 1e-10, cfg1_steps),
+            ("plume_128x192x128_fp32", RES, _abi.PREC_FP32, 1e-6, big_steps)):
+        rec = {}
+        for with_out in (False, True):
+            d = tempfile.mkdtemp(prefix="plume_out_")
+            g = None
+            try:
+                g = Plume(_abi.plume_config(res, precision=prec, tol=tol, seed=rank, device=local))
+                warm = 2
+                for s in range(warm):
+                    g.add_source(s)
+                    g.step()
+                    if with_out:
+                        g.snapshot_async(d, s)
+                if with_out:
+                    g.wait_snapshots()
+                g.sync()
+                before = sum(os.path.getsize(os.path.join(d, f)) for f in os.listdir(d))
+                t0 = time.time()
+                for s in range(warm, warm + steps):
+                    g.add_source(s)
+                    g.step()
+                    if with_out:
+                        g.snapshot_async(d, s)
+                if with_out:
+                    g.wait_snapshots()
+                g.sync()
+                secs = time.time() - t0
+                written = sum(os.path.getsize(os.path.join(d, f)) for f in os.listdir(d)) - before
+                key = "with_output" if with_out else "no_output"
+                rec[key] = {"steps_per_s": steps / secs, "steps": steps}
+                if with_out:
+                    rec[key]["bytes_written_per_step"] = written / steps
+            except Exception as e:  # a full disk on the host must not end the bench line
+                rec["with_output" if with_out else "no_output"] = {"error": str(e)[:200]}
+            finally:
+                if g is not None:
+                    g.close()
+                shutil.rmtree(d, ignore_errors=True)
+        rec["workload"] = ("%dx%dx%d %s, rel-L2 %.0e, closed box, box source; the state file and the "
+                           "stream rows each step through plume_snapshot_async, wall clock incl. the "
+                           "last write" % (res + ("FP64" if prec == _abi.PREC_FP64 else "FP32", tol)))
+        out[name] = rec
+    return out
+
+
 LARGE_RES = (256, 384, 256)
 
 
@@ -631,6 +690,8 @@ def main():
     ap.add_argument("--no-reduced", action="store_true", help="skip the reduced-step measurement")
     ap.add_argument("--large-steps", type=int, default=5,
                     help="timed steps of the 256x384x256 plume, plain and learned (0: skip)")
+    ap.add_argument("--no-output", action="store_true",
+                    help="skip the measurement of the step with its state file and streams written")
     ap.add_argument("--batch-steps", type=int, default=10,
                     help="timed steps of the 64-plume batched configuration (0: skip)")
     ap.add_argument("--net-forward", default=None, metavar="X,Y,Z",
@@ -699,6 +760,7 @@ def main():
     red = None if a.no_reduced else measure_reduced(a.steps, local, rank)
     bat = measure_batched(a.batch_steps, 3, seed=rank) if a.batch_steps > 0 else None
     big = measure_large(a.large_steps, 3, weights, local, rank) if a.large_steps > 0 else None
+    wout = None if a.no_output else measure_with_output(local, rank)
     clk = clocks.stop()
     head = lrn if lrn is not None else plain
     ms_max, value, iters = head["ms"], head["value"], head["iters"]
@@ -776,6 +838,7 @@ def main():
         "reduced_products": products_record(red, 2 * 2 * 152 * 2.070e9 / 1e12) if red else None,
         "batched": bat,
         "large_plume": big,
+        "with_output": wout,
         "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": nbox * 8,
                 "d2h_bytes_per_step": 3 * N * 8},
         "clocks": clk,

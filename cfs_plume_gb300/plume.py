@@ -217,6 +217,10 @@ class Plume:
     def wait_snapshots(self):
         _check(self.lib.plume_wait_snapshots(self.h), self.h)
 
+    def sync(self):
+        """Wait for the handle's stream (plume_sync)."""
+        _check(self.lib.plume_sync(self.h), self.h)
+
     def solve_poisson(self, b, x0=None):
         b = np.ascontiguousarray(b, dtype=np.float64)
         x = np.zeros(self.N) if x0 is None else np.array(x0, dtype=np.float64)
