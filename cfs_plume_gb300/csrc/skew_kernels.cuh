@@ -93,7 +93,9 @@ __global__ void k_from_skew(Grid g, Skew k, const T* sk, T* nat) {
 
 // set-up part 1: r = b - A x, b.b
 template <typename T>
-__device__ __forceinline__ void cgs_init_body(Blk blk_, Grid g, Skew k, const T* b, const T* x, T* r, CgState* st, double* part, double tol, int max_iters, int criterion, int x_zero) {
+__device__ __forceinline__ void cgs_init_body(Blk blk_, Grid g, Skew k, const T* b, const T* x, T* r,
+                                              CgState* st, double* part, double tol, int max_iters,
+                                              int criterion, int x_zero) {
   __shared__ double sh[32];
   DotAcc<T> bb;
   PL_BLK_STRIDE(e, (int)k.total, blk_) {
@@ -141,7 +143,8 @@ __global__ void k_cgs_init(Grid g, Skew k, const T* b, const T* x, T* r, CgState
 
 // set-up part 2: d = z, deltaNew = r.z, loop entry test
 template <typename T>
-__device__ __forceinline__ void cgs_init2_body(Blk blk_, Skew k, const T* r, const T* z, T* d, CgState* st, double* part) {
+__device__ __forceinline__ void cgs_init2_body(Blk blk_, Skew k, const T* r, const T* z, T* d, CgState* st,
+                                               double* part) {
   __shared__ double sh[32];
   DotAcc<T> rz, rr;
   PL_BLK_STRIDE(e, (int)k.total, blk_) {
@@ -651,7 +654,8 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_spmv_dir_v(Grid g, Skew k, 
 
 // Iteration part 2, vectorised: x += alpha d, r -= alpha q, signed max(r), r.r
 template <typename T>
-__device__ __forceinline__ void cgs_axpy_v_body(Blk blk_, Skew k, const T* d, const T* q, T* x, T* r, CgState* st, double* part) {
+__device__ __forceinline__ void cgs_axpy_v_body(Blk blk_, Skew k, const T* d, const T* q, T* x, T* r,
+                                                CgState* st, double* part) {
   if (st->done) return;
   typedef typename Vec16<T>::type V;
   constexpr int NV = Vec16<T>::n;
@@ -705,7 +709,8 @@ __global__ void k_cgs_axpy_v(Skew k, const T* d, const T* q, T* x, T* r, CgState
 
 // Iteration part 3, vectorised: deltaNew = r.z, beta, exit tests
 template <typename T>
-__device__ __forceinline__ void cgs_rz_v_body(Blk blk_, Skew k, const T* r, const T* z, CgState* st, double* part) {
+__device__ __forceinline__ void cgs_rz_v_body(Blk blk_, Skew k, const T* r, const T* z, CgState* st,
+                                              double* part) {
   if (st->done) return;
   typedef typename Vec16<T>::type V;
   constexpr int NV = Vec16<T>::n;

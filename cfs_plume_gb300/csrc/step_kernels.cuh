@@ -42,7 +42,9 @@ struct StepConsts {
 // ---------------------------------------------------------------- sources
 // Box source: density = heat = 1 + noise*(2u-1) on [lo, hi).
 template <typename T>
-__device__ __forceinline__ void source_box_body(Blk blk_, T* dens, T* heat, Grid g, int x0, int y0, int z0, int bx, int by, int bz, uint64_t seed, int step, double noise) {
+__device__ __forceinline__ void source_box_body(Blk blk_, T* dens, T* heat, Grid g, int x0, int y0, int z0,
+                                                int bx, int by, int bz, uint64_t seed, int step,
+                                                double noise) {
   const int n = bx * by * bz;
   PL_BLK_STRIDE(i, n, blk_) {
     const int x = x0 + i % bx;
@@ -93,7 +95,8 @@ __global__ void k_source_list(T* dens, T* heat, const int* cells, int n) {
 // setZeroBorder, addBuoyancy (force.y = beta*heat), velocity += force*dt,
 // prevorticity = velocity.
 template <typename T>
-__device__ __forceinline__ void forces_body(Blk blk_, Grid g, V3<T> vel, T* dens, const T* heat, V3<T> prevort, StepConsts<T> c, int cache) {
+__device__ __forceinline__ void forces_body(Blk blk_, Grid g, V3<T> vel, T* dens, const T* heat,
+                                            V3<T> prevort, StepConsts<T> c, int cache) {
   PL_BLK_STRIDE(i, g.N, blk_) {
     const int x = i % g.X;
     const int t = i / g.X;
@@ -219,7 +222,9 @@ __device__ inline Trilinear<T> backtrace(const Grid& g, const StepConsts<T>& c, 
 // its interior neighbour's new value, which the border thread recomputes.
 // postadvection (the pre-fix-up velocity) is written when `cache` is set.
 template <typename T>
-__device__ __forceinline__ void advect_body(Blk blk_, Grid g, StepConsts<T> c, V3<T> vo, const T* dens_o, const T* heat_o, V3<T> vn, T* dens_n, T* heat_n, V3<T> postadv, int cache, int open_x, int open_y, int open_z, int vel_out) {
+__device__ __forceinline__ void advect_body(Blk blk_, Grid g, StepConsts<T> c, V3<T> vo, const T* dens_o,
+                                            const T* heat_o, V3<T> vn, T* dens_n, T* heat_n, V3<T> postadv,
+                                            int cache, int open_x, int open_y, int open_z, int vel_out) {
   PL_BLK_STRIDE(i, g.N, blk_) {
     const int x = i % g.X;
     const int t = i / g.X;
