@@ -170,6 +170,17 @@ __device__ __forceinline__ void vort2_tile_body(Blk blk_, Grid g, V3<T> vel, V3<
     for (int z = z0; z < z1; z++) {
       m.ahead(mag, g, col, in, z);
       const int i = col + z * g.slab;
+      // the cell's own w and velocity, loaded before the barriers so that
+      // their latency overlaps the tile exchange
+      T wx = T(0), wy = T(0), wz = T(0), ux = T(0), uy = T(0), uz = T(0);
+      if (in) {
+        wx = w.x[i];
+        wy = w.y[i];
+        wz = w.z[i];
+        ux = vel.x[i];
+        uy = vel.y[i];
+        uz = vel.z[i];
+      }
       __syncthreads();
       tile_fill(sm, mag + z * g.slab, g, x, y, tx, ty, m.c, true, true);
       __syncthreads();
@@ -194,7 +205,6 @@ __device__ __forceinline__ void vort2_tile_body(Blk blk_, Grid g, V3<T> vel, V3<
             N0 *= mm;
             N1 *= mm;
             N2 *= mm;
-            const T wx = w.x[i], wy = w.y[i], wz = w.z[i];
             fx = (N1 * wz - N2 * wy) * c.dx * c.eps;
             fy = -((N0 * wz - N2 * wx) * c.dx * c.eps);
             fz = (N0 * wy - N1 * wx) * c.dx * c.eps;
@@ -202,9 +212,9 @@ __device__ __forceinline__ void vort2_tile_body(Blk blk_, Grid g, V3<T> vel, V3<
           }
         }
         if (has_f) {
-          vel.x[i] = vel.x[i] + fx * c.dt;
-          vel.y[i] = vel.y[i] + fy * c.dt;
-          vel.z[i] = vel.z[i] + fz * c.dt;
+          vel.x[i] = ux + fx * c.dt;
+          vel.y[i] = uy + fy * c.dt;
+          vel.z[i] = uz + fz * c.dt;
         }
         if (cache) {
           force.x[i] = fx;
@@ -324,11 +334,19 @@ __device__ __forceinline__ void gradient_tile_body(Blk blk_, Grid g, StepConsts<
     pc.start(p, g, col, in, z0);
     for (int z = z0; z < z1; z++) {
       pc.ahead(p, g, col, in, z);
+      const int i = col + z * g.slab;
+      const bool inner = in && !on_border(g, x, y, z);
+      // the velocity being corrected, loaded before the barriers
+      T ux = T(0), uy = T(0), uz = T(0);
+      if (inner) {
+        ux = v.x[i];
+        uy = v.y[i];
+        uz = v.z[i];
+      }
       __syncthreads();
       tile_fill(sp, p + z * g.slab, g, x, y, tx, ty, pc.c, true, true);
       __syncthreads();
-      if (in && !on_border(g, x, y, z)) {
-        const int i = col + z * g.slab;
+      if (inner) {
         const T inv = c.oneOverDx;
         const T pxp = sp.v[ty + 1][tx + 2], pxm = sp.v[ty + 1][tx];
         const T pyp = sp.v[ty + 2][tx + 1], pym = sp.v[ty][tx + 1];
@@ -351,9 +369,9 @@ __device__ __forceinline__ void gradient_tile_body(Blk blk_, Grid g, StepConsts<
           gz = (pc.c - pc.m) * inv;
         else
           gz = T(0.5) * (pc.p - pc.m) * inv;
-        v.x[i] = v.x[i] - gx;
-        v.y[i] = v.y[i] - gy;
-        v.z[i] = v.z[i] - gz;
+        v.x[i] = ux - gx;
+        v.y[i] = uy - gy;
+        v.z[i] = uz - gz;
       }
       pc.shift();
     }
