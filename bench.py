@@ -462,8 +462,11 @@ def measure_batched(steps, warmup, seed=0, n=64):
         secs, stats = b.run(warmup, steps, stats=True)
         tuning = b.tuning() if engine != "streams" else None
         b.close()
+        # the canonical bytes model per plume and step (FP32 fields, each plume's own iterations)
+        model_bytes = sum(bytes_per_step(cells[i], st.iterations, 4, 4) for i in range(n) for st in stats[i])
         arm = {"value": cells.sum() * steps / secs, "seconds": secs, "create_seconds": create_s,
                "instance_steps_per_s": n * steps / secs,
+               "achieved_gbs": model_bytes / secs / 1e9,
                "pcg_iters_per_step_mean": float(np.mean([[s.iterations for s in st] for st in stats])),
                "pcg_iters_per_step_max": int(np.max([[s.iterations for s in st] for st in stats])),
                "all_converged": all(s.converged for st in stats for s in st)}
@@ -479,8 +482,11 @@ def measure_batched(steps, warmup, seed=0, n=64):
         k = "x".join(str(v) for v in p.res)
         grids[k] = grids.get(k, 0) + 1
     f = arms["fused"]
+    peak, peak_kind = measured_peaks()
     return {"value": f["value"], "unit": "interior cell-steps/s", "engine": "fused", "instances": n,
             "steps": steps, "warmup": warmup, "seconds": f["seconds"],
+            "achieved_gbs": f["achieved_gbs"], "hbm_frac": f["achieved_gbs"] / peak, "peak_gbs": peak,
+            "bytes_model": "per plume and step N_int*(51S+3P+6 + iters*(16S+2P+3)), S = P = 4",
             "instance_steps_per_s": f["instance_steps_per_s"],
             "pcg_iters_per_step_mean": f["pcg_iters_per_step_mean"], "all_converged": f["all_converged"],
             "fused_over_streams": f["value"] / arms["streams"]["value"], "arms": arms, "grids": grids,
