@@ -817,7 +817,8 @@ class BatchEngineT : public BatchEngine {
   }
 
   // Every plume's MIC(0) diagonal, built in FP64 once (the walls never
-  // change), rounded to T and stored skewed.
+  // change) and stored skewed: P for the FP64 sweeps, P^2 rounded once for the
+  // FP32 sweeps (k_diag_to_skew).
   int build_diagonals() {
     int maxN = 0;
     for (const Host& h : hp_) maxN = std::max(maxN, h.g.N);
@@ -834,14 +835,10 @@ class BatchEngineT : public BatchEngine {
       e = cudaMemsetAsync(P64, 0, (size_t)h.g.N * sizeof(double), s_);
       if (e == cudaSuccess) e = build_mic_diagonal(h.g, P64, h.p.mic_tau, h.p.mic_sigma, s_);
       if (e == cudaSuccess) {
-        k_convert_precon<T><<<grid_for(h.g.N), 256, 0, s_>>>(h.g.N, P64, p.tmp.x);
+        k_diag_to_skew<T><<<grid_for(h.k.total), 256, 0, s_>>>(h.g, h.k, P64, p.sP,
+                                                               std::is_same<T, double>::value ? 0 : 1);
         e = cudaGetLastError();
       }
-      if (e == cudaSuccess) {
-        k_to_skew<T, T><<<grid_for(h.k.total), 256, 0, s_>>>(h.g, h.k, p.tmp.x, p.sP);
-        e = cudaGetLastError();
-      }
-      if (e == cudaSuccess) e = cudaMemsetAsync(p.tmp.x, 0, (size_t)h.g.N * sizeof(T), s_);
       if (e != cudaSuccess) rc = fail_cuda(e, "MIC diagonal", __FILE__, __LINE__);
     }
     cudaError_t e2 = cudaStreamSynchronize(s_);

@@ -280,7 +280,7 @@ class EngineT : public Engine {
     // MIC diagonal, the obstacle bytes, solver state and reduction partials.
     const size_t n = (size_t)g_.N;
     const size_t aT = align(n * sizeof(T));
-    const size_t bytes = 37 * aT + align(n * sizeof(double)) + align(n) +
+    const size_t bytes = 36 * aT + align(n * sizeof(double)) + align(n) +
                          align(sizeof(CgState)) + align(8 * kRedBlocks * sizeof(double));
     cudaError_t e = cudaMalloc(&pool_, bytes);
     if (e != cudaSuccess) {
@@ -291,7 +291,7 @@ class EngineT : public Engine {
     char* cur = pool_;
     auto take = [&](size_t b) { char* r = cur; cur += align(b); return r; };
     T** scal[] = {&dens_, &dens_old_, &heat_, &heat_old_, &pres_, &div_, &mag_,
-                  &r_,    &d_,        &q_ad_, &z_,        &qf_, &P_};
+                  &r_,    &d_,        &q_ad_, &z_,        &qf_};
     for (T** s : scal) *s = (T*)take(n * sizeof(T));
     V3<T>* vecs[] = {&vel_, &vel_old_, &spare_, &prevort_, &postadv_, &preproj_, &force_, &vort_};
     for (V3<T>* v : vecs) {
@@ -332,8 +332,6 @@ class EngineT : public Engine {
     // MIC(0) diagonal, built once: the reference rebuilds an identical one at
     // every solve (FLUID_3D_MIC.cpp:921-922) since the walls never change.
     PL_TRY(build_mic_diagonal(g_, P64_, p.mic_tau, p.mic_sigma, s_));
-    k_convert_precon<T><<<grid_for(g_.N), 256, 0, s_>>>(g_.N, P64_, P_);
-    PL_CHECK_LAUNCH();
     int rc = init_solver();
     if (rc != PLUME_OK) return rc;
     PL_TRY(cudaStreamSynchronize(s_));
@@ -784,6 +782,10 @@ class EngineT : public Engine {
     PL_CHECK_LAUNCH();
     k_from_skew<T><<<gK, 256, 0, s_>>>(g_, k_, sqf_, qf_);
     PL_CHECK_LAUNCH();
+    if (!std::is_same<T, double>::value) {  // the FP32 forward sweep writes P q
+      k_fwd_unscale<T><<<grid_for(g_.N), 256, 0, s_>>>(g_.N, P64_, qf_);
+      PL_CHECK_LAUNCH();
+    }
     PL_TRY(cudaMemcpyAsync(st_host_, st_, sizeof(CgState), cudaMemcpyDeviceToHost, s_));
     PL_TRY(cudaStreamSynchronize(s_));
     if (prof_on_) {
@@ -898,7 +900,7 @@ class EngineT : public Engine {
     wave_ctl_ = (unsigned*)cur;
     cur += align(4 * sizeof(unsigned));
     wave_prog_ = (int*)cur;
-    k_to_skew<T, T><<<grid_for(k_.total), 256, 0, s_>>>(g_, k_, P_, sP_);
+    k_diag_to_skew<T><<<grid_for(k_.total), 256, 0, s_>>>(g_, k_, P64_, sP_, std::is_same<T, double>::value ? 0 : 1);
     PL_CHECK_LAUNCH();
     // slab height: as many planes per CTA as shared memory allows, up to 8
     int dev = 0;
@@ -1517,7 +1519,7 @@ class EngineT : public Engine {
   char* pool_ = nullptr;
   T *dens_ = nullptr, *dens_old_ = nullptr, *heat_ = nullptr, *heat_old_ = nullptr;
   T *pres_ = nullptr, *div_ = nullptr, *mag_ = nullptr;
-  T *r_ = nullptr, *d_ = nullptr, *q_ad_ = nullptr, *z_ = nullptr, *qf_ = nullptr, *P_ = nullptr;
+  T *r_ = nullptr, *d_ = nullptr, *q_ad_ = nullptr, *z_ = nullptr, *qf_ = nullptr;
   V3<T> vel_{}, vel_old_{}, spare_{}, prevort_{}, postadv_{}, preproj_{}, force_{}, vort_{};
   double* P64_ = nullptr;
   // moving box: inside mask (N), last-column values (3N doubles) and postIOP,

@@ -1,8 +1,8 @@
-// skew_kernels.cuh -- CG vector kernels on the skewed interior layout used by
-// the wavefront MIC sweeps (wave.cuh).  Same arithmetic as the
-// natural-layout kernels in solver_kernels.cuh (FLUID_3D_MIC.cpp:918-1015);
-// threads run over the stored elements row by row, so loads and stores are
-// contiguous; padding elements are kept at zero.
+// skew_kernels.cuh -- the PCG loop of FLUID_3D_MIC::solvePoisson
+// (FLUID_3D_MIC.cpp:918-1015) as vector kernels on the skewed interior layout
+// of the wavefront MIC sweeps (wave.cuh); threads run over the stored
+// elements row by row, so loads and stores are contiguous; padding elements
+// are kept at zero.
 #pragma once
 #include <type_traits>
 #include "solver_kernels.cuh"
@@ -76,6 +76,30 @@ __device__ __forceinline__ void to_skew_body(Blk blk_, Grid g, Skew k, const S* 
 template <typename S, typename T>
 __global__ void k_to_skew(Grid g, Skew k, const S* nat, T* sk) {
   to_skew_body<S, T>(hw_blk(), g, k, nat, sk);
+}
+
+// The MIC(0) diagonal in the sweeps' skewed layout.  The exact (FP64) sweeps
+// take P itself; the FP32 sweeps only ever multiply by P^2 (see sweep_cell),
+// so for them the square is formed in FP64 and rounded once.
+template <typename T>
+__global__ void k_diag_to_skew(Grid g, Skew k, const double* P64, T* sk, int square) {
+  const Blk b = hw_blk();
+  PL_BLK_STRIDE(e, (int)k.total, b) {
+    int ix, iy, iz;
+    double v = 0.0;
+    if (skew_cell(k, e, ix, iy, iz)) v = P64[(ix + 1) + (iy + 1) * g.X + (iz + 1) * g.slab];
+    sk[e] = (T)(square ? v * v : v);
+  }
+}
+
+// The FP32 forward sweep hands back w = P q (natural layout, in place); q
+// itself is w / P, and zero where P is (those cells compute zero).
+template <typename T>
+__global__ void k_fwd_unscale(int n, const double* P64, T* w) {
+  PL_GRID_STRIDE(i, n) {
+    const double p = P64[i];
+    w[i] = p != 0.0 ? (T)((double)w[i] / p) : T(0);
+  }
 }
 
 // skewed interior -> natural full grid (interior cells only)
@@ -182,110 +206,6 @@ __device__ __forceinline__ void cgs_init2_body(Blk blk_, Skew k, const T* r, con
 template <typename T>
 __global__ void k_cgs_init2(Skew k, const T* r, const T* z, T* d, CgState* st, double* part) {
   cgs_init2_body<T>(hw_blk(), k, r, z, d, st, part);
-}
-
-// iteration part 1: q = A d, alpha = deltaNew / d.q
-template <typename T>
-__global__ void k_cgs_spmv(Grid g, Skew k, const T* d, T* q, CgState* st, double* part) {
-  if (st->done) return;
-  __shared__ double sh[32];
-  DotAcc<T> dq;
-  PL_GRID_STRIDE(e, (int)k.total) {
-    int ix, iy, iz;
-    T v = T(0);
-    if (skew_cell(k, e, ix, iy, iz)) {
-      v = mult_a_skew(g, k, d, e, ix, iy, iz);
-      dq.prod(d[e], v);
-    }
-    q[e] = v;
-  }
-  const double s = dq.block(sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
-  if (arrive_last(&st->ticket[0])) {
-    const double t = sum_partials(part, sh);
-    if (threadIdx.x == 0) {
-      st->dq = t;
-      if (fabs(t) > 0.0) {
-        st->alpha = st->deltaNew / t;
-      } else {
-        st->done = 1;
-        st->broke = 1;
-      }
-      st->ticket[0] = 0;
-    }
-  }
-}
-
-// iteration part 2: x += alpha d, r -= alpha q, signed max(r), r.r
-template <typename T>
-__global__ void k_cgs_axpy(Skew k, const T* d, const T* q, T* x, T* r, CgState* st, double* part) {
-  if (st->done) return;
-  __shared__ double sh[32];
-  const T alpha = (T)st->alpha;
-  T mx = T(-3.0e38);
-  DotAcc<T> rr;
-  PL_GRID_STRIDE(e, (int)k.total) {
-    x[e] += alpha * d[e];
-    const T ri = r[e] + (-alpha) * q[e];
-    r[e] = ri;
-    mx = (ri > mx) ? ri : mx;
-    rr.prod(ri, ri);
-  }
-  const double s1 = block_max_w(mx, sh, -1.0e308);
-  if (threadIdx.x == 0) part[blockIdx.x] = s1;
-  const double s2 = rr.block(sh);
-  if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
-  if (arrive_last(&st->ticket[0])) {
-    const double tm = max_partials(part, sh);
-    const double trr = sum_partials(part + kRedBlocks, sh);
-    if (threadIdx.x == 0) {
-      st->oldMaxR = st->maxR;
-      st->maxR = tm > 0.0 ? tm : 0.0;
-      st->rr = trr;
-      if (st->criterion == 1 && sqrt(trr) <= st->tol * sqrt(st->bb)) {
-        st->iter += 1;
-        st->done = 1;
-        st->converged = 1;
-      }
-      st->ticket[0] = 0;
-    }
-  }
-}
-
-// iteration part 3: deltaNew = r.z, beta, exit tests
-template <typename T>
-__global__ void k_cgs_rz(Skew k, const T* r, const T* z, CgState* st, double* part) {
-  if (st->done) return;
-  __shared__ double sh[32];
-  DotAcc<T> rz;
-  PL_GRID_STRIDE(e, (int)k.total) rz.prod(r[e], z[e]);
-  const double s = rz.block(sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
-  if (arrive_last(&st->ticket[0])) {
-    const double t = sum_partials(part, sh);
-    if (threadIdx.x == 0) {
-      st->deltaOld = st->deltaNew;
-      st->deltaNew = t;
-      st->beta = t / st->deltaOld;
-      st->iter += 1;
-      if (st->wave_err) st->done = 3;
-      if (st->criterion == 0) {
-        const double relative = fabs((st->maxR - st->oldMaxR) / st->oldMaxR);
-        if (relative < 1e-7) st->done = st->done ? st->done : 2;
-        if (!(st->maxR > st->tol)) st->converged = 1;
-      }
-      if (st->converged || st->iter >= st->max_iters) st->done = st->done ? st->done : 1;
-      st->ticket[0] = 0;
-    }
-  }
-}
-
-// iteration part 4: d = d*beta + z
-template <typename T>
-__global__ void k_cgs_dir(Skew k, const T* z, T* d, const CgState* st) {
-  if (st->done) return;
-  const T beta = (T)st->beta;
-  PL_GRID_STRIDE(e, (int)k.total) d[e] = d[e] * beta + z[e];
 }
 
 // ----------------------------------------------------- fused fast path
@@ -653,6 +573,7 @@ __global__ void __launch_bounds__(kRedThreads) k_cgs_spmv_dir_v(Grid g, Skew k, 
 }
 
 // Iteration part 2, vectorised: x += alpha d, r -= alpha q, signed max(r), r.r
+// (the PCG loop of FLUID_3D_MIC::solvePoisson, FLUID_3D_MIC.cpp:951-1013)
 template <typename T>
 __device__ __forceinline__ void cgs_axpy_v_body(Blk blk_, Skew k, const T* d, const T* q, T* x, T* r,
                                                 CgState* st, double* part) {

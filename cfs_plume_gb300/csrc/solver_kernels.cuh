@@ -281,234 +281,4 @@ __global__ void k_mic_precon_plane(Grid g, double* P64, int s, double tau, doubl
 // Builds the FP64 MIC diagonal into P64 (hyperplane launches on `s`).
 cudaError_t build_mic_diagonal(const Grid& g, double* P64, double tau, double sig, cudaStream_t s);
 
-template <typename T>
-__global__ void k_convert_precon(int n, const double* P64, T* P) {
-  PL_GRID_STRIDE(i, n) P[i] = (T)P64[i];
-}
-
-// ---------------------------------------------- MIC sweeps, one hyperplane
-// applyMICPreconditioner (FLUID_3D_MIC.cpp:870-898), each cell evaluated with
-// the reference's expression, so the result is bit-identical to the serial
-// sweep in FP64.  One launch per hyperplane; used at set-up and as the
-// reference path the wavefront kernels are tested against.
-template <typename T>
-__global__ void k_mic_fwd_plane(Grid g, const T* P, const T* r, T* q, int s,
-                                const CgState* st) {
-  if (st && st->done) return;
-  PL_GRID_STRIDE(k, g.ny * g.nz) {
-    const int j = k % g.ny, l = k / g.ny;
-    const int ix = s - j - l;
-    if (ix < 0 || ix >= g.nx) continue;
-    const int x = ix + 1, y = j + 1, z = l + 1;
-    const int i = x + y * g.X + z * g.slab;
-    const int xm = i - 1, ym = i - g.X, zm = i - g.slab;
-    const T t = r[i] - coef<T>(wall_xm(g, x)) * P[xm] * q[xm] -
-                coef<T>(wall_ym(g, y)) * P[ym] * q[ym] - coef<T>(wall_zm(g, z)) * P[zm] * q[zm];
-    q[i] = t * P[i];
-  }
-}
-
-template <typename T>
-__global__ void k_mic_bwd_plane(Grid g, const T* P, const T* q, T* zf, int s,
-                                const CgState* st) {
-  if (st && st->done) return;
-  PL_GRID_STRIDE(k, g.ny * g.nz) {
-    const int j = k % g.ny, l = k / g.ny;
-    const int ix = s - j - l;
-    if (ix < 0 || ix >= g.nx) continue;
-    const int x = ix + 1, y = j + 1, z = l + 1;
-    const int i = x + y * g.X + z * g.slab;
-    const T p = P[i];
-    const T t = q[i] - coef<T>(wall_xp(g, x)) * p * zf[i + 1] -
-                coef<T>(wall_yp(g, y)) * p * zf[i + g.X] -
-                coef<T>(wall_zp(g, z)) * p * zf[i + g.slab];
-    zf[i] = t * p;
-  }
-}
-
-// ------------------------------------------------------------ CG kernels
-// Solve set-up part 1 (lines 921-933): r = b - A x on the interior and b.b.
-template <typename T>
-__global__ void k_cg_init(Grid g, const T* b, const T* x, T* r, CgState* st, double* part,
-                          double tol, int max_iters, int criterion) {
-  __shared__ double sh[32];
-  double bb = 0.0;
-  PL_GRID_STRIDE(k, g.nint) {
-    int cx, cy, cz;
-    const int i = interior_cell(g, k, cx, cy, cz);
-    const T ax = mult_a_cell(g, x, i, cx, cy, cz);
-    r[i] = b[i] - ax;
-    bb += (double)b[i] * (double)b[i];
-  }
-  const double s = block_sum(bb, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
-  if (arrive_last(&st->ticket[0])) {
-    const double tot = sum_partials(part, sh);
-    if (threadIdx.x == 0) {
-      st->bb = tot;
-      st->tol = tol;
-      st->max_iters = max_iters;
-      st->criterion = criterion;
-      st->iter = 0;
-      st->done = 0;
-      st->converged = 0;
-      st->broke = 0;
-      st->ticket[0] = 0;
-    }
-  }
-}
-
-// Solve set-up part 2 (lines 935-944): d = z, deltaNew = r.z, and the entry
-// test of the loop.
-template <typename T>
-__global__ void k_cg_init2(Grid g, const T* r, const T* z, T* d, CgState* st, double* part) {
-  __shared__ double sh[32];
-  double rz = 0.0, rr = 0.0;
-  PL_GRID_STRIDE(k, g.nint) {
-    int cx, cy, cz;
-    const int i = interior_cell(g, k, cx, cy, cz);
-    const T zi = z[i], ri = r[i];
-    d[i] = zi;
-    rz += (double)ri * (double)zi;
-    rr += (double)ri * (double)ri;
-  }
-  const double s1 = block_sum(rz, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s1;
-  const double s2 = block_sum(rr, sh);
-  if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
-  if (arrive_last(&st->ticket[0])) {
-    const double trz = sum_partials(part, sh);
-    const double trr = sum_partials(part + kRedBlocks, sh);
-    if (threadIdx.x == 0) {
-      st->deltaNew = trz;
-      st->rr = trr;
-      if (st->criterion == 0) {
-        st->maxR = 2.0 * st->tol;  // FLUID_3D_MIC.cpp:946
-        if (!(st->maxR > st->tol) || st->max_iters <= 0) st->done = 1;
-      } else {
-        if (sqrt(trr) <= st->tol * sqrt(st->bb)) {
-          st->done = 1;
-          st->converged = 1;
-        }
-        if (st->max_iters <= 0) st->done = 1;
-      }
-      st->ticket[0] = 0;
-    }
-  }
-}
-
-// Iteration part 1 (lines 955-969): q = A d, alpha = deltaNew / d.q.
-template <typename T>
-__global__ void k_cg_spmv(Grid g, const T* d, T* q, CgState* st, double* part) {
-  if (st->done) return;
-  __shared__ double sh[32];
-  double dq = 0.0;
-  PL_GRID_STRIDE(k, g.nint) {
-    int cx, cy, cz;
-    const int i = interior_cell(g, k, cx, cy, cz);
-    const T qi = mult_a_cell(g, d, i, cx, cy, cz);
-    q[i] = qi;
-    dq += (double)d[i] * (double)qi;
-  }
-  const double s = block_sum(dq, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
-  if (arrive_last(&st->ticket[0])) {
-    const double t = sum_partials(part, sh);
-    if (threadIdx.x == 0) {
-      st->dq = t;
-      if (fabs(t) > 0.0) {
-        st->alpha = st->deltaNew / t;
-      } else {  // "PCG alpha broke down! Bailing." (lines 962-969)
-        st->done = 1;
-        st->broke = 1;
-      }
-      st->ticket[0] = 0;
-    }
-  }
-}
-
-// Iteration part 2 (lines 972-983): x += alpha d, r -= alpha q, then the
-// signed max of r (border cells hold 0) and r.r.
-template <typename T>
-__global__ void k_cg_axpy(Grid g, const T* d, const T* q, T* x, T* r, CgState* st,
-                          double* part) {
-  if (st->done) return;
-  __shared__ double sh[32];
-  const T alpha = (T)st->alpha;
-  double mx = -1.0e308, rr = 0.0;
-  PL_GRID_STRIDE(k, g.nint) {
-    int cx, cy, cz;
-    const int i = interior_cell(g, k, cx, cy, cz);
-    x[i] += alpha * d[i];
-    const T ri = r[i] + (-alpha) * q[i];
-    r[i] = ri;
-    mx = ((double)ri > mx) ? (double)ri : mx;
-    rr += (double)ri * (double)ri;
-  }
-  const double s1 = block_max(mx, sh, -1.0e308);
-  if (threadIdx.x == 0) part[blockIdx.x] = s1;
-  const double s2 = block_sum(rr, sh);
-  if (threadIdx.x == 0) part[kRedBlocks + blockIdx.x] = s2;
-  if (arrive_last(&st->ticket[0])) {
-    const double tm = max_partials(part, sh);
-    const double trr = sum_partials(part + kRedBlocks, sh);
-    if (threadIdx.x == 0) {
-      st->oldMaxR = st->maxR;
-      st->maxR = tm > 0.0 ? tm : 0.0;  // FIELD_3D::max starts at a border cell (0)
-      st->rr = trr;
-      if (st->criterion == 1 && sqrt(trr) <= st->tol * sqrt(st->bb)) {
-        st->iter += 1;
-        st->done = 1;
-        st->converged = 1;
-      }
-      st->ticket[0] = 0;
-    }
-  }
-}
-
-// Iteration part 3 (lines 985-991): deltaNew = r.z, beta; and the loop's exit
-// tests (lines 951, 1003-1010).
-template <typename T>
-__global__ void k_cg_rz(Grid g, const T* r, const T* z, CgState* st, double* part) {
-  if (st->done) return;
-  __shared__ double sh[32];
-  double rz = 0.0;
-  PL_GRID_STRIDE(k, g.nint) {
-    int cx, cy, cz;
-    const int i = interior_cell(g, k, cx, cy, cz);
-    rz += (double)r[i] * (double)z[i];
-  }
-  const double s = block_sum(rz, sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
-  if (arrive_last(&st->ticket[0])) {
-    const double t = sum_partials(part, sh);
-    if (threadIdx.x == 0) {
-      st->deltaOld = st->deltaNew;
-      st->deltaNew = t;
-      st->beta = t / st->deltaOld;
-      st->iter += 1;
-      if (st->criterion == 0) {
-        const double relative = fabs((st->maxR - st->oldMaxR) / st->oldMaxR);
-        if (relative < 1e-7) st->done = 2;            // stagnation bail
-        if (!(st->maxR > st->tol)) st->converged = 1;  // loop condition
-      }
-      if (st->converged || st->iter >= st->max_iters) st->done = st->done ? st->done : 1;
-      st->ticket[0] = 0;
-    }
-  }
-}
-
-// Iteration part 4 (lines 995-997): d = d*beta + z.  Runs even when the step
-// above ended the loop; the reference updates d before its exit tests too.
-template <typename T>
-__global__ void k_cg_dir(Grid g, const T* z, T* d, const CgState* st, int skip_if_done) {
-  if (skip_if_done && st->done) return;
-  const T beta = (T)st->beta;
-  PL_GRID_STRIDE(k, g.nint) {
-    int cx, cy, cz;
-    const int i = interior_cell(g, k, cx, cy, cz);
-    d[i] = d[i] * beta + z[i];
-  }
-}
-
 }  // namespace plume

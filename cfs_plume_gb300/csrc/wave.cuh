@@ -321,10 +321,15 @@ __device__ inline void lds_ring(const T* src, T (&v)[C]) {
 __device__ inline float madd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ inline double madd(double a, double b, double c) { return __fma_rn(a, b, c); }
 
-// One cell of the sweep.  Forward: t = ((r + wx) + wy) + wz, q = t*P, and the
-// value handed to the +x/+y/+z neighbours is w = P*q, because the reference
-// forms (A+ . P) . q = (-P) . q.  Backward: t = ((q + P zx) + P zy) + P zz,
-// z = t*P; neighbours receive z itself.
+// One cell of the sweep.  With EXACT (FP64) p = P and the reference's
+// expressions: forward t = ((r + wx) + wy) + wz, q = t*P, and the value
+// handed to the +x/+y/+z neighbours is w = P*q, because the reference forms
+// (A+ . P) . q = (-P) . q; backward t = ((q + P zx) + P zy) + P zz, z = t*P,
+// and neighbours receive z itself.  Without EXACT (FP32) p = P^2 (the skewed
+// diagonal holds the square) and the forward sweep writes w = P q in place of
+// q: forward w = P^2 ((r + wy + wz) + wx); backward, from z = P (q + P S) with
+// S = zx + zy + zz, z = w + P^2 S.  Either way one multiply-add per cell lies
+// on the x-chain and P itself is never needed.
 template <typename T, bool EXACT, bool BWD>
 __device__ inline void sweep_cell(T in, T p, T cx, T cy, T cz, T& out, T& pass) {
   if (!BWD) {
@@ -332,19 +337,18 @@ __device__ inline void sweep_cell(T in, T p, T cx, T cy, T cz, T& out, T& pass) 
       const T t = ((in + cx) + cy) + cz;
       out = t * p;
       pass = p * out;
-    } else {  // pass = P^2 (b + cx): one multiply-add on the chain
+    } else {
       const T b = in + cy + cz;
-      const T p2 = p * p;
-      pass = madd(p2, cx, p2 * b);
-      out = p * (b + cx);
+      pass = madd(p, cx, p * b);
+      out = pass;
     }
   } else {
-    T t;
-    if (EXACT)
-      t = ((in + p * cx) + p * cy) + p * cz;
-    else
-      t = (in + p * (cy + cz)) + p * cx;
-    out = t * p;
+    if (EXACT) {
+      const T t = ((in + p * cx) + p * cy) + p * cz;
+      out = t * p;
+    } else {
+      out = madd(p, cx, madd(p, cy + cz, in));
+    }
     pass = out;
   }
 }
@@ -366,8 +370,9 @@ template <typename T, int C, bool EXACT, bool BWD>
 __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int lane, int z,
                             bool no_input, const RingDst dst, bool has_dst, int* failed,
                             unsigned& tparity, unsigned& rparity, int feed_K, bool feed_fence) {
-  const int W = a.k.W, R = a.k.R;
-  const unsigned rowb = (unsigned)(W * sizeof(T));
+  constexpr int W = 32 * C;  // == a.k.W: row offsets below are compile-time constants
+  const int R = a.k.R;
+  constexpr unsigned rowb = (unsigned)(W * sizeof(T));
   constexpr int CP = ring_cp(C, sizeof(T));
   constexpr unsigned ringb = 32u * CP * sizeof(T);  // bytes of one ring row
   const int nblocks = (R + kWaveKB - 1) / kWaveKB;
