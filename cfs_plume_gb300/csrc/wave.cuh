@@ -112,13 +112,6 @@ __device__ inline void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
                "r"(bytes)
                : "memory");
 }
-__device__ inline void tma_row(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
 __device__ inline bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   unsigned ok;
   asm volatile(
@@ -141,6 +134,36 @@ __device__ inline void st_vol(int* p, int v) { *((volatile int*)p) = v; }
 // step sends nothing but the data, and no fence sits on its side either (a
 // step never waits for its own global stores to drain).
 __device__ inline void mbar_arm(uint64_t* bar, unsigned bytes) { mbar_expect_tx(bar, bytes); }
+
+// Single-lane operations of the sweep step as predicated instructions rather
+// than `if (lane == 0)` branches, so the warp never diverges and reconverges
+// inside the step: arm a slot barrier; publish a counter to shared memory;
+// issue one TMA block (arm its barrier with the bytes of both copies, then
+// the two bulk copies).
+__device__ inline void mbar_arm_if(bool pred, uint64_t* bar, unsigned bytes) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %2, 0;\n"
+      " @p mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n}" ::"r"(smem_u32(bar)),
+      "r"(bytes), "r"((int)pred)
+      : "memory");
+}
+__device__ inline void st_shared_if(bool pred, int* dst, int v) {
+  asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %2, 0;\n @p st.volatile.shared.u32 [%0], %1;\n}" ::"r"(
+                   smem_u32(dst)),
+               "r"(v), "r"((int)pred)
+               : "memory");
+}
+__device__ inline void tma_pair_if(bool pred, uint64_t* bar, void* d0, const void* s0, void* d1, const void* s1,
+                                   unsigned bytes) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %0, 0;\n"
+      " @p mbarrier.arrive.expect_tx.shared::cta.b64 _, [%1], %2;\n"
+      " @p cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%3], [%4], %6, [%1];\n"
+      " @p cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%5], [%7], %6, [%1];\n}" ::"r"(
+          (int)pred),
+      "r"(smem_u32(bar)), "r"(2u * bytes), "r"(smem_u32(d0)), "l"(s0), "r"(smem_u32(d1)), "r"(bytes), "l"(s1)
+      : "memory");
+}
 __device__ inline bool mbar_try_wait_cluster(uint64_t* bar, unsigned parity) {
   unsigned ok;
   asm volatile(
@@ -327,8 +350,9 @@ __device__ inline double madd(double a, double b, double c) { return __fma_rn(a,
 // (A+ . P) . q = (-P) . q; backward t = ((q + P zx) + P zy) + P zz, z = t*P,
 // and neighbours receive z itself.  Without EXACT (FP32) p = P^2 (the skewed
 // diagonal holds the square) and the forward sweep writes w = P q in place of
-// q: forward w = P^2 ((r + wy + wz) + wx); backward, from z = P (q + P S) with
-// S = zx + zy + zz, z = w + P^2 S.  Either way one multiply-add per cell lies
+// q: forward w = P^2 (r + wy + wz + wx); backward, from z = P (q + P S) with
+// S = zx + zy + zz, z = w + P^2 S, summed in the order the neighbour values
+// arrive (y from the lane's previous step, z from the ring, x last).  Either way one multiply-add per cell lies
 // on the x-chain and P itself is never needed.
 template <typename T, bool EXACT, bool BWD>
 __device__ inline void sweep_cell(T in, T p, T cx, T cy, T cz, T& out, T& pass) {
@@ -337,9 +361,8 @@ __device__ inline void sweep_cell(T in, T p, T cx, T cy, T cz, T& out, T& pass) 
       const T t = ((in + cx) + cy) + cz;
       out = t * p;
       pass = p * out;
-    } else {
-      const T b = in + cy + cz;
-      pass = madd(p, cx, p * b);
+    } else {  // p (in + cy) does not wait for the ring; cz, then cx, each one multiply-add
+      pass = madd(p, cx, madd(p, cz, p * (in + cy)));
       out = pass;
     }
   } else {
@@ -347,7 +370,7 @@ __device__ inline void sweep_cell(T in, T p, T cx, T cy, T cz, T& out, T& pass) 
       const T t = ((in + p * cx) + p * cy) + p * cz;
       out = t * p;
     } else {
-      out = madd(p, cx, madd(p, cy + cz, in));
+      out = madd(p, cx, madd(p, cz, madd(p, cy, in)));
     }
     pass = out;
   }
@@ -386,26 +409,24 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
   uint64_t* rbar_in = sm.rbar + warp * kWaveD;
   // block j = steps [j*KB, j*KB+KB); its rows are contiguous, so one bulk
   // copy per array per block (rows stored ascending in the slot).
+  // (lane 0 issues; the other lanes pass through the predicated copy)
   auto issue = [&](int j) {
     const int t0 = j * kWaveKB;
     const int n = min(kWaveKB, R - t0);
     const int row0 = BWD ? (R - t0 - n) : t0;
-    uint64_t* bb = &bar[j % PF];
     T* d = tma + (size_t)(j % PF) * 2 * kWaveKB * W;
-    mbar_expect_tx(bb, 2u * (unsigned)n * rowb);
-    tma_row(d, inp + (size_t)row0 * W, (unsigned)n * rowb, bb);
-    tma_row(d + (size_t)kWaveKB * W, Pp + (size_t)row0 * W, (unsigned)n * rowb, bb);
+    tma_pair_if(lane == 0, &bar[j % PF], d, inp + (size_t)row0 * W, d + (size_t)kWaveKB * W,
+                Pp + (size_t)row0 * W, (unsigned)n * rowb);
   };
   int issued = min(PF - 1, nblocks), consumed = 0;
-  if (lane == 0)
-    for (int j = 0; j < issued; j++) issue(j);
+  for (int j = 0; j < issued; j++) issue(j);
   bool ok = true;
   const T* din = tma;
   // make block j current (issue the block PF - 1 ahead, wait for j's
   // copies); false on timeout
   auto enter_block = [&](int j) -> bool {
     if (j + PF - 1 < nblocks) {
-      if (lane == 0) issue(j + PF - 1);
+      issue(j + PF - 1);
       issued = j + PF;
     }
     const int slot = j % PF;
@@ -470,7 +491,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
       }
       rparity ^= 1u << rs;
       lds_ring<T, C>(ring_in + (size_t)(rs * 32 + lane) * CP, cz);
-      if (lane == 0) mbar_arm(&rbar_in[rs], ringb);  // the slot's next use
+      mbar_arm_if(lane == 0, &rbar_in[rs], ringb);  // the slot's next use
     }
     T cx = BWD ? __shfl_down_sync(0xffffffffu, edge, 1) : __shfl_up_sync(0xffffffffu, edge, 1);
     if (BWD ? (lane == 31) : (lane == 0)) cx = T(0);
@@ -508,7 +529,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
     }
     if ((u & 3) == 3 || t + 1 == R) {  // report consumed ring steps (back-pressure)
       __syncwarp();
-      if (lane == 0) st_vol(&sm.prog[warp], t + 1);
+      st_shared_if(lane == 0, &sm.prog[warp], t + 1);
     }
     if (feed_fence && ((t + 1) % feed_K == 0 || t + 1 == R)) {
       // boundary plane of the courier path: rows visible GPU-wide every K
