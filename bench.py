@@ -616,6 +616,40 @@ def net_forward_mode(spec, warmup=3, iters=5):
     return 0
 
 
+SWEEP_SCALING_RES = [(130, 194, 18), (130, 194, 34), (130, 194, 66), (130, 194, 130), (130, 98, 130),
+                     (130, 50, 130), (130, 386, 66)]
+
+
+def sweep_scaling_mode(iters=20):
+    """--sweep-scaling: device time per MIC(0) sweep launch (CUDA events from
+    plume_profile_sweeps around plume_mic_apply) on FP32 handles whose
+    interior is 128 cells wide (4 cells per lane), varying the rows per plane
+    (interior ny + 31) and the plane count (interior nz), then the least-squares
+    fit t = a + b R + c nz: b is the cost of one row step of a warp, c the lag
+    the wavefront adds per plane."""
+    import numpy as np
+    from cfs_plume_gb300 import _abi
+    from cfs_plume_gb300.plume import Plume
+    rows = []
+    for res in SWEEP_SCALING_RES:
+        g = Plume(_abi.default_params(res=res, bc=(1, 1, 1, 1, 1, 1), precision=_abi.PREC_FP32))
+        r = np.random.default_rng(0).standard_normal(g.N)
+        g.mic_apply(r)
+        g.profile_sweeps(True)
+        for _ in range(iters):
+            g.mic_apply(r)
+        ms, n = g.sweep_times()
+        g.profile_sweeps(False)
+        g.close()
+        rows.append({"res": res, "rows": res[1] - 2 + 31, "planes": res[2] - 2, "us_per_sweep": ms / n * 1e3})
+    A = np.array([[1.0, q["rows"], q["planes"]] for q in rows])
+    y = np.array([q["us_per_sweep"] for q in rows])
+    coef = np.linalg.lstsq(A, y, rcond=None)[0]
+    print(json.dumps({"sweeps": rows, "fit_us": {"const": coef[0], "per_row": coef[1], "per_plane": coef[2]},
+                      "fit_max_abs_residual_us": float(np.abs(A @ coef - y).max())}), flush=True)
+    return 0
+
+
 def products_mode(spec, rank=32, warmup=1, iters=1):
     """--products X,Y,Z: the projected-operator build of a reduced model
     (buildOutOfCoreMatrices, plume_reduced_build_products) on seeded
@@ -704,6 +738,8 @@ def main():
                     help="only time the network's forward pass at this grid")
     ap.add_argument("--products", default=None, metavar="X,Y,Z",
                     help="only time the projected-operator build at this grid")
+    ap.add_argument("--sweep-scaling", action="store_true",
+                    help="only time the MIC sweep against rows and planes per plume (and fit)")
     a = ap.parse_args()
     rank, world, local = dist_env()
     if a.impl == "reference":
@@ -712,6 +748,8 @@ def main():
         return net_forward_mode(a.net_forward)
     if a.products:
         return products_mode(a.products)
+    if a.sweep_scaling:
+        return sweep_scaling_mode()
     a.warmup = max(a.warmup, 3)
 
     from cfs_plume_gb300 import _abi
