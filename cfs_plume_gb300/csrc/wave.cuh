@@ -688,6 +688,10 @@ __global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
     if (warp == BZ) {
       // fetch courier: upstream boundary plane -> ring 0 (st.async, local)
       if (has_up) {
+        // the value a plane hands on is its output, except in the exact
+        // forward sweep, which writes q and hands on P q (the FP32 forward
+        // sweep writes P q itself; see sweep_cell)
+        constexpr bool kScaleOut = EXACT && !BWD;
         int in_next = 0;
         long long spins = 0;
         const unsigned ring0 = smem_u32(sm.ring), rbar0 = smem_u32(sm.rbar);
@@ -715,7 +719,7 @@ __global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
 #pragma unroll
               for (int j = 0; j < C; j++) {
                 o[i][j] = __ldcg(a.out + base + j);
-                pv[i][j] = BWD ? T(1) : __ldcg(a.P + base + j);
+                pv[i][j] = kScaleOut ? __ldcg(a.P + base + j) : T(1);
               }
             }
           }
@@ -725,7 +729,7 @@ __global__ void __launch_bounds__(32 * 18) k_mic_wave(WaveArgs<T> a) {
               const int rs = (in_next + i) % kWaveD;
               T v[C];
 #pragma unroll
-              for (int j = 0; j < C; j++) v[j] = BWD ? o[i][j] : pv[i][j] * o[i][j];
+              for (int j = 0; j < C; j++) v[j] = kScaleOut ? pv[i][j] * o[i][j] : o[i][j];
               constexpr int CP = ring_cp(C, sizeof(T));
               st_async_ring<T, C>(ring0 + (unsigned)((size_t)(rs * 32 + lane) * CP * sizeof(T)), v,
                                   rbar0 + (unsigned)(rs * sizeof(uint64_t)));

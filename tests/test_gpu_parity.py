@@ -288,16 +288,29 @@ def test_solve_paths_agree_fp64(path, monkeypatch):
     assert rel_l2(xg, xo) < 1e-9
 
 
-def test_wavefront_sweeps_fp32():
-    """FP32 wavefront (reassociated cell sum) against the FP64 serial sweep."""
+@pytest.mark.parametrize("path,bz,grid", [("cluster", None, None), ("courier", "8", None), ("courier", "2", "3")])
+def test_wavefront_sweeps_fp32(path, bz, grid, monkeypatch):
+    """FP32 wavefront (diagonal stored squared, forward intermediate P q,
+    reassociated cell sums) against the FP64 serial sweep, on the cluster path
+    and on the courier path (slabs bridged through global memory, a CTA taking
+    several slabs when the grid is capped): z, and the forward intermediate q
+    that plume_mic_apply hands back."""
+    if path == "courier":
+        monkeypatch.setenv("PLUME_WAVE_NO_CLUSTER", "1")
+        monkeypatch.setenv("PLUME_WAVE_BZ", bz)
+    if grid:
+        monkeypatch.setenv("PLUME_WAVE_GRID", grid)
     p = _abi.default_params(res=(48, 64, 48), bc=(1, 1, 1, 1, 1, 1), precision=_abi.PREC_FP32)
     g = Plume(p)
     rng = np.random.default_rng(6)
     r = np.zeros(g.N)
     r.reshape(p.res[::-1])[1:-1, 1:-1, 1:-1] = rng.standard_normal((46, 62, 46))
-    zo, _ = oracle.mic_apply(p.res, tuple(p.bc), oracle.mic_precon(p.res, tuple(p.bc)), r)
-    z, _ = g.mic_apply(r)
-    assert rel_l2(z, zo) < 1e-5
+    zo, qo = oracle.mic_apply(p.res, tuple(p.bc), oracle.mic_precon(p.res, tuple(p.bc)), r)
+    for _ in range(2):  # a second call reuses the reset tickets and flags
+        z, q = g.mic_apply(r)
+        assert rel_l2(z, zo) < 1e-5
+        assert rel_l2(q, qo) < 1e-5
+    g.close()
 
 
 @pytest.mark.gpu
