@@ -872,7 +872,8 @@ def main():
                              "(host-driven CG loop); value is timed with the CG loop as a CUDA graph"},
         "stage_roofline": dict(stage_roofline(head["stages"], nint, S, peak),
                                note="per stencil stage of the headline arm: mean CUDA-event time, algorithmic "
-                                    "bytes per interior cell x N_int; grid-stride kernels, HBM-bound"),
+                                    "bytes per interior cell x N_int; neighbour stencils as shared-memory "
+                                    "halo tiles, forces and advection grid-stride; HBM-bound"),
         "solve_roofline": {"kernel": "poisson solve (all MIC-PCG kernels)", "achieved": achieved_solve,
                            "unit": "GB/s", "frac": (achieved_solve / peak) if achieved_solve else None,
                            "bytes_model": "N_int*(5S+2P+2 + iters*(16S+2P+3)) per solve"},
