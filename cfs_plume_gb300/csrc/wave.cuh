@@ -27,6 +27,7 @@
 // grid size.  Every wait is bounded; on expiry the kernel records an error
 // word, waits (bounded) for its own copies in flight and returns.
 #pragma once
+#include <type_traits>
 #include "common.cuh"
 #include "solver_kernels.cuh"
 
@@ -452,9 +453,15 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
   // kWaveKB == kWaveD, so the ring slot of step t is u: in a full block,
   // which the caller unrolls, every slot index, row offset and bookkeeping
   // test below is a compile-time constant.
-  auto step = [&](const int t, const int u, const T* blk, const int n_blk) -> bool {
+  // The warp's two roles -- whether it hands its values on (kDst) and whether
+  // it has ring input (kNoIn: the plume's first plane has none) -- are
+  // compile-time constants of the step: the block loop below is instantiated
+  // once per combination, so no step tests them.
+  auto step = [&](auto kDst, auto kNoIn, const int t, const int u, const T* blk, const int n_blk) -> bool {
+    constexpr bool HAS_DST = decltype(kDst)::value;
+    constexpr bool NO_INPUT = decltype(kNoIn)::value;
     const int rs = u;
-    if (has_dst) {
+    if constexpr (HAS_DST) {
       // the consumer may be at most D steps behind.  Its consumed-step
       // counter moves in fours, so the test is made for four steps at a
       // time: before steps t .. t+3 the consumer must have consumed step
@@ -478,7 +485,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
     lds_row<T, C>(blk + (size_t)(kWaveKB + rib) * W + lane * C, vp);
     // ---- critical chain: neighbour value -> cell updates -> hand-off ----
     T cz[C];
-    if (no_input) {
+    if constexpr (NO_INPUT) {
 #pragma unroll
       for (int j = 0; j < C; j++) cz[j] = T(0);
     } else {
@@ -511,7 +518,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
       }
       edge = pass[0];
     }
-    if (has_dst) {
+    if constexpr (HAS_DST) {
       const unsigned off = (unsigned)((size_t)(rs * 32 + lane) * CP * sizeof(T));
       st_async_ring<T, C>(dst.ring + off, pass, dst.rbar + (unsigned)(rs * sizeof(uint64_t)));
     }
@@ -539,29 +546,37 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
     }
     return true;
   };
-  for (int j = 0; j < nblocks && ok; j++) {
-    if (!enter_block(j)) {
-      ok = false;
-      break;
-    }
-    const int t0 = j * kWaveKB;
-    const int n = min(kWaveKB, R - t0);
-    const T* blk = din;
-    if (n == kWaveKB) {
+  auto run_blocks = [&](auto kDst, auto kNoIn) {
+    for (int j = 0; j < nblocks && ok; j++) {
+      if (!enter_block(j)) {
+        ok = false;
+        break;
+      }
+      const int t0 = j * kWaveKB;
+      const int n = min(kWaveKB, R - t0);
+      const T* blk = din;
+      if (n == kWaveKB) {
 #pragma unroll
-      for (int u = 0; u < kWaveKB; u++)
-        if (!step(t0 + u, u, blk, kWaveKB)) {
-          ok = false;
-          break;
-        }
-    } else {
-      for (int u = 0; u < n; u++)
-        if (!step(t0 + u, u, blk, n)) {
-          ok = false;
-          break;
-        }
+        for (int u = 0; u < kWaveKB; u++)
+          if (!step(kDst, kNoIn, t0 + u, u, blk, kWaveKB)) {
+            ok = false;
+            break;
+          }
+      } else {
+        for (int u = 0; u < n; u++)
+          if (!step(kDst, kNoIn, t0 + u, u, blk, n)) {
+            ok = false;
+            break;
+          }
+      }
     }
-  }
+  };
+  using Yes = std::true_type;
+  using No = std::false_type;
+  if (has_dst)
+    no_input ? run_blocks(Yes{}, Yes{}) : run_blocks(Yes{}, No{});
+  else
+    no_input ? run_blocks(No{}, Yes{}) : run_blocks(No{}, No{});
   // every issued TMA block must land before its slot is reused or the CTA exits
   for (int j = consumed; j < issued; j++) {
     const int k = j % PF;
