@@ -465,7 +465,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
       // the consumer may be at most D steps behind.  Its consumed-step
       // counter moves in fours, so the test is made for four steps at a
       // time: before steps t .. t+3 the consumer must have consumed step
-      // t + 3 - D.  Then this step's slot is armed.
+      // t + 3 - D (it re-arms each slot itself once it has read it).
       if ((u & 3) == 0 && next_seen <= t + 3 - kWaveD) {
         long long spins = 0;
         for (;;) {
