@@ -39,8 +39,9 @@ extern "C" {
    258.  The first call on each device looks up that array's device address
    with the device current and keeps it for the life of the process, so make
    the first call on a device before any stream capture, and make no call on
-   a device after cudaDeviceReset on it (the kept address would be stale).  Every call uses the same array and clears the parts that
-   must start at zero; calls whose work overlaps on the GPU (different streams
+   a device after cudaDeviceReset on it (the kept address would be stale).
+   Every call uses the same array and clears the parts that must start at
+   zero; calls whose work overlaps on the GPU (different streams
    or threads, no ordering between them) race on the array and must not be
    issued.  Returns a plume_status for the checks and launches; the work is
    only queued, so the caller orders or synchronizes on `stream` before
