@@ -391,7 +391,7 @@ struct RingDst {
 // ring_in/rbar_in: this warp's input ring (zeros and no waiting when
 // `no_input`).  Returns false after a bounded wait expired.
 template <typename T, int C, bool EXACT, bool BWD>
-__device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int lane, int z,
+__device__ __forceinline__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int lane, int z,
                             bool no_input, const RingDst dst, bool has_dst, int* failed,
                             unsigned& tparity, unsigned& rparity, int feed_K, bool feed_fence) {
   constexpr int W = 32 * C;  // == a.k.W: row offsets below are compile-time constants
@@ -456,10 +456,13 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
   // The warp's two roles -- whether it hands its values on (kDst) and whether
   // it has ring input (kNoIn: the plume's first plane has none) -- are
   // compile-time constants of the step: the block loop below is instantiated
-  // once per combination, so no step tests them.
-  auto step = [&](auto kDst, auto kNoIn, const int t, const int u, const T* blk, const int n_blk) -> bool {
+  // once per combination, so no step tests them.  kTail: the block may hold
+  // the plane's last row (only the last block does).
+  auto step = [&](auto kDst, auto kNoIn, auto kTail, const int t, const int u, const T* blk,
+                  const int n_blk) -> bool {
     constexpr bool HAS_DST = decltype(kDst)::value;
     constexpr bool NO_INPUT = decltype(kNoIn)::value;
+    constexpr bool TAIL = decltype(kTail)::value;
     const int rs = u;
     if constexpr (HAS_DST) {
       // the consumer may be at most D steps behind.  Its consumed-step
@@ -534,7 +537,7 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
 #pragma unroll
       for (int j = 0; j < C; j++) orow[j] = vout[j];
     }
-    if ((u & 3) == 3 || t + 1 == R) {  // report consumed ring steps (back-pressure)
+    if ((u & 3) == 3 || (TAIL && t + 1 == R)) {  // report consumed ring steps (back-pressure)
       __syncwarp();
       st_shared_if(lane == 0, &sm.prog[warp], t + 1);
     }
@@ -546,6 +549,8 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
     }
     return true;
   };
+  using Yes = std::true_type;
+  using No = std::false_type;
   auto run_blocks = [&](auto kDst, auto kNoIn) {
     for (int j = 0; j < nblocks && ok; j++) {
       if (!enter_block(j)) {
@@ -555,24 +560,22 @@ __device__ bool sweep_plane(const WaveArgs<T>& a, WaveSmem<T>& sm, int warp, int
       const int t0 = j * kWaveKB;
       const int n = min(kWaveKB, R - t0);
       const T* blk = din;
-      if (n == kWaveKB) {
+      if (t0 + kWaveKB < R) {  // a full block before the last: unrolled
 #pragma unroll
         for (int u = 0; u < kWaveKB; u++)
-          if (!step(kDst, kNoIn, t0 + u, u, blk, kWaveKB)) {
+          if (!step(kDst, kNoIn, No{}, t0 + u, u, blk, kWaveKB)) {
             ok = false;
             break;
           }
-      } else {
+      } else {  // the last block, full or not
         for (int u = 0; u < n; u++)
-          if (!step(kDst, kNoIn, t0 + u, u, blk, n)) {
+          if (!step(kDst, kNoIn, Yes{}, t0 + u, u, blk, n)) {
             ok = false;
             break;
           }
       }
     }
   };
-  using Yes = std::true_type;
-  using No = std::false_type;
   if (has_dst)
     no_input ? run_blocks(Yes{}, Yes{}) : run_blocks(Yes{}, No{});
   else
