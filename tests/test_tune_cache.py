@@ -71,3 +71,54 @@ def test_tuning_cache_round_trip(tmp_path):
     assert entries["GB300|sm152|fp32|g2|32x32x32*2"] == {"cells_epb": 4, "vec_epb": 2, "spmv_zc": 32,
                                                         "tile_zc": 4, "bz": [6, 5], "pf": [2, 3]}
     assert not [p for p in os.listdir(cache.parent) if ".tmp" in p]  # written whole, then renamed
+
+
+CORRUPT_DRIVER = r'''
+#include <cstdio>
+#include "tune_cache.h"
+using namespace plume;
+int main(int argc, char** argv) {
+  const char* texts[] = {"", "garbage", "{", "{\"sig\"", "{\"sig\": {\"cells_epb\": }}",
+                         "{\"sig\": {\"cells_epb\": 4, \"vec_epb\": 2, \"spmv_zc\": 8, \"tile_zc\": 4, \"bz\": [1,"};
+  for (const char* t : texts) {
+    int usable = 0;
+    for (const auto& e : parse_tune_cache(t)) {
+      int a = 0, b = 0, c = 0, d = 0;
+      std::vector<int> bz, pf;
+      if (json_int(e.second, "cells_epb", a) && json_int(e.second, "vec_epb", b) &&
+          json_int(e.second, "spmv_zc", c) && json_int(e.second, "tile_zc", d) &&
+          json_int_list(e.second, "bz", bz) && json_int_list(e.second, "pf", pf))
+        usable++;
+    }
+    printf("%d\n", usable);
+  }
+  // a corrupt file is replaced by a valid one holding the new entry
+  const std::string path = argv[1];
+  FILE* f = fopen(path.c_str(), "wb");
+  fputs("{\"old\": {\"cells_epb\": 4, \"bz\": [", f);
+  fclose(f);
+  BatchTuning t;
+  t.bz = {3};
+  t.pf = {2};
+  return write_tune_cache(path, "NEW|sig", t) ? 0 : 1;
+}
+'''
+
+
+def test_tuning_cache_tolerates_corrupt_files(tmp_path):
+    """Empty, garbage and truncated cache files yield no usable entry (the
+    engine then re-times the batch), and writing over a corrupt file leaves
+    valid JSON holding the new entry."""
+    src = tmp_path / "corrupt.cpp"
+    src.write_text(CORRUPT_DRIVER)
+    exe = tmp_path / "corrupt"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I", CSRC, str(src), "-o", str(exe)], capture_output=True,
+                       text=True)
+    if r.returncode != 0:
+        pytest.fail(r.stderr)
+    cache = tmp_path / "tune.json"
+    out = subprocess.run([str(exe), str(cache)], capture_output=True, text=True, check=True).stdout.split()
+    assert out == ["0"] * 6
+    with open(cache) as f:
+        entries = json.load(f)
+    assert "NEW|sig" in entries and entries["NEW|sig"]["bz"] == [3]
